@@ -1,0 +1,217 @@
+/*
+ * simgb.h -- C ABI of libsimgb, the GB300 (sm_103a) integration hot path of the
+ * Simbuca ion-cloud simulator: direct-sum Coulomb interaction, per-ion trap field
+ * terms, and the Dormand-Prince 5(4) stage / error-norm / step-control loop.
+ *
+ * Conventions
+ *  - Every entry point returns an int status (SG_OK on success); nothing throws or
+ *    calls exit() across this boundary.  sg_status_string() names a status.
+ *  - Host buffers are owned by the caller.  Device buffers are owned by the
+ *    context and freed by sg_destroy().
+ *  - Host position/velocity buffers use the reference's layout: double[n][3]
+ *    (array of structures, metres and metres/second), as IonCloud::pos/vel
+ *    (bin/ioncloud.h:27-30).  Accelerations come back as double[n][3] in m/s^2,
+ *    like _force_vars::derivs (bin/ode.h:45, bin/force.h:7).
+ *  - One context per host thread; all work of a context is ordered on the
+ *    context's CUDA stream.
+ *
+ * Physical constants are the reference's (bin/globals.h:4-16).
+ */
+#ifndef SIMGB_H
+#define SIMGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+enum {
+    SG_OK = 0,
+    SG_BAD_ARG = 1,          /* invalid argument or size                               */
+    SG_CUDA_ERR = 2,         /* a CUDA runtime call failed (see sg_last_cuda_error)    */
+    SG_H_UNDERFLOW = 3,      /* step size underflow; the reference throws
+                                "stepsize underflow created" (bin/ode.cpp:482-483)     */
+    SG_NONFINITE = 4,        /* non-finite error norm or state                         */
+    SG_TIMEOUT = 5,          /* a bounded device-side wait ran out                     */
+    SG_NO_DEVICE = 6,        /* no usable CUDA device                                  */
+    SG_TOO_MANY_REJECTS = 7, /* a step exceeded its reject budget                      */
+    SG_NOT_READY = 8         /* call order violated (e.g. step before upload)          */
+};
+
+/* ---- arithmetic of the Coulomb sum ----------------------------------------- */
+enum {
+    SG_PREC_FP64 = 0,   /* plain form: every operation in FP64                          */
+    SG_PREC_FP32C = 1   /* FP32 pair terms on cloud-centre-relative float-float
+                           coordinates, Kahan-compensated per-ion accumulation across
+                           j-tiles, and FP64 evaluation of close pairs                  */
+};
+
+/* ---- field terms (bit flags of sg_field_params.flags) ---------------------- */
+enum {
+    SG_F_COULOMB  = 1u << 0,  /* ion-ion Coulomb sum (force.cpp:84-177)               */
+    SG_F_PAUL     = 1u << 1,  /* ideal RF+DC quadrupole (force.cpp:70-75)             */
+    SG_F_TOF      = 1u << 2,  /* constant x kick E_kick (force.cpp:77-80)             */
+    SG_F_PENNING  = 1u << 3,  /* ideal Penning trap: quadrupole V0/d0 + B along z     */
+    SG_F_QUAD     = 1u << 4,  /* azimuthal quadrupole RF excitation                   */
+    SG_F_DIPOLE   = 1u << 5,  /* uniform dipole RF excitation along x                 */
+    SG_F_FRICTION = 1u << 6,  /* buffer-gas friction a = -delta v                     */
+    SG_F_FROZEN_T = 1u << 7   /* evaluate every stage at the step-start time, as the
+                                 reference does (force.cpp:36 reads lifetime); without
+                                 it stage s is evaluated at t + c_s h                 */
+};
+
+/* Per-cloud field description.  SI units.  Terms without a flag are ignored.
+ *  Paul (reference _trap_param, bin/trapparameters.h:6-27):
+ *    a_x += q e/m (kappa Vdc/z0^2 - Vrf cos(2 pi freq_rf t)/r0^2) x
+ *    a_y += q e/m (kappa Vdc/z0^2 + Vrf cos(2 pi freq_rf t)/r0^2) y
+ *    a_z += q e/m (-2 kappa Vdc/z0^2) z ;   TOF: a_x += q e/m E_kick
+ *  Penning (no reference implementation; potential V0/(2 d0^2) (z^2 - (x^2+y^2)/2)):
+ *    a += q e/m ( V0/(2 d0^2) x + B v_y,  V0/(2 d0^2) y - B v_x,  -V0/d0^2 z )
+ *  Quadrupole excitation, on for tq_on <= t < tq_off:
+ *    a_x += q e/m (2 Uq/r_el^2) cos(2 pi nu_q t + phi_q) y
+ *    a_y += q e/m (2 Uq/r_el^2) cos(2 pi nu_q t + phi_q) x
+ *  Dipole excitation, on for td_on <= t < td_off:
+ *    a_x += q e/m (Ud/r_el) cos(2 pi nu_d t + phi_d)
+ *  Friction: a -= delta v.
+ *  Coulomb: a_i += coulomb_scale k_e e^2 q_i/m_i sum_{j!=i} q_j (x_i-x_j)/|x_i-x_j|^3.
+ */
+typedef struct sg_field_params {
+    uint32_t flags;
+    uint32_t pad0;
+    double coulomb_scale;
+    /* Paul trap and TOF kick */
+    double Vrf, Vdc, kappa, r0, z0, freq_rf, E_kick;
+    /* Penning trap */
+    double B, V0, d0;
+    /* RF excitations */
+    double r_el;
+    double Uq, nu_q, phi_q, tq_on, tq_off;
+    double Ud, nu_d, phi_d, td_on, td_off;
+    /* buffer gas */
+    double delta;
+} sg_field_params;
+
+/* Dormand-Prince controller settings of one cloud (the reference's _ode_vars
+ * fields rk_rtol, rk_atol, h, EPS; bin/ode.h:66-83, bin/ode.cpp:515-520). */
+typedef struct sg_ode_params {
+    double rtol, atol;   /* reference defaults 1e-7 / 1e-7 (ode.cpp:515-516)           */
+    double h0;           /* first trial step                                            */
+    double t0;           /* cloud lifetime at upload                                    */
+    double t_end;        /* the cloud stops advancing once t >= t_end                    */
+    int32_t adaptive;    /* 1: step-size control on (ode.cpp:478); 0: fixed step h0     */
+    int32_t max_rejects; /* reject budget per step (0 = unlimited)                      */
+} sg_ode_params;
+
+/* State of one cloud after a call. */
+typedef struct sg_step_info {
+    double t;            /* cloud lifetime                                              */
+    double h;            /* step size for the next attempt (the reference's odev.h)     */
+    double h_last;       /* step size of the last accepted step                         */
+    double err;          /* error norm of the last attempt                              */
+    double errold;       /* controller memory (ode.cpp:447)                             */
+    int64_t steps;       /* accepted steps                                              */
+    int64_t rejects;     /* rejected attempts                                           */
+    int64_t force_evals; /* force evaluations (7 per attempt, as the reference counts)  */
+    int64_t coulomb_evals; /* Coulomb sums actually launched                            */
+    int32_t status;      /* SG_OK, SG_H_UNDERFLOW, SG_NONFINITE, SG_TOO_MANY_REJECTS    */
+    int32_t done;        /* 1 once t >= t_end                                           */
+    int32_t reject;      /* controller flag (ode.cpp:443-454)                           */
+    int32_t pad;
+} sg_step_info;
+
+typedef struct sg_ctx sg_ctx;
+
+/* ---- context ----------------------------------------------------------------- */
+int sg_create(int device, sg_ctx** out);
+int sg_destroy(sg_ctx* ctx);
+const char* sg_status_string(int status);
+int sg_last_cuda_error(sg_ctx* ctx);          /* last cudaError_t seen (0 = none)     */
+int sg_sync(sg_ctx* ctx);                     /* wait for the context stream          */
+int sg_version(void);
+
+/* ---- stand-alone force calls (host buffers, synchronous) --------------------- */
+
+/* Coulomb accelerations only: acc[i] = kq[i] * sum_{j!=i} q[j] (x_i-x_j)/|x_i-x_j|^3.
+ * With kq[i] = coulomb_scale k_e e^2 q_i/m_i this is the CPU sum of the reference
+ * (bin/force.cpp:147-174) and the term the GPU backends return (force.cpp:84-105). */
+int sg_coulomb_accel(sg_ctx* ctx, int precision, int n, const double* pos,
+                     const double* q, const double* kq, double* acc);
+
+/* Complete force() replacement (bin/force.cpp:34-178): field terms of `fp` at time t
+ * (stage time; SG_F_FROZEN_T is irrelevant here) plus the Coulomb sum when
+ * SG_F_COULOMB is set.  mass in kg, charge in units of e. */
+int sg_force(sg_ctx* ctx, int precision, int n, const double* pos, const double* vel,
+             const double* mass, const int* charge, double t,
+             const sg_field_params* fp, double* acc);
+
+/* ---- resident clouds: Dormand-Prince integration on the device -------------- */
+
+/* Describe n_clouds independent clouds with counts[c] ions each (ions of cloud c
+ * follow those of cloud c-1 in every host array).  Allocates device state. */
+int sg_batch_create(sg_ctx* ctx, int n_clouds, const int* counts,
+                    const sg_field_params* fp, const sg_ode_params* op, int precision);
+/* Upload state (host double[n_total][3] pos/vel, kg masses, integer charges) and
+ * reset every cloud's controller to its sg_ode_params. */
+int sg_batch_upload(sg_ctx* ctx, const double* pos, const double* vel,
+                    const double* mass, const int* charge);
+/* Upload positions and velocities only (controller state kept). */
+int sg_batch_set_state(sg_ctx* ctx, const double* pos, const double* vel);
+/* Download positions and velocities (host double[n_total][3]). */
+int sg_batch_download(sg_ctx* ctx, double* pos, double* vel);
+/* Enqueue n_attempts Dormand-Prince attempts for every cloud that is not done
+ * (an accepted attempt commits the step, a rejected one shrinks h; ode.cpp:459-494).
+ * Asynchronous: returns once the work is queued. */
+int sg_batch_attempts(sg_ctx* ctx, int n_attempts);
+/* One accepted step for every cloud that is not done: attempts until each cloud
+ * has accepted (or failed).  Synchronous. */
+int sg_dp45_step(sg_ctx* ctx, sg_step_info* info);
+/* Advance every cloud to its t_end (or until max_attempts attempts); synchronous. */
+int sg_batch_run(sg_ctx* ctx, int64_t max_attempts, sg_step_info* info);
+/* Per-cloud controller state (host array of n_clouds). Synchronous. */
+int sg_batch_info(sg_ctx* ctx, sg_step_info* info);
+/* Change one cloud's field parameters (e.g. a trap ramp between steps). */
+int sg_batch_set_field(sg_ctx* ctx, int cloud, const sg_field_params* fp);
+/* Change one cloud's end time. */
+int sg_batch_set_t_end(sg_ctx* ctx, int cloud, double t_end);
+/* Record each Coulomb launch with CUDA events (1) or not (0); read back the total
+ * kernel time and launch count since the last reset. */
+int sg_set_kernel_timing(sg_ctx* ctx, int on);
+int sg_kernel_timing(sg_ctx* ctx, double* coulomb_ms, int64_t* coulomb_launches,
+                     double* coulomb_interactions);
+/* Capture the attempt sequence in a CUDA graph (1) or launch it directly (0). */
+int sg_set_use_graph(sg_ctx* ctx, int on);
+/* Host-side timer on the context stream (CUDA events). */
+int sg_timer_start(sg_ctx* ctx);
+int sg_timer_stop(sg_ctx* ctx, double* ms);
+
+/* Per-cloud moments of the resident state (host double[n_clouds][12]):
+ * centroid x,y,z; RMS size x,y,z; mean v^2 per axis x,y,z (m^2/s^2);
+ * T_radial, T_axial in kelvin (the reference's Temperature(), bin/ioncloud.cpp:316-335,
+ * with per-ion masses); number of ions. */
+int sg_batch_moments(sg_ctx* ctx, double* out);
+
+/* ---- measurement probes ----------------------------------------------------- */
+/* Issue-rate probes: FP32 FFMA, packed FP32x2 FFMA2 and FP64 DFMA throughput of the
+ * device in GFLOP/s (2 flops per FMA lane), measured with CUDA events. */
+int sg_probe_peaks(sg_ctx* ctx, double* fp32_gflops, double* fp32x2_gflops,
+                   double* fp64_gflops);
+
+/* ---- drop-in slot of the reference's CUNBODY backend ------------------------
+ * Same symbols and argument meaning as the closed library (bin/cunbody.h:11-33):
+ *   ai[i] = sum_j mj[j] (xj[j]-xi[i]) / (|xj[j]-xi[i]|^2 + eps2)^{3/2}
+ * begin is asynchronous, end blocks and writes ai; cunbody1_force does both.
+ * Evaluated in FP64 on the default device with a process-wide context. */
+void cunbody1_force(double xj[][3], double mj[], double xi[][3], double eps2,
+                    double ai[][3], int ni, int nj);
+void cunbody1_force_begin(double xj[][3], double mj[], double xi[][3], double eps2,
+                          double ai[][3], int ni, int nj);
+void cunbody1_force_end(double xj[][3], double mj[], double xi[][3], double eps2,
+                        double ai[][3], int ni, int nj);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIMGB_H */

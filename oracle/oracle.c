@@ -1,0 +1,504 @@
+/*
+ * oracle.c -- CPU restatement of the Simbuca hot path (test infrastructure only;
+ * see oracle.h).  Each function names the reference lines it restates.
+ *
+ * Threads: the Coulomb rows are split over POSIX threads.  Every row is still
+ * summed by one thread in the reference's order, so results do not depend on the
+ * thread count.
+ */
+#include "oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+static int g_threads = 1;
+
+void orc_set_threads(int n) { g_threads = n < 1 ? 1 : (n > 256 ? 256 : n); }
+int orc_get_threads(void) { return g_threads; }
+
+/* std::max / std::min of the reference (C++98 <algorithm>): max(a,b) = a<b ? b : a */
+static inline double ref_max(double a, double b) { return (a < b) ? b : a; }
+static inline double ref_min(double a, double b) { return (b < a) ? b : a; }
+
+/* ---------------------------------------------------------------------------
+ * Coulomb rows.  bin/force.cpp:147-174 (serial CPU path, no MPI):
+ *   kTqiTqjDmj = coulomb_scale*ke*el_charge*charge[j]*el_charge/mass[j];
+ *   for i != j: rx = pos2[i]-pos2[j] ...; distSqr = rx*rx+ry*ry+rz*rz;
+ *     invDist = 1./sqrt(distSqr); invDistCube = invDist*invDist*invDist;
+ *     fx += rx*invDistCube*kTqiTqjDmj*charge_i;
+ *   derivs[j] -= fx
+ * Here "self" is the reference's j_ and "other" its i_.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+    int n, r0, r1;
+    const double* pos;
+    const double* qd;     /* charge of the other ion as double              */
+    const double* kq;     /* per-row coefficient kTqiTqjDmj, or NULL        */
+    const double* mass;   /* used with charge when kq == NULL               */
+    const int* charge;
+    double coulomb_scale;
+    double* out;          /* rows r0..r1 */
+    int mode;             /* 0: out -= f (reference derivs); 1: out = -f (kq)  */
+    int out_offset;       /* out row index = row - out_offset                */
+} coul_job;
+
+static void coul_rows(const coul_job* jb) {
+    const double* pos = jb->pos;
+    const int n = jb->n;
+    for (int j = jb->r0; j < jb->r1; j++) {
+        double fx = 0.0, fy = 0.0, fz = 0.0;
+        double kT;
+        if (jb->kq) {
+            kT = jb->kq[j];
+        } else {
+            /* left-to-right as written at force.cpp:153 */
+            kT = jb->coulomb_scale * ORC_KE * ORC_EL_CHARGE * jb->charge[j] * ORC_EL_CHARGE /
+                 jb->mass[j];
+        }
+        const double bjx = pos[3 * j + 0], bjy = pos[3 * j + 1], bjz = pos[3 * j + 2];
+        for (int i = 0; i < n; i++) {
+            if (i != j) {
+                double rx = pos[3 * i + 0] - bjx;
+                double ry = pos[3 * i + 1] - bjy;
+                double rz = pos[3 * i + 2] - bjz;
+                double distSqr = rx * rx + ry * ry + rz * rz;
+                double invDist = 1. / sqrt(distSqr);
+                double invDistCube = (invDist * invDist * invDist);
+                double qi = jb->charge ? (double)jb->charge[i] : jb->qd[i];
+                fx += rx * invDistCube * kT * qi;
+                fy += ry * invDistCube * kT * qi;
+                fz += rz * invDistCube * kT * qi;
+            }
+        }
+        double* o = jb->out + 3 * (size_t)(j - jb->out_offset);
+        if (jb->mode == 0) {
+            o[0] -= fx;
+            o[1] -= fy;
+            o[2] -= fz;
+        } else {
+            o[0] = 0.0 - fx;
+            o[1] = 0.0 - fy;
+            o[2] = 0.0 - fz;
+        }
+    }
+}
+
+static void* coul_thread(void* arg) {
+    coul_rows((const coul_job*)arg);
+    return NULL;
+}
+
+static void coul_parallel(coul_job base, int r0, int r1) {
+    int nt = g_threads;
+    int rows = r1 - r0;
+    if (nt <= 1 || rows < 64) {
+        base.r0 = r0;
+        base.r1 = r1;
+        coul_rows(&base);
+        return;
+    }
+    if (nt > rows) nt = rows;
+    pthread_t th[256];
+    coul_job jobs[256];
+    int started = 0;
+    for (int t = 0; t < nt; t++) {
+        jobs[t] = base;
+        jobs[t].r0 = r0 + (int)((long long)rows * t / nt);
+        jobs[t].r1 = r0 + (int)((long long)rows * (t + 1) / nt);
+        if (t == 0) continue;
+        if (pthread_create(&th[t], NULL, coul_thread, &jobs[t]) != 0) {
+            coul_rows(&jobs[t]); /* no thread available: do it here */
+            th[t] = 0;
+        } else {
+            started |= 0;
+        }
+    }
+    coul_rows(&jobs[0]);
+    for (int t = 1; t < nt; t++)
+        if (th[t]) pthread_join(th[t], NULL);
+    (void)started;
+}
+
+void orc_coulomb_sub(int n, const double* pos, const double* mass, const int* charge,
+                     double coulomb_scale, double* derivs) {
+    coul_job jb;
+    memset(&jb, 0, sizeof jb);
+    jb.n = n;
+    jb.pos = pos;
+    jb.mass = mass;
+    jb.charge = charge;
+    jb.coulomb_scale = coulomb_scale;
+    jb.out = derivs;
+    jb.mode = 0;
+    coul_parallel(jb, 0, n);
+}
+
+void orc_coulomb_kq(int n, const double* pos, const double* q, const double* kq,
+                    double* acc) {
+    coul_job jb;
+    memset(&jb, 0, sizeof jb);
+    jb.n = n;
+    jb.pos = pos;
+    jb.qd = q;
+    jb.kq = kq;
+    jb.out = acc;
+    jb.mode = 1;
+    coul_parallel(jb, 0, n);
+}
+
+void orc_coulomb_kq_rows(int n, const double* pos, const double* q, const double* kq,
+                         int i0, int i1, double* acc_rows) {
+    coul_job jb;
+    memset(&jb, 0, sizeof jb);
+    jb.n = n;
+    jb.pos = pos;
+    jb.qd = q;
+    jb.kq = kq;
+    jb.out = acc_rows;
+    jb.mode = 1;
+    jb.out_offset = i0;
+    coul_parallel(jb, i0, i1);
+}
+
+/* ---------------------------------------------------------------------------
+ * Field terms.  Paul trap and TOF: bin/force.cpp:40-44 and 58-82, same operation
+ * order.  Penning, excitations and friction: no reference code; formulas in simgb.h.
+ * ------------------------------------------------------------------------- */
+void orc_field(int n, const double* pos, const double* vel, const double* mass,
+               const int* charge, double t, const sg_field_params* fp, double* derivs) {
+    const double kVdc = fp->kappa * fp->Vdc;
+    const double Vrf = fp->Vrf;
+    const double r02 = fp->r0 * fp->r0;
+    const double z02 = fp->z0 * fp->z0;
+    const double omega_rf = fp->freq_rf * 2 * ORC_PI;
+    const uint32_t f = fp->flags;
+
+    /* Penning and drive coefficients (per unit q e/m) */
+    const double kp = (f & SG_F_PENNING) ? fp->V0 / (2.0 * fp->d0 * fp->d0) : 0.0;
+    double gq = 0.0, gd = 0.0;
+    if ((f & SG_F_QUAD) && t >= fp->tq_on && t < fp->tq_off)
+        gq = (2.0 * fp->Uq / (fp->r_el * fp->r_el)) * cos(2.0 * ORC_PI * fp->nu_q * t + fp->phi_q);
+    if ((f & SG_F_DIPOLE) && t >= fp->td_on && t < fp->td_off)
+        gd = (fp->Ud / fp->r_el) * cos(2.0 * ORC_PI * fp->nu_d * t + fp->phi_d);
+
+    for (int j_ = 0; j_ < n; j_++) {
+        double x = pos[3 * j_ + 0], y = pos[3 * j_ + 1], z = pos[3 * j_ + 2];
+        double vx = vel[3 * j_ + 0], vy = vel[3 * j_ + 1], vz = vel[3 * j_ + 2];
+        double* d = derivs + 3 * (size_t)j_;
+        d[0] = 0;
+        d[1] = 0;
+        d[2] = 0;
+        if (f & SG_F_PAUL) {
+            double qDmassa = charge[j_] * ORC_EL_CHARGE / mass[j_];
+            d[0] += qDmassa * (kVdc / z02 - Vrf * cos(omega_rf * t) / r02) * x;
+            d[1] += qDmassa * (kVdc / z02 + Vrf * cos(omega_rf * t) / r02) * y;
+            d[2] += qDmassa * (-2.0 * kVdc / z02) * z;
+        }
+        if (f & SG_F_TOF) {
+            double qDmassa = charge[j_] * ORC_EL_CHARGE / mass[j_];
+            d[0] += qDmassa * fp->E_kick;
+        }
+        if (f & (SG_F_PENNING | SG_F_QUAD | SG_F_DIPOLE)) {
+            double qm = charge[j_] * ORC_EL_CHARGE / mass[j_];
+            double ex = 0.0, ey = 0.0, ez = 0.0;
+            if (f & SG_F_PENNING) {
+                ex = kp * x + fp->B * vy;
+                ey = kp * y - fp->B * vx;
+                ez = -2.0 * kp * z;
+            }
+            ex += gq * y + gd;
+            ey += gq * x;
+            d[0] += qm * ex;
+            d[1] += qm * ey;
+            d[2] += qm * ez;
+        }
+        if (f & SG_F_FRICTION) {
+            d[0] -= fp->delta * vx;
+            d[1] -= fp->delta * vy;
+            d[2] -= fp->delta * vz;
+        }
+        (void)vz;
+    }
+}
+
+void orc_force(int n, const double* pos, const double* vel, const double* mass,
+               const int* charge, double t, const sg_field_params* fp, double* derivs) {
+    orc_field(n, pos, vel, mass, charge, t, fp, derivs);
+    if (fp->flags & SG_F_COULOMB) orc_coulomb_sub(n, pos, mass, charge, fp->coulomb_scale, derivs);
+}
+
+/* ---------------------------------------------------------------------------
+ * Dormand_Prince_5, bin/ode.cpp:61-218.  k[s][j][0..2] = stage velocity,
+ * k[s][j][3..5] = stage acceleration.  Stage s of the reference reads the time
+ * from the cloud lifetime (force.cpp:36), i.e. the step start for every stage;
+ * without SG_F_FROZEN_T stage s is evaluated at t + c_s h.
+ * ------------------------------------------------------------------------- */
+static const double DPc2 = 1.0 / 5.0, DPc3 = 3.0 / 10.0, DPc4 = 4.0 / 5.0, DPc5 = 8.0 / 9.0,
+                    DPc6 = 1.0, DPc7 = 1.0;
+static const double DPa21 = 1.0 / 5.0, DPa31 = 3.0 / 40.0, DPa32 = 9.0 / 40.0,
+                    DPa41 = 44.0 / 45.0, DPa42 = -56.0 / 15.0, DPa43 = 32.0 / 9.0,
+                    DPa51 = 19372.0 / 6561.0, DPa52 = -25360.0 / 2187.0,
+                    DPa53 = 64448.0 / 6561.0, DPa54 = -212.0 / 729.0,
+                    DPa61 = 9017.0 / 3168.0, DPa62 = -355.0 / 33.0, DPa63 = 46732.0 / 5247.0,
+                    DPa64 = 49.0 / 176.0, DPa65 = -5103.0 / 18656.0, DPa71 = 35.0 / 384.0,
+                    DPa73 = 500.0 / 1113.0, DPa74 = 125.0 / 192.0, DPa75 = -2187.0 / 6784.0,
+                    DPa76 = 11.0 / 84.0;
+static const double DPb1 = 35.0 / 384.0, DPb3 = 500.0 / 1113.0, DPb4 = 125.0 / 192.0,
+                    DPb5 = -2187.0 / 6784.0, DPb6 = 11.0 / 84.0;
+static const double DPe1 = 71.0 / 57600.0, DPe3 = -71.0 / 16695.0, DPe4 = 71.0 / 1920.0,
+                    DPe5 = -17253.0 / 339200.0, DPe6 = 22.0 / 525.0, DPe7 = -1.0 / 40.0;
+
+#define KS(s, j, c) k[((size_t)(s) * n + (j)) * 6 + (c)]
+
+double orc_dp45_attempt(int n, const double* pos, const double* vel, const double* mass,
+                        const int* charge, const sg_field_params* fp, orc_ctrl* cs,
+                        double* pos2, double* vel2, double* k, double* derivs) {
+    const double h = cs->h;
+    const int frozen = (fp->flags & SG_F_FROZEN_T) != 0;
+    const double t0 = cs->t;
+    double ts[7];
+    const double cc[7] = {0.0, DPc2, DPc3, DPc4, DPc5, DPc6, DPc7};
+    for (int s = 0; s < 7; s++) ts[s] = frozen ? t0 : t0 + cc[s] * h;
+
+    double err = 0.0, sk;
+    for (int j = 0; j < n; j++) {
+        KS(0, j, 0) = vel[3 * j + 0];
+        KS(0, j, 1) = vel[3 * j + 1];
+        KS(0, j, 2) = vel[3 * j + 2];
+    }
+    memcpy(pos2, pos, sizeof(double) * 3 * (size_t)n);
+    memcpy(vel2, vel, sizeof(double) * 3 * (size_t)n);
+
+    /* stage 1 -> 2 */
+    orc_force(n, pos2, vel2, mass, charge, ts[0], fp, derivs);
+    for (int j = 0; j < n; j++) {
+        for (int c = 0; c < 3; c++) KS(0, j, 3 + c) = derivs[3 * j + c];
+        for (int c = 0; c < 3; c++) pos2[3 * j + c] = pos[3 * j + c] + h * (DPa21 * KS(0, j, c));
+        for (int c = 0; c < 3; c++)
+            KS(1, j, c) = vel2[3 * j + c] = vel[3 * j + c] + h * (DPa21 * KS(0, j, 3 + c));
+    }
+    /* stage 2 -> 3 */
+    orc_force(n, pos2, vel2, mass, charge, ts[1], fp, derivs);
+    for (int j = 0; j < n; j++) {
+        for (int c = 0; c < 3; c++) KS(1, j, 3 + c) = derivs[3 * j + c];
+        for (int c = 0; c < 3; c++)
+            pos2[3 * j + c] = pos[3 * j + c] + h * (DPa31 * KS(0, j, c) + DPa32 * KS(1, j, c));
+        for (int c = 0; c < 3; c++)
+            KS(2, j, c) = vel2[3 * j + c] =
+                vel[3 * j + c] + h * (DPa31 * KS(0, j, 3 + c) + DPa32 * KS(1, j, 3 + c));
+    }
+    /* stage 3 -> 4 */
+    orc_force(n, pos2, vel2, mass, charge, ts[2], fp, derivs);
+    for (int j = 0; j < n; j++) {
+        for (int c = 0; c < 3; c++) KS(2, j, 3 + c) = derivs[3 * j + c];
+        for (int c = 0; c < 3; c++)
+            pos2[3 * j + c] = pos[3 * j + c] + h * (DPa41 * KS(0, j, c) + DPa42 * KS(1, j, c) +
+                                                    DPa43 * KS(2, j, c));
+        for (int c = 0; c < 3; c++)
+            KS(3, j, c) = vel2[3 * j + c] =
+                vel[3 * j + c] + h * (DPa41 * KS(0, j, 3 + c) + DPa42 * KS(1, j, 3 + c) +
+                                      DPa43 * KS(2, j, 3 + c));
+    }
+    /* stage 4 -> 5 */
+    orc_force(n, pos2, vel2, mass, charge, ts[3], fp, derivs);
+    for (int j = 0; j < n; j++) {
+        for (int c = 0; c < 3; c++) KS(3, j, 3 + c) = derivs[3 * j + c];
+        for (int c = 0; c < 3; c++)
+            pos2[3 * j + c] = pos[3 * j + c] + h * (DPa51 * KS(0, j, c) + DPa52 * KS(1, j, c) +
+                                                    DPa53 * KS(2, j, c) + DPa54 * KS(3, j, c));
+        for (int c = 0; c < 3; c++)
+            KS(4, j, c) = vel2[3 * j + c] =
+                vel[3 * j + c] + h * (DPa51 * KS(0, j, 3 + c) + DPa52 * KS(1, j, 3 + c) +
+                                      DPa53 * KS(2, j, 3 + c) + DPa54 * KS(3, j, 3 + c));
+    }
+    /* stage 5 -> 6 */
+    orc_force(n, pos2, vel2, mass, charge, ts[4], fp, derivs);
+    for (int j = 0; j < n; j++) {
+        for (int c = 0; c < 3; c++) KS(4, j, 3 + c) = derivs[3 * j + c];
+        for (int c = 0; c < 3; c++)
+            pos2[3 * j + c] =
+                pos[3 * j + c] + h * (DPa61 * KS(0, j, c) + DPa62 * KS(1, j, c) +
+                                      DPa63 * KS(2, j, c) + DPa64 * KS(3, j, c) +
+                                      DPa65 * KS(4, j, c));
+        for (int c = 0; c < 3; c++)
+            KS(5, j, c) = vel2[3 * j + c] =
+                vel[3 * j + c] + h * (DPa61 * KS(0, j, 3 + c) + DPa62 * KS(1, j, 3 + c) +
+                                      DPa63 * KS(2, j, 3 + c) + DPa64 * KS(3, j, 3 + c) +
+                                      DPa65 * KS(4, j, 3 + c));
+    }
+    /* stage 6 -> 7 */
+    orc_force(n, pos2, vel2, mass, charge, ts[5], fp, derivs);
+    for (int j = 0; j < n; j++) {
+        for (int c = 0; c < 3; c++) KS(5, j, 3 + c) = derivs[3 * j + c];
+        for (int c = 0; c < 3; c++)
+            pos2[3 * j + c] =
+                pos[3 * j + c] + h * (DPa71 * KS(0, j, c) + DPa73 * KS(2, j, c) +
+                                      DPa74 * KS(3, j, c) + DPa75 * KS(4, j, c) +
+                                      DPa76 * KS(5, j, c));
+        for (int c = 0; c < 3; c++)
+            KS(6, j, c) = vel2[3 * j + c] =
+                vel[3 * j + c] + h * (DPa71 * KS(0, j, 3 + c) + DPa73 * KS(2, j, 3 + c) +
+                                      DPa74 * KS(3, j, 3 + c) + DPa75 * KS(4, j, 3 + c) +
+                                      DPa76 * KS(5, j, 3 + c));
+    }
+    /* stage 7 and the 5th-order solution (ode.cpp:175-187) */
+    orc_force(n, pos2, vel2, mass, charge, ts[6], fp, derivs);
+    for (int j = 0; j < n; j++) {
+        for (int c = 0; c < 3; c++) KS(6, j, 3 + c) = derivs[3 * j + c];
+        for (int c = 0; c < 3; c++)
+            pos2[3 * j + c] =
+                pos[3 * j + c] + h * (DPb1 * KS(0, j, c) + DPb3 * KS(2, j, c) +
+                                      DPb4 * KS(3, j, c) + DPb5 * KS(4, j, c) +
+                                      DPb6 * KS(5, j, c));
+        for (int c = 0; c < 3; c++)
+            vel2[3 * j + c] =
+                vel[3 * j + c] + h * (DPb1 * KS(0, j, 3 + c) + DPb3 * KS(2, j, 3 + c) +
+                                      DPb4 * KS(3, j, 3 + c) + DPb5 * KS(4, j, 3 + c) +
+                                      DPb6 * KS(5, j, 3 + c));
+    }
+    /* embedded error, ode.cpp:189-215 */
+    for (int j = 0; j < n; j++) {
+        double yerr[6];
+        for (int i = 0; i < 6; i++)
+            yerr[i] = h * (DPe1 * KS(0, j, i) + DPe3 * KS(2, j, i) + DPe4 * KS(3, j, i) +
+                           DPe5 * KS(4, j, i) + DPe6 * KS(5, j, i) + DPe7 * KS(6, j, i));
+        for (int c = 0; c < 3; c++) {
+            sk = cs->atol + cs->rtol * ref_max(fabs(pos[3 * j + c]), fabs(pos2[3 * j + c]));
+            err = err + (yerr[c] / sk) * (yerr[c] / sk);
+        }
+        for (int c = 0; c < 3; c++) {
+            sk = cs->atol + cs->rtol * ref_max(fabs(vel[3 * j + c]), fabs(vel2[3 * j + c]));
+            err = err + (yerr[3 + c] / sk) * (yerr[3 + c] / sk);
+        }
+    }
+    err = sqrt(err / (6 * n));
+    cs->err = err;
+    cs->force_evals += 7;
+    return err;
+}
+
+/* error_succes, bin/ode.cpp:426-457 (beta = 0, alpha = 0.2, safe = 0.9,
+ * minscale = 0.2, maxscale = 10). */
+int orc_error_succes(double err, orc_ctrl* c) {
+    const double beta = 0.0, alpha = 0.2 - beta * 0.75, safe = 0.9, minscale = 0.2,
+                 maxscale = 10.0;
+    double scale;
+    if (err <= 1.0) {
+        if (err == 0.0)
+            scale = maxscale;
+        else {
+            scale = safe * pow(err, -alpha) * pow(c->errold, beta);
+            if (scale < minscale) scale = minscale;
+            if (scale > maxscale) scale = maxscale;
+        }
+        if (c->reject)
+            c->hnext = c->h * ref_min(scale, 1.0);
+        else
+            c->hnext = c->h * scale;
+        c->errold = ref_max(err, 1.0e-4);
+        c->reject = 0;
+        return 1;
+    } else {
+        scale = ref_max(safe * pow(err, -alpha), minscale);
+        c->h *= scale;
+        c->reject = 1;
+        return 0;
+    }
+}
+
+/* step, bin/ode.cpp:459-494, driven as move_particles does (bin/ion_fly.cpp:83-101):
+ * while lifetime < endtime: step().  A non-finite error norm stops with
+ * SG_NONFINITE (the reference would keep shrinking h by NaN). */
+int64_t orc_dp45_run(int n, double* pos, double* vel, const double* mass,
+                     const int* charge, const sg_field_params* fp, orc_ctrl* c,
+                     int64_t max_steps, double* hist, int64_t hist_cap) {
+    double* k = (double*)malloc(sizeof(double) * 7 * 6 * (size_t)n);
+    double* pos2 = (double*)malloc(sizeof(double) * 3 * (size_t)n);
+    double* vel2 = (double*)malloc(sizeof(double) * 3 * (size_t)n);
+    double* derivs = (double*)malloc(sizeof(double) * 3 * (size_t)n);
+    int64_t nh = 0;
+    int64_t done_steps = 0;
+    c->status = SG_OK;
+    if (!k || !pos2 || !vel2 || !derivs) {
+        free(k); free(pos2); free(vel2); free(derivs);
+        return -SG_BAD_ARG;
+    }
+    while (done_steps < max_steps && c->t < c->t_end) {
+        int rejects_here = 0;
+        for (;;) {
+            double tstart = c->t, hs = c->h;
+            double err = orc_dp45_attempt(n, pos, vel, mass, charge, fp, c, pos2, vel2, k, derivs);
+            int acc = 1;
+            if (!isfinite(err)) {
+                c->status = SG_NONFINITE;
+                acc = 0;
+            } else if (c->adaptive) {
+                c->attempts++;
+                acc = orc_error_succes(err, c);
+                if (!acc) {
+                    c->rejects++;
+                    rejects_here++;
+                    if (fabs(c->h) <= fabs(pos[0]) * DBL_EPSILON) c->status = SG_H_UNDERFLOW;
+                    else if (c->max_rejects > 0 && rejects_here >= c->max_rejects)
+                        c->status = SG_TOO_MANY_REJECTS;
+                }
+            } else {
+                c->attempts++;
+            }
+            if (hist && nh < hist_cap) {
+                hist[4 * nh + 0] = tstart;
+                hist[4 * nh + 1] = hs;
+                hist[4 * nh + 2] = err;
+                hist[4 * nh + 3] = acc;
+            }
+            nh++;
+            if (c->status != SG_OK) goto out;
+            if (acc) break;
+        }
+        memcpy(pos, pos2, sizeof(double) * 3 * (size_t)n);
+        memcpy(vel, vel2, sizeof(double) * 3 * (size_t)n);
+        c->t = c->t + c->h;
+        c->h = c->hnext;
+        c->steps++;
+        done_steps++;
+    }
+out:
+    free(k); free(pos2); free(vel2); free(derivs);
+    if (c->status != SG_OK) return -(int64_t)c->status;
+    return nh;
+}
+
+/* Cloud moments.  Temperature restates IonCloud::Temperature (bin/ioncloud.cpp:316-335):
+ * T_r = (0.5/N sum m (vx^2+vy^2)) * 2/(3 kb), T_z = (0.5/N sum m vz^2) * 2/(3 kb). */
+void orc_moments(int n, const double* pos, const double* vel, const double* mass,
+                 double* out) {
+    double s[3] = {0, 0, 0}, s2[3] = {0, 0, 0}, v2[3] = {0, 0, 0};
+    double er = 0.0, ez = 0.0;
+    for (int i = 0; i < n; i++) {
+        for (int c = 0; c < 3; c++) {
+            double x = pos[3 * i + c], v = vel[3 * i + c];
+            s[c] += x;
+            s2[c] += x * x;
+            v2[c] += v * v;
+        }
+        er += mass[i] * (vel[3 * i + 0] * vel[3 * i + 0] + vel[3 * i + 1] * vel[3 * i + 1]);
+        ez += mass[i] * (vel[3 * i + 2] * vel[3 * i + 2]);
+    }
+    for (int c = 0; c < 3; c++) {
+        double m = n ? s[c] / n : 0.0;
+        out[c] = m;
+        double var = n ? s2[c] / n - m * m : 0.0;
+        out[3 + c] = var > 0 ? sqrt(var) : 0.0;
+        out[6 + c] = n ? v2[c] / n : 0.0;
+    }
+    if (n) {
+        er *= (0.5 / n);
+        ez *= (0.5 / n);
+    }
+    out[9] = er * (2.0 / (3.0 * ORC_KB));
+    out[10] = ez * (2.0 / (3.0 * ORC_KB));
+    out[11] = n;
+}

@@ -1,0 +1,171 @@
+"""Python host API over the libsimgb C ABI (include/simgb.h).
+
+``Context`` owns a CUDA stream and device buffers; ``Batch`` is a set of resident
+clouds integrated on the device.  Arrays are numpy, host memory, in the reference's
+layouts (positions/velocities ``[n, 3]`` float64, masses in kg, integer charges).
+There is no CPU fallback: every call goes through libsimgb.so.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import abi
+from .abi import FieldParams, OdeParams, StepInfo, check, dptr, iptr
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and a.shape != shape:
+        a = a.reshape(shape)
+    return a
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self._L = abi.load()
+        h = ctypes.c_void_p()
+        check(self._L.sg_create(int(device), ctypes.byref(h)), "sg_create")
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.sg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- stand-alone force calls ---------------------------------------------
+    def coulomb_accel(self, pos, q, kq, precision=abi.SG_PREC_FP64):
+        pos = _f64(pos)
+        n = pos.shape[0]
+        q = _f64(q)
+        kq = _f64(kq)
+        out = np.empty((n, 3))
+        check(self._L.sg_coulomb_accel(self._h, int(precision), n, dptr(pos), dptr(q), dptr(kq),
+                                       dptr(out)), "sg_coulomb_accel")
+        return out
+
+    def force(self, pos, vel, mass, charge, t, fp: FieldParams, precision=abi.SG_PREC_FP64):
+        pos = _f64(pos)
+        vel = _f64(vel)
+        mass = _f64(mass)
+        charge = np.ascontiguousarray(charge, dtype=np.int32)
+        n = pos.shape[0]
+        out = np.empty((n, 3))
+        check(self._L.sg_force(self._h, int(precision), n, dptr(pos), dptr(vel), dptr(mass),
+                               iptr(charge), float(t), ctypes.byref(fp), dptr(out)), "sg_force")
+        return out
+
+    def probe_peaks(self):
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(self._L.sg_probe_peaks(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+              "sg_probe_peaks")
+        return {"fp32_gflops": a.value, "fp32x2_gflops": b.value, "fp64_gflops": c.value}
+
+    def timer_start(self):
+        check(self._L.sg_timer_start(self._h), "sg_timer_start")
+
+    def timer_stop(self) -> float:
+        ms = ctypes.c_double()
+        check(self._L.sg_timer_stop(self._h, ctypes.byref(ms)), "sg_timer_stop")
+        return ms.value
+
+    def sync(self):
+        check(self._L.sg_sync(self._h), "sg_sync")
+
+    def set_kernel_timing(self, on: bool):
+        check(self._L.sg_set_kernel_timing(self._h, int(bool(on))), "sg_set_kernel_timing")
+
+    def kernel_timing(self):
+        ms, n, inter = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
+        check(self._L.sg_kernel_timing(self._h, ctypes.byref(ms), ctypes.byref(n),
+                                       ctypes.byref(inter)), "sg_kernel_timing")
+        return {"coulomb_ms": ms.value, "coulomb_launches": n.value, "interactions": inter.value}
+
+    def set_use_graph(self, on: bool):
+        check(self._L.sg_set_use_graph(self._h, int(bool(on))), "sg_set_use_graph")
+
+
+class Batch:
+    """Resident clouds advanced on the device by the Dormand-Prince loop."""
+
+    def __init__(self, ctx: Context, counts, fields, odes, precision=abi.SG_PREC_FP64):
+        self.ctx = ctx
+        self._L = ctx._L
+        self.counts = np.ascontiguousarray(counts, dtype=np.int32)
+        self.n_clouds = len(self.counts)
+        self.n = int(self.counts.sum())
+        self.precision = int(precision)
+        fa = (FieldParams * self.n_clouds)(*[f.copy() for f in fields])
+        oa = (OdeParams * self.n_clouds)(*odes)
+        self._fields = fa
+        check(self._L.sg_batch_create(ctx.handle, self.n_clouds, iptr(self.counts), fa, oa,
+                                      self.precision), "sg_batch_create")
+        self._info = (StepInfo * self.n_clouds)()
+
+    def upload(self, pos, vel, mass, charge):
+        pos, vel, mass = _f64(pos), _f64(vel), _f64(mass)
+        charge = np.ascontiguousarray(charge, dtype=np.int32)
+        assert pos.shape == (self.n, 3) and vel.shape == (self.n, 3)
+        check(self._L.sg_batch_upload(self.ctx.handle, dptr(pos), dptr(vel), dptr(mass),
+                                      iptr(charge)), "sg_batch_upload")
+
+    def set_state(self, pos, vel):
+        pos, vel = _f64(pos), _f64(vel)
+        check(self._L.sg_batch_set_state(self.ctx.handle, dptr(pos), dptr(vel)),
+              "sg_batch_set_state")
+
+    def download(self, pos=None, vel=None):
+        pos = np.empty((self.n, 3)) if pos is None else pos
+        vel = np.empty((self.n, 3)) if vel is None else vel
+        check(self._L.sg_batch_download(self.ctx.handle, dptr(pos), dptr(vel)),
+              "sg_batch_download")
+        return pos, vel
+
+    def attempts(self, n: int):
+        check(self._L.sg_batch_attempts(self.ctx.handle, int(n)), "sg_batch_attempts")
+
+    def step(self, raise_on_error=True):
+        st = self._L.sg_dp45_step(self.ctx.handle, self._info)
+        if raise_on_error:
+            check(st, "sg_dp45_step")
+        return [s.as_dict() for s in self._info], st
+
+    def run(self, max_attempts: int = 1 << 62, raise_on_error=True):
+        st = self._L.sg_batch_run(self.ctx.handle, int(max_attempts), self._info)
+        if raise_on_error:
+            check(st, "sg_batch_run")
+        return [s.as_dict() for s in self._info], st
+
+    def info(self):
+        check(self._L.sg_batch_info(self.ctx.handle, self._info), "sg_batch_info")
+        return [s.as_dict() for s in self._info]
+
+    def moments(self):
+        out = np.empty((self.n_clouds, 12))
+        check(self._L.sg_batch_moments(self.ctx.handle, dptr(out)), "sg_batch_moments")
+        return out
+
+    def set_field(self, cloud: int, fp: FieldParams):
+        check(self._L.sg_batch_set_field(self.ctx.handle, int(cloud), ctypes.byref(fp)),
+              "sg_batch_set_field")
+
+    def set_t_end(self, cloud: int, t_end: float):
+        check(self._L.sg_batch_set_t_end(self.ctx.handle, int(cloud), float(t_end)),
+              "sg_batch_set_t_end")

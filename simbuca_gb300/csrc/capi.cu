@@ -1,0 +1,1032 @@
+// capi.cu -- the extern "C" boundary of libsimgb (include/simgb.h): contexts, device
+// state of resident clouds, work planning, CUDA-graph replay of the Dormand-Prince
+// attempt, stand-alone force calls and the CUNBODY-compatible slot.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "sg_internal.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Device state of a set of clouds (a batch; a stand-alone call uses a batch of one).
+// ---------------------------------------------------------------------------
+struct Problem {
+    int n_clouds = 0, n = 0, npad = 0, precision = 0, n_rows = 0, n_items = 0, max_slots = 0;
+    bool any_coulomb = false;
+    bool uploaded = false;
+    std::vector<SgCloud> hc;
+    std::vector<SgCtrl> hctrl0;
+    std::vector<SgRowBlock> hrows;
+    std::vector<SgWorkItem> hitems;
+    std::vector<int> counts;
+    SgCloud* dc = nullptr;
+    SgCtrl* dctrl = nullptr;
+    SgRowBlock* drows = nullptr;
+    SgWorkItem* ditems = nullptr;
+    double *y = nullptr, *ys = nullptr, *k = nullptr, *part = nullptr, *coul1 = nullptr,
+           *coul7 = nullptr, *kq = nullptr, *qm = nullptr, *qd = nullptr, *mass = nullptr,
+           *c64 = nullptr, *err_part = nullptr, *mom = nullptr, *stage = nullptr;
+    float* c32 = nullptr;
+    int* flags = nullptr;  // [0] error word, [1] hold-on-accept
+    SgCtrl* hctrl = nullptr;  // pinned mirror of dctrl
+    double interactions = 0.0;  // per Coulomb evaluation, all clouds
+    std::vector<double> cloud_inter;
+};
+
+struct TimedLaunch {
+    cudaEvent_t a, b;
+    double inter;
+};
+
+}  // namespace
+
+struct sg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int last_err = 0;
+    int n_sm = 148;
+    Problem batch;
+    Problem solo;
+    bool timing = false;
+    std::vector<TimedLaunch> pending;
+    std::vector<cudaEvent_t> free_ev;
+    double coul_ms = 0.0, coul_inter = 0.0;
+    long long coul_launches = 0;
+    bool use_graph = true;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    float* probe_sink = nullptr;
+    // CUNBODY slot buffers
+    double *cb_xj = nullptr, *cb_mj = nullptr, *cb_xi = nullptr, *cb_ai = nullptr;
+    double* cb_host = nullptr;
+    int cb_ni = 0, cb_nj = 0;
+};
+
+namespace {
+
+#define CK(call)                                   \
+    do {                                           \
+        cudaError_t e_ = (call);                   \
+        if (e_ != cudaSuccess) {                   \
+            ctx->last_err = (int)e_;               \
+            return SG_CUDA_ERR;                    \
+        }                                          \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void**)p, count * sizeof(T));
+}
+
+void free_problem(Problem& P) {
+    cudaFree(P.dc);
+    cudaFree(P.dctrl);
+    cudaFree(P.drows);
+    cudaFree(P.ditems);
+    double* ds[] = {P.y, P.ys, P.k, P.part, P.coul1, P.coul7, P.kq, P.qm,
+                    P.qd, P.mass, P.c64, P.err_part, P.mom, P.stage};
+    for (double* d : ds) cudaFree(d);
+    cudaFree(P.c32);
+    cudaFree(P.flags);
+    if (P.hctrl) cudaFreeHost(P.hctrl);
+    P = Problem();
+}
+
+inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
+
+// Partition clouds into row blocks and Coulomb work items.  Items are sized so that
+// (a) there are several waves of blocks on the device and (b) no single item is a
+// large share of the total work; they are issued largest first.
+void plan(Problem& P, int n_sm) {
+    const int C = P.n_clouds;
+    std::vector<sg_field_params> fps(C);
+    for (int c = 0; c < C; c++) fps[c] = P.hc[c].fp;  // callers set the field terms first
+    P.hc.assign(C, SgCloud());
+    P.hrows.clear();
+    P.hitems.clear();
+    P.cloud_inter.assign(C, 0.0);
+    int off = 0, poff = 0;
+    P.any_coulomb = false;
+    for (int c = 0; c < C; c++) {
+        SgCloud& cl = P.hc[c];
+        memset(&cl, 0, sizeof cl);
+        cl.fp = fps[c];
+        cl.off = off;
+        cl.n = P.counts[c];
+        cl.poff = poff;
+        cl.npad = round_up(cl.n, SG_PAD);
+        cl.rb0 = (int)P.hrows.size();
+        for (int i = 0; i < cl.n; i += SG_ROWS) {
+            SgRowBlock rb;
+            rb.cloud = c;
+            rb.i0 = off + i;
+            rb.n = std::min(SG_ROWS, cl.n - i);
+            rb.pad = 0;
+            P.hrows.push_back(rb);
+        }
+        cl.nrb = (int)P.hrows.size() - cl.rb0;
+        off += cl.n;
+        poff += cl.npad;
+    }
+    P.n = off;
+    P.npad = poff;
+    P.n_rows = (int)P.hrows.size();
+
+    const bool f32 = P.precision == SG_PREC_FP32C;
+    const int ib = f32 ? SG_C32_IB : SG_C64_IB;
+    const int per_sm = f32 ? 3 : 4;
+    const double conc = (double)n_sm * per_sm;
+    double total = 0.0;
+    for (int c = 0; c < C; c++)
+        if (P.hc[c].fp.flags & SG_F_COULOMB) total += (double)P.hc[c].n * P.hc[c].npad;
+    std::vector<int> S(C, 0);
+    long long items = 0;
+    const double cap = std::max(total / (conc * 2.0), 512.0 * 512.0);
+    for (int c = 0; c < C; c++) {
+        const SgCloud& cl = P.hc[c];
+        if (!(cl.fp.flags & SG_F_COULOMB) || cl.n == 0) continue;
+        const double jmax = std::max(128.0, std::floor(cap / std::min(ib, cl.n) / 128.0) * 128.0);
+        S[c] = std::max(1, (int)std::ceil(cl.npad / jmax));
+        items += (long long)((cl.n + ib - 1) / ib) * S[c];
+    }
+    const double target = conc * 4.0;
+    if (items > 0 && items < target) {
+        const int f = (int)std::ceil(target / (double)items);
+        for (int c = 0; c < C; c++)
+            if (S[c] > 0) S[c] = std::min(S[c] * f, std::max(1, P.hc[c].npad / 256));
+    }
+    P.max_slots = 0;
+    for (int c = 0; c < C; c++) {
+        SgCloud& cl = P.hc[c];
+        if (S[c] == 0) {
+            cl.nslots = 0;
+            continue;
+        }
+        P.any_coulomb = true;
+        const int jc = round_up((cl.npad + S[c] - 1) / S[c], 128);
+        int slot = 0;
+        for (int j0 = 0; j0 < cl.npad; j0 += jc, slot++) {
+            const int nj = std::min(jc, cl.npad - j0);
+            for (int i = 0; i < cl.n; i += ib) {
+                SgWorkItem it;
+                memset(&it, 0, sizeof it);
+                it.cloud = c;
+                it.i0 = cl.poff + i;
+                it.ni = std::min(ib, cl.n - i);
+                it.j0 = cl.poff + j0;
+                it.nj = nj;
+                it.slot = slot;
+                P.hitems.push_back(it);
+            }
+        }
+        cl.nslots = slot;
+        P.max_slots = std::max(P.max_slots, slot);
+        P.cloud_inter[c] = (double)cl.n * (cl.n - 1);
+    }
+    std::stable_sort(P.hitems.begin(), P.hitems.end(), [](const SgWorkItem& a, const SgWorkItem& b) {
+        return (long long)a.ni * a.nj > (long long)b.ni * b.nj;
+    });
+    P.n_items = (int)P.hitems.size();
+}
+
+// FP32 frame of a cloud: centre = centroid, L = largest per-axis RMS spread; the
+// close-pair threshold wc = 1/rc^3 with rc = 0.6 x the mean ion spacing of a Gaussian
+// cloud of the same spreads, in frame units.
+void set_frame(SgCloud& cl, const double* pos_aos, int off) {
+    const int n = cl.n;
+    double m[3] = {0, 0, 0}, v[3] = {0, 0, 0};
+    for (int i = 0; i < n; i++)
+        for (int c = 0; c < 3; c++) m[c] += pos_aos[3 * (size_t)(off + i) + c];
+    for (int c = 0; c < 3; c++) m[c] = n ? m[c] / n : 0.0;
+    for (int i = 0; i < n; i++)
+        for (int c = 0; c < 3; c++) {
+            const double d = pos_aos[3 * (size_t)(off + i) + c] - m[c];
+            v[c] += d * d;
+        }
+    double s[3], L = 0.0;
+    for (int c = 0; c < 3; c++) {
+        s[c] = n ? std::sqrt(v[c] / n) : 0.0;
+        L = std::max(L, s[c]);
+    }
+    if (!(L > 0.0) || !std::isfinite(L)) L = 1e-3;
+    cl.cx = m[0];
+    cl.cy = m[1];
+    cl.cz = m[2];
+    cl.L = L;
+    cl.invL = 1.0 / L;
+    double vol = std::pow(2.0 * SG_PI, 1.5);
+    for (int c = 0; c < 3; c++) vol *= std::max(s[c] / L, 1e-3);
+    const double spacing = std::cbrt(vol / std::max(n, 1));
+    const double rc = 0.6 * spacing;
+    cl.wc = (float)(1.0 / (rc * rc * rc));
+}
+
+int alloc_problem(sg_ctx* ctx, Problem& P) {
+    const size_t N = (size_t)std::max(P.n, 1), NP = (size_t)std::max(P.npad, 1);
+    CK(dalloc(&P.dc, (size_t)std::max(P.n_clouds, 1)));
+    CK(dalloc(&P.dctrl, (size_t)std::max(P.n_clouds, 1)));
+    CK(dalloc(&P.drows, (size_t)std::max(P.n_rows, 1)));
+    CK(dalloc(&P.ditems, (size_t)std::max(P.n_items, 1)));
+    CK(dalloc(&P.y, 6 * N));
+    CK(dalloc(&P.ys, 6 * N));
+    CK(dalloc(&P.k, 42 * N));
+    CK(dalloc(&P.part, (size_t)std::max(P.max_slots, 1) * 3 * NP));
+    CK(dalloc(&P.coul1, 3 * N));
+    CK(dalloc(&P.coul7, 3 * N));
+    CK(dalloc(&P.kq, N));
+    CK(dalloc(&P.qm, N));
+    CK(dalloc(&P.qd, N));
+    CK(dalloc(&P.mass, N));
+    CK(dalloc(&P.c64, 4 * NP));
+    CK(dalloc(&P.c32, 7 * NP));
+    CK(dalloc(&P.err_part, (size_t)std::max(P.n_rows, 1)));
+    CK(dalloc(&P.mom, (size_t)std::max(P.n_rows, 1) * 11));
+    CK(dalloc(&P.stage, 6 * N));
+    CK(dalloc(&P.flags, 4));
+    CK(cudaMemset(P.flags, 0, 4 * sizeof(int)));
+    CK(cudaMemset(P.coul1, 0, 3 * N * sizeof(double)));
+    CK(cudaMemset(P.part, 0, (size_t)std::max(P.max_slots, 1) * 3 * NP * sizeof(double)));
+    CK(cudaMallocHost((void**)&P.hctrl, sizeof(SgCtrl) * (size_t)std::max(P.n_clouds, 1)));
+    CK(cudaMemcpy(P.drows, P.hrows.data(), sizeof(SgRowBlock) * P.hrows.size(),
+                  cudaMemcpyHostToDevice));
+    if (P.n_items)
+        CK(cudaMemcpy(P.ditems, P.hitems.data(), sizeof(SgWorkItem) * P.hitems.size(),
+                      cudaMemcpyHostToDevice));
+    return SG_OK;
+}
+
+SgDpArgs dp_args(Problem& P) {
+    SgDpArgs a;
+    a.rows = P.drows;
+    a.clouds = P.dc;
+    a.ctrl = P.dctrl;
+    a.y = P.y;
+    a.ys = P.ys;
+    a.k = P.k;
+    a.part = P.part;
+    a.coul1 = P.coul1;
+    a.coul7 = P.coul7;
+    a.kq = P.kq;
+    a.qm = P.qm;
+    a.c64 = P.c64;
+    a.c32 = P.c32;
+    a.err_part = P.err_part;
+    a.n = P.n;
+    a.npad = P.npad;
+    a.fp32c = P.precision == SG_PREC_FP32C ? 1 : 0;
+    return a;
+}
+
+cudaEvent_t take_event(sg_ctx* ctx) {
+    if (!ctx->free_ev.empty()) {
+        cudaEvent_t e = ctx->free_ev.back();
+        ctx->free_ev.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Accumulate the finished timed launches (call after the stream is synchronised).
+void flush_timing(sg_ctx* ctx) {
+    for (auto& tl : ctx->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, tl.a, tl.b) == cudaSuccess) {
+            ctx->coul_ms += ms;
+            ctx->coul_launches += 1;
+            ctx->coul_inter += tl.inter;
+        }
+        ctx->free_ev.push_back(tl.a);
+        ctx->free_ev.push_back(tl.b);
+    }
+    ctx->pending.clear();
+}
+
+int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter) {
+    if (!P.any_coulomb || P.n_items == 0) return SG_OK;
+    SgCoulombArgs ca;
+    ca.c32 = P.c32;
+    ca.c64 = P.c64;
+    ca.items = P.ditems;
+    ca.n_items = P.n_items;
+    ca.clouds = P.dc;
+    ca.ctrl = with_ctrl ? P.dctrl : nullptr;
+    ca.part = P.part;
+    ca.npad_total = P.npad;
+    ca.errword = P.flags;
+    TimedLaunch tl{nullptr, nullptr, inter};
+    if (ctx->timing) {
+        tl.a = take_event(ctx);
+        tl.b = take_event(ctx);
+        CK(cudaEventRecord(tl.a, ctx->stream));
+    }
+    if (P.precision == SG_PREC_FP32C)
+        CK(sg_launch_coulomb_fp32c(ca, ctx->stream));
+    else
+        CK(sg_launch_coulomb_fp64(ca, ctx->stream));
+    if (ctx->timing) {
+        CK(cudaEventRecord(tl.b, ctx->stream));
+        ctx->pending.push_back(tl);
+    }
+    return SG_OK;
+}
+
+// Interactions of the clouds that are still active (host view of the last sync).
+double active_interactions(Problem& P) {
+    double s = 0.0;
+    for (int c = 0; c < P.n_clouds; c++)
+        if (!P.hctrl[c].done && P.hctrl[c].status == SG_OK) s += P.cloud_inter[c];
+    return s;
+}
+
+// One Dormand-Prince attempt of every active cloud (bin/ode.cpp:61-218, 426-494).
+int enqueue_attempt(sg_ctx* ctx, Problem& P) {
+    SgDpArgs a = dp_args(P);
+    const double inter = ctx->timing ? active_interactions(P) : 0.0;
+    CK(sg_dp_stage(a, 1, P.n_rows, ctx->stream));
+    for (int s = 2; s <= 7; s++) {
+        int st = launch_coulomb(ctx, P, true, inter);
+        if (st != SG_OK) return st;
+        CK(sg_dp_stage(a, s, P.n_rows, ctx->stream));
+    }
+    CK(sg_dp_control(P.dc, P.dctrl, P.err_part, P.y, P.n_clouds, P.flags + 1, ctx->stream));
+    CK(sg_dp_commit(a, P.n_rows, ctx->stream));
+    return SG_OK;
+}
+
+int drop_graph(sg_ctx* ctx) {
+    if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+    }
+    return SG_OK;
+}
+
+int run_attempts(sg_ctx* ctx, Problem& P, int n) {
+    if (ctx->use_graph && !ctx->timing) {
+        if (!ctx->graph) {
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            int st = enqueue_attempt(ctx, P);
+            cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+            if (st != SG_OK) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            CK(e);
+            e = cudaGraphInstantiate(&ctx->graph, g, 0);
+            cudaGraphDestroy(g);
+            CK(e);
+        }
+        for (int i = 0; i < n; i++) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+        return SG_OK;
+    }
+    for (int i = 0; i < n; i++) {
+        int st = enqueue_attempt(ctx, P);
+        if (st != SG_OK) return st;
+    }
+    return SG_OK;
+}
+
+int sync_ctrl(sg_ctx* ctx, Problem& P) {
+    CK(cudaMemcpyAsync(P.hctrl, P.dctrl, sizeof(SgCtrl) * P.n_clouds, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    int errword = 0;
+    CK(cudaMemcpyAsync(&errword, P.flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    flush_timing(ctx);
+    if (errword != 0) return errword;
+    return SG_OK;
+}
+
+void fill_info(const Problem& P, sg_step_info* info) {
+    if (!info) return;
+    for (int c = 0; c < P.n_clouds; c++) {
+        const SgCtrl& s = P.hctrl[c];
+        sg_step_info& o = info[c];
+        memset(&o, 0, sizeof o);
+        o.t = s.t;
+        o.h = s.h;
+        o.h_last = s.h_last;
+        o.err = s.err;
+        o.errold = s.errold;
+        o.steps = s.steps;
+        o.rejects = s.rejects;
+        o.force_evals = s.force_evals;
+        o.coulomb_evals = s.coulomb_evals;
+        o.status = s.status;
+        o.done = s.done;
+        o.reject = s.reject;
+    }
+}
+
+// Per-ion constants of the reference: q e/m (force.cpp:71) and the Coulomb factor
+// coulomb_scale*ke*e*q*e/m written in the order of force.cpp:153.
+void ion_constants(const Problem& P, const double* mass, const int* charge,
+                   std::vector<double>& kq, std::vector<double>& qm, std::vector<double>& qd) {
+    kq.resize(P.n);
+    qm.resize(P.n);
+    qd.resize(P.n);
+    for (int c = 0; c < P.n_clouds; c++) {
+        const SgCloud& cl = P.hc[c];
+        for (int i = cl.off; i < cl.off + cl.n; i++) {
+            kq[i] = cl.fp.coulomb_scale * SG_KE * SG_EL_CHARGE * charge[i] * SG_EL_CHARGE / mass[i];
+            qm[i] = charge[i] * SG_EL_CHARGE / mass[i];
+            qd[i] = (double)charge[i];
+        }
+    }
+}
+
+// Uploads positions/velocities (AoS host) into y and rebuilds the Coulomb inputs.
+int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel) {
+    const size_t N = (size_t)P.n;
+    CK(cudaMemcpyAsync(P.stage, pos, 3 * N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    if (vel)
+        CK(cudaMemcpyAsync(P.stage + 3 * N, vel, 3 * N * sizeof(double), cudaMemcpyHostToDevice,
+                           ctx->stream));
+    CK(sg_aos_to_soa(P.stage, vel ? P.stage + 3 * N : nullptr, P.y, P.n, ctx->stream));
+    for (int c = 0; c < P.n_clouds; c++) set_frame(P.hc[c], pos, P.hc[c].off);
+    CK(cudaMemcpyAsync(P.dc, P.hc.data(), sizeof(SgCloud) * P.n_clouds, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    SgDpArgs a = dp_args(P);
+    CK(sg_coords_from_state(a, P.qd, P.n_rows, ctx->stream));
+    return SG_OK;
+}
+
+int check_fp(const sg_field_params* fp) {
+    if (!fp) return SG_BAD_ARG;
+    if ((fp->flags & SG_F_PAUL) && (fp->r0 == 0.0 || fp->z0 == 0.0)) return SG_BAD_ARG;
+    if ((fp->flags & SG_F_PENNING) && fp->d0 == 0.0) return SG_BAD_ARG;
+    if ((fp->flags & (SG_F_QUAD | SG_F_DIPOLE)) && fp->r_el == 0.0) return SG_BAD_ARG;
+    return SG_OK;
+}
+
+// Prepares `solo` for a stand-alone call on n ions.
+int solo_prepare(sg_ctx* ctx, int n, int precision, const sg_field_params& fp) {
+    Problem& P = ctx->solo;
+    const bool same = P.n_clouds == 1 && P.n == n && P.precision == precision &&
+                      ((P.hc[0].fp.flags & SG_F_COULOMB) == (fp.flags & SG_F_COULOMB));
+    if (!same) {
+        free_problem(P);
+        P.n_clouds = 1;
+        P.counts.assign(1, n);
+        P.precision = precision;
+        P.hc.assign(1, SgCloud());
+        P.hc[0].fp = fp;
+        plan(P, ctx->n_sm);
+        int st = alloc_problem(ctx, P);
+        if (st != SG_OK) {
+            free_problem(P);
+            return st;
+        }
+    }
+    P.hc[0].fp = fp;
+    return SG_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int sg_version(void) { return 100; }
+
+const char* sg_status_string(int s) {
+    switch (s) {
+        case SG_OK: return "ok";
+        case SG_BAD_ARG: return "bad argument";
+        case SG_CUDA_ERR: return "CUDA error";
+        case SG_H_UNDERFLOW: return "stepsize underflow created";
+        case SG_NONFINITE: return "non-finite error norm";
+        case SG_TIMEOUT: return "device wait timed out";
+        case SG_NO_DEVICE: return "no CUDA device";
+        case SG_TOO_MANY_REJECTS: return "too many rejected attempts";
+        case SG_NOT_READY: return "state not uploaded";
+        default: return "unknown status";
+    }
+}
+
+int sg_create(int device, sg_ctx** out) {
+    if (!out) return SG_BAD_ARG;
+    *out = nullptr;
+    int nd = 0;
+    if (cudaGetDeviceCount(&nd) != cudaSuccess || nd <= 0) return SG_NO_DEVICE;
+    if (device < 0 || device >= nd) return SG_BAD_ARG;
+    sg_ctx* ctx = new sg_ctx();
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        delete ctx;
+        return SG_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) ctx->n_sm = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&ctx->t0) != cudaSuccess || cudaEventCreate(&ctx->t1) != cudaSuccess) {
+        delete ctx;
+        return SG_CUDA_ERR;
+    }
+    *out = ctx;
+    return SG_OK;
+}
+
+int sg_destroy(sg_ctx* ctx) {
+    if (!ctx) return SG_BAD_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    flush_timing(ctx);
+    drop_graph(ctx);
+    free_problem(ctx->batch);
+    free_problem(ctx->solo);
+    for (cudaEvent_t e : ctx->free_ev) cudaEventDestroy(e);
+    cudaEventDestroy(ctx->t0);
+    cudaEventDestroy(ctx->t1);
+    cudaFree(ctx->probe_sink);
+    cudaFree(ctx->cb_xj);
+    cudaFree(ctx->cb_mj);
+    cudaFree(ctx->cb_xi);
+    cudaFree(ctx->cb_ai);
+    if (ctx->cb_host) cudaFreeHost(ctx->cb_host);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SG_OK;
+}
+
+int sg_last_cuda_error(sg_ctx* ctx) { return ctx ? ctx->last_err : 0; }
+
+int sg_sync(sg_ctx* ctx) {
+    if (!ctx) return SG_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    flush_timing(ctx);
+    return SG_OK;
+}
+
+int sg_coulomb_accel(sg_ctx* ctx, int precision, int n, const double* pos, const double* q,
+                     const double* kq, double* acc) {
+    if (!ctx || n < 0 || (n > 0 && (!pos || !q || !kq || !acc))) return SG_BAD_ARG;
+    if (precision != SG_PREC_FP64 && precision != SG_PREC_FP32C) return SG_BAD_ARG;
+    if (n == 0) return SG_OK;
+    CK(cudaSetDevice(ctx->device));
+    sg_field_params fp;
+    memset(&fp, 0, sizeof fp);
+    fp.flags = SG_F_COULOMB;
+    fp.coulomb_scale = 1.0;
+    int st = solo_prepare(ctx, n, precision, fp);
+    if (st != SG_OK) return st;
+    Problem& P = ctx->solo;
+    CK(cudaMemcpyAsync(P.qd, q, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.kq, kq, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    st = upload_state(ctx, P, pos, nullptr);
+    if (st != SG_OK) return st;
+    st = launch_coulomb(ctx, P, false, (double)n * (n - 1));
+    if (st != SG_OK) return st;
+    SgDpArgs a = dp_args(P);
+    CK(sg_force_finish(a, 0.0, 0, P.stage, P.n_rows, ctx->stream));
+    CK(cudaMemcpyAsync(acc, P.stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    int errword = 0;
+    CK(cudaMemcpyAsync(&errword, P.flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    flush_timing(ctx);
+    return errword ? errword : SG_OK;
+}
+
+int sg_force(sg_ctx* ctx, int precision, int n, const double* pos, const double* vel,
+             const double* mass, const int* charge, double t, const sg_field_params* fp,
+             double* acc) {
+    if (!ctx || n < 0 || (n > 0 && (!pos || !vel || !mass || !charge || !acc))) return SG_BAD_ARG;
+    if (precision != SG_PREC_FP64 && precision != SG_PREC_FP32C) return SG_BAD_ARG;
+    if (check_fp(fp) != SG_OK) return SG_BAD_ARG;
+    if (n == 0) return SG_OK;
+    CK(cudaSetDevice(ctx->device));
+    int st = solo_prepare(ctx, n, precision, *fp);
+    if (st != SG_OK) return st;
+    Problem& P = ctx->solo;
+    std::vector<double> kq, qm, qd;
+    ion_constants(P, mass, charge, kq, qm, qd);
+    CK(cudaMemcpyAsync(P.qd, qd.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.kq, kq.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.qm, qm.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    st = upload_state(ctx, P, pos, vel);
+    if (st != SG_OK) return st;
+    if (fp->flags & SG_F_COULOMB) {
+        st = launch_coulomb(ctx, P, false, (double)n * (n - 1));
+        if (st != SG_OK) return st;
+    }
+    SgDpArgs a = dp_args(P);
+    CK(sg_force_finish(a, t, 1, P.stage, P.n_rows, ctx->stream));
+    CK(cudaMemcpyAsync(acc, P.stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    int errword = 0;
+    CK(cudaMemcpyAsync(&errword, P.flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    flush_timing(ctx);
+    return errword ? errword : SG_OK;
+}
+
+int sg_batch_create(sg_ctx* ctx, int n_clouds, const int* counts, const sg_field_params* fp,
+                    const sg_ode_params* op, int precision) {
+    if (!ctx || n_clouds <= 0 || !counts || !fp || !op) return SG_BAD_ARG;
+    if (precision != SG_PREC_FP64 && precision != SG_PREC_FP32C) return SG_BAD_ARG;
+    long long total = 0;
+    for (int c = 0; c < n_clouds; c++) {
+        if (counts[c] <= 0 || check_fp(&fp[c]) != SG_OK) return SG_BAD_ARG;
+        if (!(op[c].rtol >= 0.0) || !(op[c].atol >= 0.0) || !(op[c].h0 > 0.0)) return SG_BAD_ARG;
+        total += counts[c];
+    }
+    if (total > (1ll << 30)) return SG_BAD_ARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    flush_timing(ctx);
+    drop_graph(ctx);
+    free_problem(ctx->batch);
+    Problem& P = ctx->batch;
+    P.n_clouds = n_clouds;
+    P.counts.assign(counts, counts + n_clouds);
+    P.precision = precision;
+    P.hc.assign(n_clouds, SgCloud());
+    for (int c = 0; c < n_clouds; c++) P.hc[c].fp = fp[c];
+    plan(P, ctx->n_sm);
+    P.hctrl0.assign(n_clouds, SgCtrl());
+    for (int c = 0; c < n_clouds; c++) {
+        SgCtrl& s = P.hctrl0[c];
+        memset(&s, 0, sizeof s);
+        s.t = op[c].t0;
+        s.h = op[c].h0;
+        s.hnext = op[c].h0;
+        s.errold = 1.0e-4;  // Init_ode, bin/ode.cpp:540
+        s.t_end = op[c].t_end;
+        s.rtol = op[c].rtol;
+        s.atol = op[c].atol;
+        s.adaptive = op[c].adaptive;
+        s.max_rejects = op[c].max_rejects;
+        s.status = SG_OK;
+        s.done = (s.t >= s.t_end) ? 1 : 0;
+    }
+    int st = alloc_problem(ctx, P);
+    if (st != SG_OK) {
+        free_problem(P);
+        return st;
+    }
+    memcpy(P.hctrl, P.hctrl0.data(), sizeof(SgCtrl) * n_clouds);
+    return SG_OK;
+}
+
+int sg_batch_upload(sg_ctx* ctx, const double* pos, const double* vel, const double* mass,
+                    const int* charge) {
+    if (!ctx || !pos || !vel || !mass || !charge) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    for (int i = 0; i < P.n; i++)
+        if (!(mass[i] > 0.0)) return SG_BAD_ARG;
+    CK(cudaSetDevice(ctx->device));
+    std::vector<double> kq, qm, qd;
+    ion_constants(P, mass, charge, kq, qm, qd);
+    const size_t N = (size_t)P.n;
+    CK(cudaMemcpyAsync(P.kq, kq.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.qm, qm.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.qd, qd.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.mass, mass, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    memcpy(P.hctrl, P.hctrl0.data(), sizeof(SgCtrl) * P.n_clouds);
+    CK(cudaMemcpyAsync(P.dctrl, P.hctrl0.data(), sizeof(SgCtrl) * P.n_clouds,
+                       cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(P.flags, 0, 4 * sizeof(int), ctx->stream));
+    int st = upload_state(ctx, P, pos, vel);
+    if (st != SG_OK) return st;
+    // stage-1 Coulomb sum of the initial state
+    st = launch_coulomb(ctx, P, true, active_interactions(P));
+    if (st != SG_OK) return st;
+    SgDpArgs a = dp_args(P);
+    CK(sg_reduce_slots(a, P.coul1, P.n_rows, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    flush_timing(ctx);
+    P.uploaded = true;
+    drop_graph(ctx);  // frames changed: the captured kernels read them from memory, but
+                      // re-capturing keeps the graph tied to the current buffers
+    return SG_OK;
+}
+
+int sg_batch_set_state(sg_ctx* ctx, const double* pos, const double* vel) {
+    if (!ctx || !pos || !vel) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (!P.uploaded) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    int st = upload_state(ctx, P, pos, vel);
+    if (st != SG_OK) return st;
+    st = launch_coulomb(ctx, P, true, active_interactions(P));
+    if (st != SG_OK) return st;
+    SgDpArgs a = dp_args(P);
+    CK(sg_reduce_slots(a, P.coul1, P.n_rows, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    flush_timing(ctx);
+    return SG_OK;
+}
+
+int sg_batch_download(sg_ctx* ctx, double* pos, double* vel) {
+    if (!ctx || !pos || !vel) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (!P.uploaded) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    const size_t N = (size_t)P.n;
+    CK(sg_soa_to_aos(P.y, P.stage, P.stage + 3 * N, P.n, ctx->stream));
+    CK(cudaMemcpyAsync(pos, P.stage, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(vel, P.stage + 3 * N, 3 * N * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
+int sg_batch_attempts(sg_ctx* ctx, int n_attempts) {
+    if (!ctx || n_attempts < 0) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (!P.uploaded) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    return run_attempts(ctx, P, n_attempts);
+}
+
+int sg_dp45_step(sg_ctx* ctx, sg_step_info* info) {
+    if (!ctx) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (!P.uploaded) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    const int one = 1, zero = 0;
+    CK(cudaMemcpyAsync(P.flags + 1, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    int st = SG_OK;
+    // every cloud that is active now takes exactly one accepted step (or fails)
+    for (long long guard = 0; guard < (1ll << 40); guard++) {
+        st = run_attempts(ctx, P, 1);
+        if (st != SG_OK) break;
+        st = sync_ctrl(ctx, P);
+        if (st != SG_OK) break;
+        bool all = true;
+        for (int c = 0; c < P.n_clouds; c++) {
+            const SgCtrl& s = P.hctrl[c];
+            if (!(s.done || s.hold || s.status != SG_OK)) all = false;
+        }
+        if (all) break;
+    }
+    CK(cudaMemcpyAsync(P.flags + 1, &zero, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(sg_clear_hold(P.dctrl, P.n_clouds, ctx->stream));
+    int st2 = sync_ctrl(ctx, P);
+    if (st == SG_OK) st = st2;
+    fill_info(P, info);
+    if (st != SG_OK) return st;
+    for (int c = 0; c < P.n_clouds; c++)
+        if (P.hctrl[c].status != SG_OK) return P.hctrl[c].status;
+    return SG_OK;
+}
+
+int sg_batch_run(sg_ctx* ctx, int64_t max_attempts, sg_step_info* info) {
+    if (!ctx || max_attempts < 0) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (!P.uploaded) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    int st = sync_ctrl(ctx, P);
+    int64_t done_attempts = 0;
+    int chunk = 1;
+    while (st == SG_OK && done_attempts < max_attempts) {
+        bool all = true;
+        for (int c = 0; c < P.n_clouds; c++)
+            if (!P.hctrl[c].done && P.hctrl[c].status == SG_OK) all = false;
+        if (all) break;
+        const int n = (int)std::min<int64_t>(chunk, max_attempts - done_attempts);
+        st = run_attempts(ctx, P, n);
+        if (st != SG_OK) break;
+        done_attempts += n;
+        st = sync_ctrl(ctx, P);
+        chunk = std::min(chunk * 2, 64);
+    }
+    fill_info(P, info);
+    return st;
+}
+
+int sg_batch_info(sg_ctx* ctx, sg_step_info* info) {
+    if (!ctx || !info) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    int st = sync_ctrl(ctx, P);
+    fill_info(P, info);
+    return st;
+}
+
+int sg_batch_set_field(sg_ctx* ctx, int cloud, const sg_field_params* fp) {
+    if (!ctx || check_fp(fp) != SG_OK) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (cloud < 0 || cloud >= P.n_clouds) return SG_BAD_ARG;
+    if ((fp->flags & SG_F_COULOMB) != (P.hc[cloud].fp.flags & SG_F_COULOMB)) return SG_BAD_ARG;
+    CK(cudaSetDevice(ctx->device));
+    P.hc[cloud].fp = *fp;
+    CK(cudaMemcpyAsync(&P.dc[cloud].fp, fp, sizeof(sg_field_params), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
+int sg_batch_set_t_end(sg_ctx* ctx, int cloud, double t_end) {
+    if (!ctx) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (cloud < 0 || cloud >= P.n_clouds) return SG_BAD_ARG;
+    CK(cudaSetDevice(ctx->device));
+    int st = sync_ctrl(ctx, P);
+    if (st != SG_OK) return st;
+    SgCtrl s = P.hctrl[cloud];
+    s.t_end = t_end;
+    if (s.status == SG_OK) s.done = (s.t >= t_end) ? 1 : 0;
+    P.hctrl[cloud] = s;
+    CK(cudaMemcpyAsync(&P.dctrl[cloud], &P.hctrl[cloud], sizeof(SgCtrl), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
+int sg_set_kernel_timing(sg_ctx* ctx, int on) {
+    if (!ctx) return SG_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    flush_timing(ctx);
+    ctx->timing = on != 0;
+    ctx->coul_ms = 0.0;
+    ctx->coul_inter = 0.0;
+    ctx->coul_launches = 0;
+    return SG_OK;
+}
+
+int sg_kernel_timing(sg_ctx* ctx, double* coulomb_ms, int64_t* launches, double* inter) {
+    if (!ctx) return SG_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    flush_timing(ctx);
+    if (coulomb_ms) *coulomb_ms = ctx->coul_ms;
+    if (launches) *launches = ctx->coul_launches;
+    if (inter) *inter = ctx->coul_inter;
+    return SG_OK;
+}
+
+int sg_set_use_graph(sg_ctx* ctx, int on) {
+    if (!ctx) return SG_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    drop_graph(ctx);
+    ctx->use_graph = on != 0;
+    return SG_OK;
+}
+
+int sg_timer_start(sg_ctx* ctx) {
+    if (!ctx) return SG_BAD_ARG;
+    CK(cudaEventRecord(ctx->t0, ctx->stream));
+    return SG_OK;
+}
+
+int sg_timer_stop(sg_ctx* ctx, double* ms) {
+    if (!ctx || !ms) return SG_BAD_ARG;
+    CK(cudaEventRecord(ctx->t1, ctx->stream));
+    CK(cudaEventSynchronize(ctx->t1));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, ctx->t0, ctx->t1));
+    *ms = f;
+    return SG_OK;
+}
+
+int sg_batch_moments(sg_ctx* ctx, double* out) {
+    if (!ctx || !out) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (!P.uploaded) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    SgDpArgs a = dp_args(P);
+    CK(sg_moments(a, P.mass, P.mom, P.n_rows, ctx->stream));
+    std::vector<double> h((size_t)P.n_rows * 11);
+    CK(cudaMemcpyAsync(h.data(), P.mom, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int c = 0; c < P.n_clouds; c++) {
+        const SgCloud& cl = P.hc[c];
+        double s[11] = {0};
+        for (int b = 0; b < cl.nrb; b++)
+            for (int q = 0; q < 11; q++) s[q] += h[(size_t)(cl.rb0 + b) * 11 + q];
+        double* o = out + 12 * (size_t)c;
+        const double n = cl.n;
+        for (int ax = 0; ax < 3; ax++) {
+            const double m = s[ax] / n;
+            o[ax] = m;
+            const double var = s[3 + ax] / n - m * m;
+            o[3 + ax] = var > 0 ? std::sqrt(var) : 0.0;
+            o[6 + ax] = s[6 + ax] / n;
+        }
+        // IonCloud::Temperature (bin/ioncloud.cpp:316-335)
+        o[9] = s[9] * (0.5 / n) * (2.0 / (3.0 * SG_KB));
+        o[10] = s[10] * (0.5 / n) * (2.0 / (3.0 * SG_KB));
+        o[11] = n;
+    }
+    return SG_OK;
+}
+
+int sg_probe_peaks(sg_ctx* ctx, double* fp32, double* fp32x2, double* fp64) {
+    if (!ctx) return SG_BAD_ARG;
+    CK(cudaSetDevice(ctx->device));
+    const int blocks = ctx->n_sm * 8, threads = 256;
+    if (!ctx->probe_sink) CK(dalloc(&ctx->probe_sink, (size_t)blocks * threads));
+    double* outs[3] = {fp32, fp32x2, fp64};
+    for (int w = 0; w < 3; w++) {
+        if (!outs[w]) continue;
+        CK(sg_probe_launch(w, blocks, threads, ctx->probe_sink, ctx->stream));  // warm-up
+        double best = 0.0;
+        for (int rep = 0; rep < 3; rep++) {
+            CK(cudaEventRecord(ctx->t0, ctx->stream));
+            CK(sg_probe_launch(w, blocks, threads, ctx->probe_sink, ctx->stream));
+            CK(cudaEventRecord(ctx->t1, ctx->stream));
+            CK(cudaEventSynchronize(ctx->t1));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ctx->t0, ctx->t1));
+            const double flops = 2.0 * 8.0 * sg_probe_iters(w) * (double)blocks * threads;
+            best = std::max(best, flops / (ms * 1e-3) / 1e9);
+        }
+        *outs[w] = best;
+    }
+    return SG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// CUNBODY slot (bin/cunbody.h:11-33): one process-wide context on the current device.
+// ---------------------------------------------------------------------------
+namespace {
+std::mutex g_cb_mu;
+sg_ctx* g_cb_ctx = nullptr;
+
+int cb_begin(double xj[][3], double mj[], double xi[][3], double eps2, int ni, int nj) {
+    if (!g_cb_ctx) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (sg_create(dev, &g_cb_ctx) != SG_OK) return SG_NO_DEVICE;
+    }
+    sg_ctx* ctx = g_cb_ctx;
+    CK(cudaSetDevice(ctx->device));
+    if (ni > ctx->cb_ni || nj > ctx->cb_nj) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->cb_xj);
+        cudaFree(ctx->cb_mj);
+        cudaFree(ctx->cb_xi);
+        cudaFree(ctx->cb_ai);
+        if (ctx->cb_host) cudaFreeHost(ctx->cb_host);
+        ctx->cb_xj = ctx->cb_mj = ctx->cb_xi = ctx->cb_ai = ctx->cb_host = nullptr;
+        ctx->cb_ni = std::max(ni, ctx->cb_ni);
+        ctx->cb_nj = std::max(nj, ctx->cb_nj);
+        CK(dalloc(&ctx->cb_xj, 3 * (size_t)ctx->cb_nj));
+        CK(dalloc(&ctx->cb_mj, (size_t)ctx->cb_nj));
+        CK(dalloc(&ctx->cb_xi, 3 * (size_t)ctx->cb_ni));
+        CK(dalloc(&ctx->cb_ai, 3 * (size_t)ctx->cb_ni));
+        CK(cudaMallocHost((void**)&ctx->cb_host, 3 * sizeof(double) * (size_t)ctx->cb_ni));
+    }
+    CK(cudaMemcpyAsync(ctx->cb_xj, xj, 3 * sizeof(double) * nj, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->cb_mj, mj, sizeof(double) * nj, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->cb_xi, xi, 3 * sizeof(double) * ni, cudaMemcpyHostToDevice, ctx->stream));
+    CK(sg_cunbody_launch(ctx->cb_xj, ctx->cb_mj, ctx->cb_xi, eps2, ctx->cb_ai, ni, nj, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->cb_host, ctx->cb_ai, 3 * sizeof(double) * ni, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    return SG_OK;
+}
+
+int cb_end(double ai[][3], int ni) {
+    sg_ctx* ctx = g_cb_ctx;
+    if (!ctx) return SG_NOT_READY;
+    CK(cudaStreamSynchronize(ctx->stream));
+    memcpy(ai, ctx->cb_host, 3 * sizeof(double) * (size_t)ni);
+    return SG_OK;
+}
+}  // namespace
+
+extern "C" {
+
+void cunbody1_force_begin(double xj[][3], double mj[], double xi[][3], double eps2,
+                          double ai[][3], int ni, int nj) {
+    (void)ai;
+    std::lock_guard<std::mutex> lk(g_cb_mu);
+    if (ni <= 0) return;
+    if (cb_begin(xj, mj, xi, eps2, ni, nj) != SG_OK)
+        fprintf(stderr, "simgb: cunbody1_force_begin failed\n");
+}
+
+void cunbody1_force_end(double xj[][3], double mj[], double xi[][3], double eps2,
+                        double ai[][3], int ni, int nj) {
+    (void)xj;
+    (void)mj;
+    (void)xi;
+    (void)eps2;
+    (void)nj;
+    std::lock_guard<std::mutex> lk(g_cb_mu);
+    if (ni <= 0) return;
+    if (cb_end(ai, ni) != SG_OK) fprintf(stderr, "simgb: cunbody1_force_end failed\n");
+}
+
+void cunbody1_force(double xj[][3], double mj[], double xi[][3], double eps2, double ai[][3],
+                    int ni, int nj) {
+    cunbody1_force_begin(xj, mj, xi, eps2, ai, ni, nj);
+    cunbody1_force_end(xj, mj, xi, eps2, ai, ni, nj);
+}
+
+}  // extern "C"

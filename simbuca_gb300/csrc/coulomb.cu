@@ -1,0 +1,491 @@
+// coulomb.cu -- direct-sum Coulomb kernels of libsimgb (sm_103a).
+//
+// Both kernels compute, for every i-ion of a work item and the j-range of the item,
+//     P_i = sum_{j != i} q_j (x_i - x_j) / |x_i - x_j|^3          (SI units, m^-2)
+// and store P_i in the item's partial-sum slot; the stage kernels multiply the sum of
+// the slots by kq_i = coulomb_scale k_e e^2 q_i / m_i.  This is the CPU loop of the
+// reference (bin/force.cpp:147-174) regrouped into tiles: same pair terms, no
+// softening, self term excluded by index.
+//
+// FP32c (coulomb_fp32c_kernel): pair terms in FP32 on cloud-frame coordinates
+// u = (x - c)/L held as float-float pairs (hi, lo).  The difference
+// u_j - u_i = (hi_j - hi_i) + (lo_j - lo_i) keeps the pair distance accurate to an
+// FP32 rounding even for ions far from the frame centre.  1/r is the SFU
+// approximation (rsqrt.approx), 1/r^3 is capped at wc: the rare close pairs whose
+// 1/r^3 exceeds wc are re-evaluated in FP64 once the tile is done, and the capped
+// FP32 contribution is taken out again exactly.  Within a 128-ion j-tile the terms
+// are summed in FP32; tile sums are added with Kahan compensation.  Arithmetic uses
+// the packed FP32x2 instructions of sm_100+ (add/mul/fma.rn.f32x2) on pairs of
+// consecutive j-ions.  j-tiles are fetched with TMA bulk copies (cp.async.bulk) into
+// a 4-stage shared-memory ring guarded by mbarriers.
+//
+// FP64 (coulomb_fp64_kernel): the plain form, every operation in FP64; 1/sqrt(r^2)
+// is an FP32 SFU seed refined by one third-order step of the binomial series
+// 1/sqrt(1-e) = 1 + e/2 + 3e^2/8 (e = 1 - r^2 y0^2), accurate to ~1 ulp.
+#include <stdio.h>
+
+#include "sg_internal.cuh"
+
+namespace {
+
+// ---- PTX helpers ---------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ uint64_t globaltimer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait on an mbarrier phase: false once SG_WAIT_NS have passed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    if (mbar_try(bar, parity)) return true;
+    const uint64_t t0 = globaltimer();
+    for (;;) {
+        if (mbar_try(bar, parity)) return true;
+        if (globaltimer() - t0 > SG_WAIT_NS) return false;
+    }
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// packed FP32x2 (two floats in one 64-bit register pair)
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk(f2 v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// Softening added to r^2 in frame units (u ~ 1): below the rounding of any real
+// pair distance, it keeps the self pair (dx = 0) finite: 1/r^3 = 1e36 < FLT_MAX.
+constexpr float kTiny = 1e-24f;
+
+// One FP32c pair term, scalar form.  Written with explicit rounding intrinsics so the
+// close-pair re-evaluation reproduces it bit for bit.
+struct PairF {
+    float dx, dy, dz, y3;
+};
+__device__ __forceinline__ PairF pair_f32(float xjh, float yjh, float zjh, float xjl, float yjl,
+                                          float zjl, float xih, float yih, float zih, float xil,
+                                          float yil, float zil) {
+    PairF p;
+    p.dx = __fadd_rn(__fsub_rn(xjh, xih), __fsub_rn(xjl, xil));
+    p.dy = __fadd_rn(__fsub_rn(yjh, yih), __fsub_rn(yjl, yil));
+    p.dz = __fadd_rn(__fsub_rn(zjh, zih), __fsub_rn(zjl, zil));
+    float r2 = __fmaf_rn(p.dx, p.dx, kTiny);
+    r2 = __fmaf_rn(p.dy, p.dy, r2);
+    r2 = __fmaf_rn(p.dz, p.dz, r2);
+    const float y = rsqrt_approx(r2);
+    p.y3 = __fmul_rn(__fmul_rn(y, y), y);
+    return p;
+}
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+}
+
+
+// Re-evaluates the close pairs of ion ig against one shared-memory tile: pairs whose
+// FP32 1/r^3 exceeded wc get their exact FP64 term, minus the capped FP32 term the
+// main loop already summed (a product of two floats, exact in FP64).
+__device__ __noinline__ void close_pairs(const float (*tl)[SG_TILE], int len, int j0, int ig,
+                                         f2 xh, f2 yh, f2 zh, f2 xl, f2 yl, f2 zl, float wc,
+                                         double invL2, const double* __restrict__ c64,
+                                         int npad_total, double* ox, double* oy, double* oz) {
+    float xih, yih, zih, xil, yil, zil, dummy;
+    upk(xh, xih, dummy);
+    upk(yh, yih, dummy);
+    upk(zh, zih, dummy);
+    upk(xl, xil, dummy);
+    upk(yl, yil, dummy);
+    upk(zl, zil, dummy);
+    const double xi = c64[ig], yi = c64[npad_total + ig], zi = c64[2 * (size_t)npad_total + ig];
+    double cx = 0.0, cy = 0.0, cz = 0.0;
+    for (int jj = 0; jj < len; jj++) {
+        const PairF p = pair_f32(tl[0][jj], tl[1][jj], tl[2][jj], tl[4][jj], tl[5][jj],
+                                 tl[6][jj], xih, yih, zih, xil, yil, zil);
+        const int jg = j0 + jj;
+        if (p.y3 > wc && jg != ig) {
+            const float wf = __fmul_rn(tl[3][jj], wc);
+            const double rx = xi - c64[jg];
+            const double ry = yi - c64[npad_total + jg];
+            const double rz = zi - c64[2 * (size_t)npad_total + jg];
+            const double r2d = rx * rx + ry * ry + rz * rz;
+            const double inv = 1.0 / sqrt(r2d);
+            const double wq = c64[3 * (size_t)npad_total + jg] * inv * inv * inv;
+            cx += wq * rx + invL2 * ((double)wf * (double)p.dx);
+            cy += wq * ry + invL2 * ((double)wf * (double)p.dy);
+            cz += wq * rz + invL2 * ((double)wf * (double)p.dz);
+        }
+    }
+    *ox += cx;
+    *oy += cy;
+    *oz += cz;
+}
+
+
+// Main loop over one shared-memory j-tile for the IPT ions of a thread: packed FP32x2
+// over consecutive j pairs.  DIAG: the tile contains the thread's own ions, whose self
+// pair must not raise the close-pair flag.
+template <int IPT, bool DIAG>
+__device__ __forceinline__ void tile_pairs(const float* tx, const float* ty, const float* tz,
+                                           const float* tq, const float* txl, const float* tyl,
+                                           const float* tzl, int len, int j0, const int* ipad,
+                                           const f2* xh, const f2* yh, const f2* zh,
+                                           const f2* xl, const f2* yl, const f2* zl, f2 tiny2,
+                                           float wc, f2* ax, f2* ay, f2* az, float* y3max) {
+#pragma unroll 2
+    for (int jj = 0; jj < len; jj += 2) {
+        const f2 Xj = *reinterpret_cast<const f2*>(tx + jj);
+        const f2 Yj = *reinterpret_cast<const f2*>(ty + jj);
+        const f2 Zj = *reinterpret_cast<const f2*>(tz + jj);
+        const f2 Qj = *reinterpret_cast<const f2*>(tq + jj);
+        const f2 XLj = *reinterpret_cast<const f2*>(txl + jj);
+        const f2 YLj = *reinterpret_cast<const f2*>(tyl + jj);
+        const f2 ZLj = *reinterpret_cast<const f2*>(tzl + jj);
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            const f2 dx = add2(sub2(Xj, xh[k]), sub2(XLj, xl[k]));
+            const f2 dy = add2(sub2(Yj, yh[k]), sub2(YLj, yl[k]));
+            const f2 dz = add2(sub2(Zj, zh[k]), sub2(ZLj, zl[k]));
+            f2 r2 = fma2(dx, dx, tiny2);
+            r2 = fma2(dy, dy, r2);
+            r2 = fma2(dz, dz, r2);
+            float ra, rb;
+            upk(r2, ra, rb);
+            const f2 y = pk(rsqrt_approx(ra), rsqrt_approx(rb));
+            const f2 y3 = mul2(mul2(y, y), y);
+            float ua, ub;
+            upk(y3, ua, ub);
+            if (DIAG) {
+                const float ma = (j0 + jj == ipad[k]) ? 0.f : ua;
+                const float mb = (j0 + jj + 1 == ipad[k]) ? 0.f : ub;
+                y3max[k] = fmaxf(y3max[k], fmaxf(ma, mb));
+            } else {
+                y3max[k] = fmaxf(y3max[k], fmaxf(ua, ub));
+            }
+            const f2 w = mul2(Qj, pk(fminf(ua, wc), fminf(ub, wc)));
+            ax[k] = fma2(w, dx, ax[k]);
+            ay[k] = fma2(w, dy, ay[k]);
+            az[k] = fma2(w, dz, az[k]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP32c kernel.  Global layout: c32 = 7 float arrays of npad_total entries
+// (x, y, z, q, xl, yl, zl in frame units); shared tile = the same 7 arrays of SG_TILE.
+// ---------------------------------------------------------------------------
+template <int NT, int IPT>
+__global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restrict__ c32,
+                                                            const double* __restrict__ c64,
+                                                            const SgWorkItem* __restrict__ items,
+                                                            const SgCloud* __restrict__ clouds,
+                                                            const SgCtrl* __restrict__ ctrl,
+                                                            double* __restrict__ part,
+                                                            int npad_total, int* errword) {
+    constexpr int T = SG_TILE;
+    __shared__ __align__(128) float tile[SG_STAGES][7][T];
+    __shared__ __align__(8) uint64_t full[SG_STAGES];
+    __shared__ double corr[3][NT * IPT];
+
+    const SgWorkItem it = items[blockIdx.x];
+    if (ctrl != nullptr && (ctrl[it.cloud].done || ctrl[it.cloud].hold || ctrl[it.cloud].status != SG_OK)) return;
+    const SgCloud& cl = clouds[it.cloud];
+    const float wc = cl.wc;
+    const double invL2 = cl.invL * cl.invL;
+    const int tid = threadIdx.x;
+    const float* X = c32;
+    const float* Y = c32 + npad_total;
+    const float* Z = c32 + 2 * (size_t)npad_total;
+    const float* Q = c32 + 3 * (size_t)npad_total;
+    const float* XL = c32 + 4 * (size_t)npad_total;
+    const float* YL = c32 + 5 * (size_t)npad_total;
+    const float* ZL = c32 + 6 * (size_t)npad_total;
+
+    // i-ions of this thread: it.i0 + tid + k*NT (clamped into the item for loads)
+    int ipad[IPT];
+    f2 xh[IPT], yh[IPT], zh[IPT], xl[IPT], yl[IPT], zl[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        int li = tid + k * NT;
+        int ii = it.i0 + (li < it.ni ? li : 0);
+        ipad[k] = li < it.ni ? ii : -1;
+        float a = X[ii], b = Y[ii], c = Z[ii], d = XL[ii], e = YL[ii], f = ZL[ii];
+        xh[k] = pk(a, a);
+        yh[k] = pk(b, b);
+        zh[k] = pk(c, c);
+        xl[k] = pk(d, d);
+        yl[k] = pk(e, e);
+        zl[k] = pk(f, f);
+        corr[0][li] = 0.0;
+        corr[1][li] = 0.0;
+        corr[2][li] = 0.0;
+    }
+    float ks[IPT][3], kc[IPT][3];
+#pragma unroll
+    for (int k = 0; k < IPT; k++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) ks[k][c] = kc[k][c] = 0.f;
+
+    const int ntiles = (it.nj + T - 1) / T;
+    bool ok = true;
+    if (tid == 0) {
+        for (int s = 0; s < SG_STAGES; s++) mbar_init(&full[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    // prologue: fill the ring
+    if (tid == 0) {
+        for (int s = 0; s < SG_STAGES && s < ntiles; s++) {
+            const int j0 = it.j0 + s * T;
+            const int len = min(T, it.j0 + it.nj - j0);
+            const uint32_t bytes = (uint32_t)len * 4u;
+            mbar_arrive_tx(&full[s], 7u * bytes);
+            for (int a = 0; a < 7; a++)
+                bulk_g2s(&tile[s][a][0], c32 + (size_t)a * npad_total + j0, bytes, &full[s]);
+        }
+    }
+
+    const f2 tiny2 = pk(kTiny, kTiny);
+    for (int t = 0; t < ntiles; t++) {
+        const int s = t % SG_STAGES;
+        const uint32_t parity = (uint32_t)((t / SG_STAGES) & 1);
+        const int j0 = it.j0 + t * T;
+        const int len = min(T, it.j0 + it.nj - j0);
+        const bool arrived = mbar_wait(&full[s], parity);
+        if (!__syncthreads_and(arrived)) {  // block-uniform decision
+            ok = false;
+            if (tid == 0) {
+                atomicExch(errword, SG_TIMEOUT);
+                // drain the copies still in flight (tiles t .. t+STAGES-1), bounded
+                for (int u = t; u < ntiles && u < t + SG_STAGES; u++)
+                    (void)mbar_wait(&full[u % SG_STAGES], (uint32_t)((u / SG_STAGES) & 1));
+            }
+            __syncthreads();
+            break;
+        }
+
+        f2 ax[IPT], ay[IPT], az[IPT];
+        float y3max[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            ax[k] = ay[k] = az[k] = 0ull;
+            y3max[k] = 0.f;
+        }
+        const float* tx = tile[s][0];
+        const float* ty = tile[s][1];
+        const float* tz = tile[s][2];
+        const float* tq = tile[s][3];
+        const float* txl = tile[s][4];
+        const float* tyl = tile[s][5];
+        const float* tzl = tile[s][6];
+        // The tile holding this block's own ions takes the variant that keeps the self
+        // pair (dx = 0, contributes nothing) out of the close-pair flag.
+        const bool diag = (j0 < it.i0 + it.ni) && (j0 + len > it.i0);
+        if (!diag)
+            tile_pairs<IPT, false>(tx, ty, tz, tq, txl, tyl, tzl, len, j0, ipad, xh, yh, zh, xl,
+                                   yl, zl, tiny2, wc, ax, ay, az, y3max);
+        else
+            tile_pairs<IPT, true>(tx, ty, tz, tq, txl, tyl, tzl, len, j0, ipad, xh, yh, zh, xl,
+                                  yl, zl, tiny2, wc, ax, ay, az, y3max);
+        // fold the tile sums into the compensated accumulators
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            float a, b;
+            upk(ax[k], a, b);
+            kahan_add(ks[k][0], kc[k][0], __fadd_rn(a, b));
+            upk(ay[k], a, b);
+            kahan_add(ks[k][1], kc[k][1], __fadd_rn(a, b));
+            upk(az[k], a, b);
+            kahan_add(ks[k][2], kc[k][2], __fadd_rn(a, b));
+        }
+        // close pairs of this tile: FP64 term in, capped FP32 term out
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            if (y3max[k] > wc && ipad[k] >= 0) {
+                const int li = tid + k * NT;
+                close_pairs(tile[s], len, j0, ipad[k], xh[k], yh[k], zh[k], xl[k], yl[k], zl[k],
+                            wc, invL2, c64, npad_total, &corr[0][li], &corr[1][li],
+                            &corr[2][li]);
+            }
+        }
+        __syncthreads();  // every thread is done with ring slot s
+        if (tid == 0 && t + SG_STAGES < ntiles) {
+            fence_proxy_async();
+            const int jn = it.j0 + (t + SG_STAGES) * T;
+            const int ln = min(T, it.j0 + it.nj - jn);
+            const uint32_t bytes = (uint32_t)ln * 4u;
+            mbar_arrive_tx(&full[s], 7u * bytes);
+            for (int a = 0; a < 7; a++)
+                bulk_g2s(&tile[s][a][0], c32 + (size_t)a * npad_total + jn, bytes, &full[s]);
+        }
+    }
+    if (!ok) return;
+    double* P = part + (size_t)it.slot * 3 * npad_total;
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        if (ipad[k] < 0) continue;
+        const int li = tid + k * NT;
+        const int ig = ipad[k];
+        // P_i = sum q_j (x_i - x_j)/r^3 = -invL^2 sum w (u_j - u_i) + close-pair terms
+        P[ig] = -invL2 * ((double)ks[k][0] - (double)kc[k][0]) + corr[0][li];
+        P[npad_total + ig] = -invL2 * ((double)ks[k][1] - (double)kc[k][1]) + corr[1][li];
+        P[2 * (size_t)npad_total + ig] =
+            -invL2 * ((double)ks[k][2] - (double)kc[k][2]) + corr[2][li];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 kernel (plain form).  c64 = 4 double arrays (x, y, z, q) in SI units.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double rsqrt_fp64(double r2) {
+    // FP32 SFU seed, then y = y0 (1 + e/2 + 3 e^2/8), e = 1 - r2 y0^2 (binomial series of
+    // (1-e)^(-1/2)); the truncation error is ~(5/16) e^3 with |e| < 2^-22.
+    const double y0 = (double)rsqrt_approx(__double2float_rn(r2));
+    const double e = fma(-r2 * y0, y0, 1.0);
+    const double p = fma(e, 0.375, 0.5);
+    return fma(y0 * e, p, y0);
+}
+
+template <int NT, int IPT>
+__global__ void __launch_bounds__(NT) coulomb_fp64_kernel(const double* __restrict__ c64,
+                                                           const SgWorkItem* __restrict__ items,
+                                                           const SgCtrl* __restrict__ ctrl,
+                                                           double* __restrict__ part,
+                                                           int npad_total) {
+    constexpr int T = NT;
+    __shared__ double tile[4][T];
+    const SgWorkItem it = items[blockIdx.x];
+    if (ctrl != nullptr && (ctrl[it.cloud].done || ctrl[it.cloud].hold || ctrl[it.cloud].status != SG_OK)) return;
+    const int tid = threadIdx.x;
+    const double* X = c64;
+    const double* Y = c64 + npad_total;
+    const double* Z = c64 + 2 * (size_t)npad_total;
+    const double* Q = c64 + 3 * (size_t)npad_total;
+    int ipad[IPT];
+    double xi[IPT], yi[IPT], zi[IPT], ax[IPT], ay[IPT], az[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        const int li = tid + k * NT;
+        const int ii = it.i0 + (li < it.ni ? li : 0);
+        ipad[k] = li < it.ni ? ii : -1;
+        xi[k] = X[ii];
+        yi[k] = Y[ii];
+        zi[k] = Z[ii];
+        ax[k] = ay[k] = az[k] = 0.0;
+    }
+    for (int j0 = it.j0; j0 < it.j0 + it.nj; j0 += T) {
+        const int len = min(T, it.j0 + it.nj - j0);
+        __syncthreads();
+        if (tid < len) {
+            tile[0][tid] = X[j0 + tid];
+            tile[1][tid] = Y[j0 + tid];
+            tile[2][tid] = Z[j0 + tid];
+            tile[3][tid] = Q[j0 + tid];
+        }
+        __syncthreads();
+        for (int jj = 0; jj < len; jj++) {
+            const double xj = tile[0][jj], yj = tile[1][jj], zj = tile[2][jj], qj = tile[3][jj];
+            const int jg = j0 + jj;
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                const double rx = xi[k] - xj, ry = yi[k] - yj, rz = zi[k] - zj;
+                const double r2 = rx * rx + ry * ry + rz * rz;
+                const double y = rsqrt_fp64(r2);
+                double w = qj * (y * y * y);
+                w = (jg == ipad[k]) ? 0.0 : w;
+                ax[k] = fma(w, rx, ax[k]);
+                ay[k] = fma(w, ry, ay[k]);
+                az[k] = fma(w, rz, az[k]);
+            }
+        }
+    }
+    double* P = part + (size_t)it.slot * 3 * npad_total;
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        if (ipad[k] < 0) continue;
+        P[ipad[k]] = ax[k];
+        P[npad_total + ipad[k]] = ay[k];
+        P[2 * (size_t)npad_total + ipad[k]] = az[k];
+    }
+}
+
+}  // namespace
+
+cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s) {
+    if (a.n_items <= 0) return cudaSuccess;
+    coulomb_fp32c_kernel<SG_C32_THREADS, SG_C32_IPT><<<a.n_items, SG_C32_THREADS, 0, s>>>(
+        a.c32, a.c64, a.items,
+        a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_launch_coulomb_fp64(const SgCoulombArgs& a, cudaStream_t s) {
+    if (a.n_items <= 0) return cudaSuccess;
+    coulomb_fp64_kernel<SG_C64_THREADS, SG_C64_IPT><<<a.n_items, SG_C64_THREADS, 0, s>>>(
+        a.c64, a.items, a.ctrl, a.part, a.npad_total);
+    return cudaGetLastError();
+}

@@ -1,0 +1,467 @@
+// dp45.cu -- Dormand-Prince 5(4) stage, error-norm and step-control kernels of
+// libsimgb (sm_103a), plus the O(N) helpers of the stand-alone force calls.
+//
+// Device layout (FP64, structure of arrays over all ions of all clouds, N ions):
+//   y   [6][N]     state at the step start: x, y, z, vx, vy, vz  (IonCloud::pos/vel)
+//   ys  [6][N]     stage state (IonCloud::pos2/vel2)
+//   k   [7][6][N]  stage derivatives: stage velocity, stage acceleration (_ode_vars::k1..k7)
+//   coul1, coul7 [3][N]  Coulomb sums P of stage 1 and stage 7
+// The Coulomb inputs of the next stage are written by the stage kernel itself:
+//   c64 [4][Npad] SI x, y, z, q;  c32 [7][Npad] frame hi x, y, z, q, lo x, y, z.
+//
+// One attempt = stage1, (coulomb, stage s) for s = 2..7, control, commit.  The stage-1
+// Coulomb sum is never recomputed: after an accepted step the positions of stage 1
+// are those of stage 7 (coul1 <- coul7), after a rejected one they are unchanged.
+// The force count still follows the reference (7 per attempt, bin/ode.cpp:101-175).
+#include <math.h>
+
+#include "sg_internal.cuh"
+
+namespace {
+
+// Tableau of bin/ode.cpp:76-86.
+__constant__ double c_a[8][7] = {
+    {0, 0, 0, 0, 0, 0, 0},
+    {0, 0, 0, 0, 0, 0, 0},
+    {1.0 / 5.0, 0, 0, 0, 0, 0, 0},
+    {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0, 0, 0},
+    {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0, 0, 0, 0, 0},
+    {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0, 0, 0, 0},
+    {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0, 0, 0},
+    {35.0 / 384.0, 0.0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0, 0}};
+__constant__ double c_c[8] = {0, 0.0, 1.0 / 5.0, 3.0 / 10.0, 4.0 / 5.0, 8.0 / 9.0, 1.0, 1.0};
+// e = b - b* (bin/ode.cpp:85-86); index by stage 1..7
+__constant__ double c_e[8] = {0,
+                              71.0 / 57600.0,
+                              0.0,
+                              -71.0 / 16695.0,
+                              71.0 / 1920.0,
+                              -17253.0 / 339200.0,
+                              22.0 / 525.0,
+                              -1.0 / 40.0};
+
+typedef SgDpArgs DpArgs;
+
+__device__ __forceinline__ void write_coords(const DpArgs& a, const SgCloud& cl, int ig,
+                                             double x, double y, double z) {
+    a.c64[ig] = x;
+    a.c64[a.npad + ig] = y;
+    a.c64[2 * (size_t)a.npad + ig] = z;
+    if (a.fp32c) {
+        const double u = (x - cl.cx) * cl.invL, v = (y - cl.cy) * cl.invL,
+                     w = (z - cl.cz) * cl.invL;
+        const float uh = __double2float_rn(u), vh = __double2float_rn(v),
+                    wh = __double2float_rn(w);
+        a.c32[ig] = uh;
+        a.c32[a.npad + ig] = vh;
+        a.c32[2 * (size_t)a.npad + ig] = wh;
+        a.c32[4 * (size_t)a.npad + ig] = __double2float_rn(u - (double)uh);
+        a.c32[5 * (size_t)a.npad + ig] = __double2float_rn(v - (double)vh);
+        a.c32[6 * (size_t)a.npad + ig] = __double2float_rn(w - (double)wh);
+    }
+}
+
+// Stage S (1..7) evaluated: finish its force, store k_S, build stage S+1 (or, for
+// S = 7, the embedded error of the attempt).
+template <int S>
+__global__ void __launch_bounds__(SG_ROWS) dp_stage_kernel(DpArgs a) {
+    __shared__ double red[SG_ROWS / 32];
+    const SgRowBlock rb = a.rows[blockIdx.x];
+    const SgCtrl& cs = a.ctrl[rb.cloud];
+    if (cs.done || cs.hold || cs.status != SG_OK) return;
+    const SgCloud& cl = a.clouds[rb.cloud];
+    const int li = threadIdx.x;
+    const bool active = li < rb.n;
+    const int i = rb.i0 + (active ? li : 0);
+    const int ig = cl.poff + (i - cl.off);
+    const size_t N = (size_t)a.n;
+    const double h = cs.h;
+    const bool frozen = (cl.fp.flags & SG_F_FROZEN_T) != 0;
+    const double ts = frozen ? cs.t : cs.t + c_c[S] * h;
+
+    double acc2 = 0.0;
+    if (active) {
+        const double* st = (S == 1) ? a.y : a.ys;
+        const double px = st[i], py = st[N + i], pz = st[2 * N + i];
+        const double vx = st[3 * N + i], vy = st[4 * N + i], vz = st[5 * N + i];
+        double cx = 0.0, cy = 0.0, cz = 0.0;
+        if (cl.fp.flags & SG_F_COULOMB) {
+            if (S == 1) {
+                cx = a.coul1[i];
+                cy = a.coul1[N + i];
+                cz = a.coul1[2 * N + i];
+            } else {
+                for (int sl = 0; sl < cl.nslots; sl++) {
+                    const double* P = a.part + (size_t)sl * 3 * a.npad;
+                    cx += P[ig];
+                    cy += P[a.npad + ig];
+                    cz += P[2 * (size_t)a.npad + ig];
+                }
+                if (S == 7) {
+                    a.coul7[i] = cx;
+                    a.coul7[N + i] = cy;
+                    a.coul7[2 * N + i] = cz;
+                }
+            }
+        }
+        double fx, fy, fz;
+        sg_field_accel(cl.fp, ts, a.qm[i], px, py, pz, vx, vy, vz, fx, fy, fz);
+        const double kqi = a.kq[i];
+        double* kS = a.k + (size_t)(S - 1) * 6 * N;
+        kS[i] = vx;
+        kS[N + i] = vy;
+        kS[2 * N + i] = vz;
+        kS[3 * N + i] = fx + kqi * cx;
+        kS[4 * N + i] = fy + kqi * cy;
+        kS[5 * N + i] = fz + kqi * cz;
+
+        if (S < 7) {
+            // stage S+1: y + h * sum_j a[S+1][j] k_j   (bin/ode.cpp:107-173)
+            double out[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+                double s = 0.0;
+#pragma unroll
+                for (int j = 1; j <= S; j++) s += c_a[S + 1][j - 1] * a.k[((size_t)(j - 1) * 6 + c) * N + i];
+                out[c] = a.y[c * N + i] + h * s;
+            }
+#pragma unroll
+            for (int c = 0; c < 6; c++) a.ys[c * N + i] = out[c];
+            write_coords(a, cl, ig, out[0], out[1], out[2]);
+        } else {
+            // embedded error of the attempt (bin/ode.cpp:189-205); y5 = stage-7 state
+            const double rtol = cs.rtol, atol = cs.atol;
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+                double e = 0.0;
+#pragma unroll
+                for (int j = 1; j <= 7; j++)
+                    if (j != 2) e += c_e[j] * a.k[((size_t)(j - 1) * 6 + c) * N + i];
+                const double yerr = h * e;
+                const double y0 = fabs(a.y[c * N + i]), y1 = fabs(a.ys[c * N + i]);
+                const double sk = atol + rtol * ((y0 < y1) ? y1 : y0);
+                const double r = yerr / sk;
+                acc2 += r * r;
+            }
+        }
+    }
+    if (S == 7) {
+        // deterministic block reduction -> one partial per row block
+        for (int o = 16; o > 0; o >>= 1) acc2 += __shfl_down_sync(0xffffffffu, acc2, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc2;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int w = 0; w < SG_ROWS / 32; w++) s += red[w];
+            a.err_part[blockIdx.x] = s;
+        }
+    }
+}
+
+// error_succes + step bookkeeping (bin/ode.cpp:426-494), one thread per cloud.
+// With *hold_on_accept set, a cloud that accepts holds (skips further attempts) until
+// the host clears the hold: used to take exactly one step per cloud.
+__global__ void dp_control_kernel(const SgCloud* __restrict__ clouds, SgCtrl* __restrict__ ctrl,
+                                  const double* __restrict__ err_part, const double* __restrict__ y,
+                                  int n_clouds, const int* __restrict__ hold_on_accept) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_clouds) return;
+    SgCtrl cs = ctrl[c];
+    const SgCloud cl = clouds[c];
+    if (cs.done || cs.hold || cs.status != SG_OK) {
+        ctrl[c].accepted = 0;
+        return;
+    }
+    double s = 0.0;
+    for (int b = 0; b < cl.nrb; b++) s += err_part[cl.rb0 + b];
+    const double err = sqrt(s / (6 * cl.n));
+    cs.err = err;
+    cs.force_evals += 7;
+    cs.coulomb_evals += (cl.fp.flags & SG_F_COULOMB) ? 6 : 0;
+    int accepted = 1;
+    if (!isfinite(err)) {
+        cs.status = SG_NONFINITE;
+        cs.done = 1;
+        accepted = 0;
+    } else if (cs.adaptive) {
+        const double alpha = 0.2, safe = 0.9, minscale = 0.2, maxscale = 10.0;
+        if (err <= 1.0) {
+            double scale;
+            if (err == 0.0)
+                scale = maxscale;
+            else {
+                scale = safe * pow(err, -alpha);
+                if (scale < minscale) scale = minscale;
+                if (scale > maxscale) scale = maxscale;
+            }
+            cs.hnext = cs.reject ? cs.h * ((1.0 < scale) ? 1.0 : scale) : cs.h * scale;
+            cs.errold = (err < 1.0e-4) ? 1.0e-4 : err;
+            cs.reject = 0;
+        } else {
+            double scale = safe * pow(err, -alpha);
+            scale = (scale < minscale) ? minscale : scale;
+            cs.h *= scale;
+            cs.reject = 1;
+            accepted = 0;
+            cs.rejects++;
+            cs.rejects_here++;
+            const double x0 = fabs(y[cl.off]);  // IonCloud::pos[0][0] (bin/ode.cpp:482)
+            if (fabs(cs.h) <= x0 * 2.220446049250313e-16) {
+                cs.status = SG_H_UNDERFLOW;
+                cs.done = 1;
+            } else if (cs.max_rejects > 0 && cs.rejects_here >= cs.max_rejects) {
+                cs.status = SG_TOO_MANY_REJECTS;
+                cs.done = 1;
+            }
+        }
+    }
+    if (accepted) {
+        cs.h_last = cs.h;
+        cs.t = cs.t + cs.h;
+        cs.h = cs.hnext;
+        cs.steps++;
+        cs.rejects_here = 0;
+        if (cs.t >= cs.t_end) cs.done = 1;
+        if (*hold_on_accept) cs.hold = 1;
+    }
+    cs.accepted = accepted;
+    ctrl[c] = cs;
+}
+
+__global__ void clear_hold_kernel(SgCtrl* ctrl, int n_clouds) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < n_clouds) ctrl[c].hold = 0;
+}
+
+// Commit an accepted attempt: pos <- pos2, vel <- vel2 (bin/ode.cpp:488-489) and the
+// stage-7 Coulomb sum becomes the next stage-1 sum.
+__global__ void __launch_bounds__(SG_ROWS) dp_commit_kernel(DpArgs a) {
+    const SgRowBlock rb = a.rows[blockIdx.x];
+    if (!a.ctrl[rb.cloud].accepted) return;
+    const int li = threadIdx.x;
+    if (li >= rb.n) return;
+    const int i = rb.i0 + li;
+    const size_t N = (size_t)a.n;
+#pragma unroll
+    for (int c = 0; c < 6; c++) a.y[c * N + i] = a.ys[c * N + i];
+#pragma unroll
+    for (int c = 0; c < 3; c++) a.coul1[c * N + i] = a.coul7[c * N + i];
+}
+
+// Coulomb inputs of the state y (set-up and stand-alone calls); ghosts get q = 0.
+__global__ void __launch_bounds__(SG_ROWS) coords_from_state_kernel(DpArgs a,
+                                                                    const double* __restrict__ q) {
+    const SgRowBlock rb = a.rows[blockIdx.x];
+    const SgCloud& cl = a.clouds[rb.cloud];
+    const int li = threadIdx.x;
+    const size_t N = (size_t)a.n;
+    // this block also covers the ghost tail of its cloud when it holds the cloud's last row
+    const bool last = (rb.i0 + rb.n == cl.off + cl.n);
+    if (li < rb.n) {
+        const int i = rb.i0 + li;
+        const int ig = cl.poff + (i - cl.off);
+        write_coords(a, cl, ig, a.y[i], a.y[N + i], a.y[2 * N + i]);
+        a.c64[3 * (size_t)a.npad + ig] = q[i];
+        if (a.fp32c) a.c32[3 * (size_t)a.npad + ig] = (float)q[i];
+    }
+    if (last) {
+        for (int g = cl.n + li; g < cl.npad; g += blockDim.x) {
+            const int ig = cl.poff + g;
+            // far away, no charge: contributes exactly zero as a j-ion
+            const double far = 1.0e3 + 1.0e-3 * g;
+            a.c64[ig] = far;
+            a.c64[a.npad + ig] = far;
+            a.c64[2 * (size_t)a.npad + ig] = far;
+            a.c64[3 * (size_t)a.npad + ig] = 0.0;
+            if (a.fp32c) {
+                const float ff = 1.0e4f + (float)g;
+                a.c32[ig] = ff;
+                a.c32[a.npad + ig] = ff;
+                a.c32[2 * (size_t)a.npad + ig] = ff;
+                a.c32[3 * (size_t)a.npad + ig] = 0.f;
+                a.c32[4 * (size_t)a.npad + ig] = 0.f;
+                a.c32[5 * (size_t)a.npad + ig] = 0.f;
+                a.c32[6 * (size_t)a.npad + ig] = 0.f;
+            }
+        }
+    }
+}
+
+// Sum of the partial-sum slots into dst[3][N] (stage-1 Coulomb sum after set-up).
+__global__ void __launch_bounds__(SG_ROWS) reduce_slots_kernel(DpArgs a, double* dst) {
+    const SgRowBlock rb = a.rows[blockIdx.x];
+    const SgCloud& cl = a.clouds[rb.cloud];
+    const int li = threadIdx.x;
+    if (li >= rb.n) return;
+    const int i = rb.i0 + li;
+    const int ig = cl.poff + (i - cl.off);
+    const size_t N = (size_t)a.n;
+    double cx = 0.0, cy = 0.0, cz = 0.0;
+    for (int sl = 0; sl < cl.nslots; sl++) {
+        const double* P = a.part + (size_t)sl * 3 * a.npad;
+        cx += P[ig];
+        cy += P[a.npad + ig];
+        cz += P[2 * (size_t)a.npad + ig];
+    }
+    dst[i] = cx;
+    dst[N + i] = cy;
+    dst[2 * N + i] = cz;
+}
+
+// Stand-alone force: out[i][c] (AoS) = field(t) + kq_i * sum_slots P (if Coulomb).
+__global__ void __launch_bounds__(SG_ROWS) force_finish_kernel(DpArgs a, double t,
+                                                               int with_field,
+                                                               double* __restrict__ out) {
+    const SgRowBlock rb = a.rows[blockIdx.x];
+    const SgCloud& cl = a.clouds[rb.cloud];
+    const int li = threadIdx.x;
+    if (li >= rb.n) return;
+    const int i = rb.i0 + li;
+    const int ig = cl.poff + (i - cl.off);
+    const size_t N = (size_t)a.n;
+    double cx = 0.0, cy = 0.0, cz = 0.0;
+    if (cl.fp.flags & SG_F_COULOMB) {
+        for (int sl = 0; sl < cl.nslots; sl++) {
+            const double* P = a.part + (size_t)sl * 3 * a.npad;
+            cx += P[ig];
+            cy += P[a.npad + ig];
+            cz += P[2 * (size_t)a.npad + ig];
+        }
+    }
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    if (with_field)
+        sg_field_accel(cl.fp, t, a.qm[i], a.y[i], a.y[N + i], a.y[2 * N + i], a.y[3 * N + i],
+                       a.y[4 * N + i], a.y[5 * N + i], fx, fy, fz);
+    const double kqi = a.kq[i];
+    out[3 * (size_t)i + 0] = fx + kqi * cx;
+    out[3 * (size_t)i + 1] = fy + kqi * cy;
+    out[3 * (size_t)i + 2] = fz + kqi * cz;
+}
+
+// AoS host layout -> SoA state (positions and velocities).
+__global__ void aos_to_soa_kernel(const double* __restrict__ pos, const double* __restrict__ vel,
+                                  double* __restrict__ y, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t N = (size_t)n;
+    for (int c = 0; c < 3; c++) {
+        y[c * N + i] = pos[3 * (size_t)i + c];
+        y[(3 + c) * N + i] = vel ? vel[3 * (size_t)i + c] : 0.0;
+    }
+}
+
+__global__ void soa_to_aos_kernel(const double* __restrict__ y, double* __restrict__ pos,
+                                  double* __restrict__ vel, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t N = (size_t)n;
+    for (int c = 0; c < 3; c++) {
+        pos[3 * (size_t)i + c] = y[c * N + i];
+        vel[3 * (size_t)i + c] = y[(3 + c) * N + i];
+    }
+}
+
+// Per-row-block moment partials: sum x, x^2 per axis, v^2 per axis, m(vx^2+vy^2), m vz^2.
+__global__ void __launch_bounds__(SG_ROWS) moments_kernel(DpArgs a, const double* __restrict__ mass,
+                                                          double* __restrict__ out) {
+    __shared__ double red[11][SG_ROWS / 32];
+    const SgRowBlock rb = a.rows[blockIdx.x];
+    const int li = threadIdx.x;
+    const size_t N = (size_t)a.n;
+    double v[11];
+    for (int q = 0; q < 11; q++) v[q] = 0.0;
+    if (li < rb.n) {
+        const int i = rb.i0 + li;
+        for (int c = 0; c < 3; c++) {
+            const double x = a.y[c * N + i], u = a.y[(3 + c) * N + i];
+            v[c] = x;
+            v[3 + c] = x * x;
+            v[6 + c] = u * u;
+        }
+        v[9] = mass[i] * (v[6] + v[7]);
+        v[10] = mass[i] * v[8];
+    }
+    for (int q = 0; q < 11; q++) {
+        double s = v[q];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((li & 31) == 0) red[q][li >> 5] = s;
+    }
+    __syncthreads();
+    if (li < 11) {
+        double s = 0.0;
+        for (int w = 0; w < SG_ROWS / 32; w++) s += red[li][w];
+        out[(size_t)blockIdx.x * 11 + li] = s;
+    }
+}
+
+}  // namespace
+
+// ---- host-side launchers (called from capi.cu) ------------------------------------
+
+cudaError_t sg_dp_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t st) {
+    if (n_rows <= 0) return cudaSuccess;
+    switch (stage) {
+        case 1: dp_stage_kernel<1><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        case 2: dp_stage_kernel<2><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        case 3: dp_stage_kernel<3><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        case 4: dp_stage_kernel<4><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        case 5: dp_stage_kernel<5><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        case 6: dp_stage_kernel<6><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        case 7: dp_stage_kernel<7><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t sg_dp_control(const SgCloud* clouds, SgCtrl* ctrl, const double* err_part,
+                          const double* y, int n_clouds, const int* hold_on_accept,
+                          cudaStream_t st) {
+    dp_control_kernel<<<(n_clouds + 127) / 128, 128, 0, st>>>(clouds, ctrl, err_part, y, n_clouds,
+                                                              hold_on_accept);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_clear_hold(SgCtrl* ctrl, int n_clouds, cudaStream_t st) {
+    clear_hold_kernel<<<(n_clouds + 127) / 128, 128, 0, st>>>(ctrl, n_clouds);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_dp_commit(const SgDpArgs& a, int n_rows, cudaStream_t st) {
+    dp_commit_kernel<<<n_rows, SG_ROWS, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_coords_from_state(const SgDpArgs& a, const double* q, int n_rows, cudaStream_t st) {
+    coords_from_state_kernel<<<n_rows, SG_ROWS, 0, st>>>(a, q);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_reduce_slots(const SgDpArgs& a, double* dst, int n_rows, cudaStream_t st) {
+    reduce_slots_kernel<<<n_rows, SG_ROWS, 0, st>>>(a, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_force_finish(const SgDpArgs& a, double t, int with_field, double* out, int n_rows,
+                            cudaStream_t st) {
+    force_finish_kernel<<<n_rows, SG_ROWS, 0, st>>>(a, t, with_field, out);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_aos_to_soa(const double* pos, const double* vel, double* y, int n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    aos_to_soa_kernel<<<(n + 255) / 256, 256, 0, st>>>(pos, vel, y, n);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_soa_to_aos(const double* y, double* pos, double* vel, int n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    soa_to_aos_kernel<<<(n + 255) / 256, 256, 0, st>>>(y, pos, vel, n);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_moments(const SgDpArgs& a, const double* mass, double* out, int n_rows,
+                       cudaStream_t st) {
+    moments_kernel<<<n_rows, SG_ROWS, 0, st>>>(a, mass, out);
+    return cudaGetLastError();
+}
+

@@ -1,0 +1,184 @@
+// sg_internal.cuh -- shared device-side definitions of libsimgb (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/simgb.h"
+
+// ---- constants of the reference (bin/globals.h:4-16) -------------------------
+#define SG_PI 3.14159265358979323
+#define SG_EL_CHARGE 1.60217733e-19
+#define SG_KE 8.987551787E9
+#define SG_KB 1.3806504E-23
+
+// ---- launch geometry ---------------------------------------------------------
+// FP32c Coulomb: 128 threads x 4 ions per thread = 512 i-ions per block; j-tiles of
+// 128 ions (2 KB of float4 hi + 2 KB of float4 lo) streamed by TMA bulk copies.
+#define SG_C32_THREADS 128
+#define SG_C32_IPT 4
+#define SG_C32_IB (SG_C32_THREADS * SG_C32_IPT)
+#define SG_TILE 128
+#define SG_STAGES 4
+// FP64 Coulomb: 128 threads x 2 ions per thread.
+#define SG_C64_THREADS 128
+#define SG_C64_IPT 2
+#define SG_C64_IB (SG_C64_THREADS * SG_C64_IPT)
+// Per-cloud ion ranges are padded to a multiple of this (ghost ions carry q = 0).
+#define SG_PAD 32
+// O(N) kernels: ions per block.
+#define SG_ROWS 256
+
+// Bounded device waits: a wait gives up after this many nanoseconds of
+// %globaltimer and raises SG_TIMEOUT in the context's error word.
+#define SG_WAIT_NS 1000000000ull
+
+// One unit of Coulomb work: i-ions [i0, i0+ni) (padded indices) of cloud `cloud`
+// against j-ions [j0, j0+nj) of the same cloud; the partial sums go to slot `slot`.
+struct SgWorkItem {
+    int32_t cloud;
+    int32_t i0, ni;
+    int32_t j0, nj;
+    int32_t slot;
+    int32_t pad0, pad1;
+};
+
+// Rows of one cloud handled by one block of the O(N) kernels.
+struct SgRowBlock {
+    int32_t cloud;
+    int32_t i0;     // first ion (unpadded global index)
+    int32_t n;      // ions in this block (<= SG_ROWS)
+    int32_t pad;
+};
+
+// Device description of a cloud.
+struct SgCloud {
+    int32_t off;     // first ion, unpadded global index
+    int32_t n;       // ions
+    int32_t poff;    // first ion, padded global index
+    int32_t npad;    // padded ions (multiple of SG_PAD)
+    int32_t nslots;  // Coulomb partial-sum slots (j-chunks) of this cloud
+    int32_t rb0, nrb;  // row blocks [rb0, rb0+nrb)
+    int32_t pad;
+    double cx, cy, cz;   // centre of the FP32 frame (m)
+    double L, invL;      // scale of the FP32 frame (m)
+    float wc;            // FP32c close-pair threshold on 1/r^3 (frame units)
+    float pad2;
+    sg_field_params fp;
+};
+
+// Per-cloud Dormand-Prince controller (the scalar part of _ode_vars, bin/ode.h:58-97).
+struct SgCtrl {
+    double t, h, hnext, errold, err, t_end, rtol, atol, h_last;
+    int32_t reject, adaptive, max_rejects, status, done, accepted, rejects_here, hold;
+    long long steps, rejects, force_evals, coulomb_evals;
+};
+
+// ---- field terms ---------------------------------------------------------------
+// Paul/TOF follow bin/force.cpp:40-44,70-80; the Penning trap, the RF excitations and
+// friction follow the formulas of include/simgb.h.
+__device__ __forceinline__ void sg_field_accel(const sg_field_params& fp, double t, double qm,
+                                               double x, double y, double z, double vx,
+                                               double vy, double vz, double& ax, double& ay,
+                                               double& az) {
+    const uint32_t f = fp.flags;
+    ax = 0.0;
+    ay = 0.0;
+    az = 0.0;
+    if (f & SG_F_PAUL) {
+        const double kVdc = fp.kappa * fp.Vdc;
+        const double r02 = fp.r0 * fp.r0, z02 = fp.z0 * fp.z0;
+        const double c = fp.Vrf * cos(fp.freq_rf * 2 * SG_PI * t) / r02;
+        ax += qm * (kVdc / z02 - c) * x;
+        ay += qm * (kVdc / z02 + c) * y;
+        az += qm * (-2.0 * kVdc / z02) * z;
+    }
+    if (f & SG_F_TOF) ax += qm * fp.E_kick;
+    if (f & (SG_F_PENNING | SG_F_QUAD | SG_F_DIPOLE)) {
+        double ex = 0.0, ey = 0.0, ez = 0.0;
+        if (f & SG_F_PENNING) {
+            const double kp = fp.V0 / (2.0 * fp.d0 * fp.d0);
+            ex = kp * x + fp.B * vy;
+            ey = kp * y - fp.B * vx;
+            ez = -2.0 * kp * z;
+        }
+        if ((f & SG_F_QUAD) && t >= fp.tq_on && t < fp.tq_off) {
+            const double g = (2.0 * fp.Uq / (fp.r_el * fp.r_el)) *
+                             cos(2.0 * SG_PI * fp.nu_q * t + fp.phi_q);
+            ex += g * y;
+            ey += g * x;
+        }
+        if ((f & SG_F_DIPOLE) && t >= fp.td_on && t < fp.td_off)
+            ex += (fp.Ud / fp.r_el) * cos(2.0 * SG_PI * fp.nu_d * t + fp.phi_d);
+        ax += qm * ex;
+        ay += qm * ey;
+        az += qm * ez;
+    }
+    if (f & SG_F_FRICTION) {
+        ax -= fp.delta * vx;
+        ay -= fp.delta * vy;
+        az -= fp.delta * vz;
+    }
+}
+
+// ---- Dormand-Prince 5(4) tableau (bin/ode.cpp:76-86) ------------------------------
+#define DP_C2 (1.0 / 5.0)
+#define DP_C3 (3.0 / 10.0)
+#define DP_C4 (4.0 / 5.0)
+#define DP_C5 (8.0 / 9.0)
+
+// Arguments of the O(N) Dormand-Prince kernels (dp45.cu).
+struct SgDpArgs {
+    const SgRowBlock* rows;
+    const SgCloud* clouds;
+    SgCtrl* ctrl;
+    double* y;            // [6][N]
+    double* ys;           // [6][N]
+    double* k;            // [7][6][N]
+    const double* part;   // [slots][3][Npad]
+    double* coul1;        // [3][N]
+    double* coul7;        // [3][N]
+    const double* kq;     // [N]
+    const double* qm;     // [N]
+    double* c64;          // [4][Npad]
+    float* c32;           // [7][Npad]
+    double* err_part;     // [rows]
+    int n;                // ions (unpadded)
+    int npad;             // padded ions
+    int fp32c;            // write the FP32 frame coordinates
+};
+
+// ---- launchers implemented in the .cu files ------------------------------------
+cudaError_t sg_dp_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t st);
+cudaError_t sg_dp_control(const SgCloud* clouds, SgCtrl* ctrl, const double* err_part,
+                          const double* y, int n_clouds, const int* hold_on_accept,
+                          cudaStream_t st);
+cudaError_t sg_clear_hold(SgCtrl* ctrl, int n_clouds, cudaStream_t st);
+int sg_probe_iters(int which);
+cudaError_t sg_dp_commit(const SgDpArgs& a, int n_rows, cudaStream_t st);
+cudaError_t sg_coords_from_state(const SgDpArgs& a, const double* q, int n_rows, cudaStream_t st);
+cudaError_t sg_reduce_slots(const SgDpArgs& a, double* dst, int n_rows, cudaStream_t st);
+cudaError_t sg_force_finish(const SgDpArgs& a, double t, int with_field, double* out, int n_rows,
+                            cudaStream_t st);
+cudaError_t sg_aos_to_soa(const double* pos, const double* vel, double* y, int n, cudaStream_t st);
+cudaError_t sg_soa_to_aos(const double* y, double* pos, double* vel, int n, cudaStream_t st);
+cudaError_t sg_moments(const SgDpArgs& a, const double* mass, double* out, int n_rows,
+                       cudaStream_t st);
+cudaError_t sg_cunbody_launch(const double* xj, const double* mj, const double* xi, double eps2,
+                              double* ai, int ni, int nj, cudaStream_t st);
+cudaError_t sg_probe_launch(int which, int blocks, int threads, float* sink, cudaStream_t st);
+
+struct SgCoulombArgs {
+    const float* c32;        // [7][Npad] frame coords hi x,y,z, charge, lo x,y,z (FP32c)
+    const double* c64;       // [4][Npad] SI coords x,y,z and charge (FP64, close pairs)
+    const SgWorkItem* items;
+    int n_items;
+    const SgCloud* clouds;
+    const SgCtrl* ctrl;      // may be null (stand-alone calls)
+    double* part;            // [slots][3][Npad]
+    int npad_total;
+    int* errword;
+};
+
+cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s);
+cudaError_t sg_launch_coulomb_fp64(const SgCoulombArgs& a, cudaStream_t s);

@@ -1,0 +1,110 @@
+"""Generates the golden vectors in this directory by running the reference Simbuca
+CPU path itself, compiled from its own sources (oracle/Makefile `make ref`).
+
+    python tests/golden/make_golden.py
+
+Needs the reference checkout (the `ref` make target reads its sources); the
+committed .npz files are what the tests use everywhere else.  Inputs are seeded
+synthetic clouds (numpy Philox), stored next to the outputs.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from simbuca_gb300 import configs  # noqa: E402
+
+AMU = oracle.AMU
+# Paul trap of the reference (_trap_param defaults, bin/trapparameters.cpp:2-10) with a
+# TOF kick: Vrf, Vdc, kappa, r0, z0, freq_rf, E_kick
+TRAPP = np.array([50.0, 5.0, 0.001, 0.04, 0.04, 50e5, 100.0])
+
+
+def cloud(n, seed, sigma=0.5e-3, temp=300.0, mixed=False):
+    rng = configs.rng_for(seed)
+    m = np.full(n, 132.905)
+    c = configs.gaussian_cloud(rng, n, sigma, temp, m)
+    if mixed:
+        c.charge = np.where(np.arange(n) % 3 == 0, 2, 1).astype(np.int32)
+        c.mass = np.where(np.arange(n) % 2 == 0, 132.905, 86.909) * AMU
+    return c
+
+
+def main():
+    oracle.build(ref=True)
+    assert oracle.ref_available(), "reference harness did not build"
+    out = {}
+
+    # 1. force() on the 1,000-ion cloud of the small workload: Coulomb only, and
+    #    Paul trap + TOF + Coulomb at a stage time.
+    c = configs.penning_1k().clouds[0]
+    t = 1.3e-7
+    f_coul = oracle.ref_force(c.pos, c.vel, c.mass, c.charge, t, trap=0, tof=0, coulomb=1,
+                              coulomb_scale=1.0, trapp=TRAPP)
+    f_all = oracle.ref_force(c.pos, c.vel, c.mass, c.charge, t, trap=1, tof=1, coulomb=1,
+                             coulomb_scale=1.0, trapp=TRAPP)
+    np.savez_compressed(os.path.join(HERE, "force_1k.npz"), pos=c.pos, vel=c.vel, mass=c.mass,
+                        charge=c.charge, t=t, trapp=TRAPP, f_coulomb=f_coul, f_all=f_all)
+    out["force_1k"] = f_all.shape
+
+    # 2. mixed charges and masses, scaled Coulomb
+    c = cloud(300, 11, mixed=True)
+    f = oracle.ref_force(c.pos, c.vel, c.mass, c.charge, 0.0, trap=1, tof=0, coulomb=1,
+                         coulomb_scale=0.75, trapp=TRAPP)
+    np.savez_compressed(os.path.join(HERE, "force_mixed.npz"), pos=c.pos, vel=c.vel, mass=c.mass,
+                        charge=c.charge, t=0.0, trapp=TRAPP, coulomb_scale=0.75, f=f)
+
+    # 3. edge sizes: one ion (no partner), two ions
+    edges = {}
+    for n in (1, 2, 3):
+        c = cloud(n, 20 + n)
+        edges[f"pos{n}"], edges[f"vel{n}"] = c.pos, c.vel
+        edges[f"mass{n}"], edges[f"charge{n}"] = c.mass, c.charge
+        edges[f"f{n}"] = oracle.ref_force(c.pos, c.vel, c.mass, c.charge, 2e-8, trap=1, tof=0,
+                                          coulomb=1, coulomb_scale=1.0, trapp=TRAPP)
+    np.savez_compressed(os.path.join(HERE, "force_edges.npz"), **edges)
+
+    # 4. adaptive Dormand-Prince: Paul trap + Coulomb, attempt history (t, h, err, accepted)
+    runs = {}
+    for tag, n, seed, rtol, atol, t_end in (("tight", 128, 5, 1e-9, 1e-15, 4e-7),
+                                            ("default", 200, 6, 1e-7, 1e-7, 2e-6)):
+        c = cloud(n, seed)
+        p, v, ctrl, hist, nh = oracle.ref_dp45_run(
+            c.pos, c.vel, c.mass, c.charge, trap=1, tof=0, coulomb=1, coulomb_scale=1.0,
+            trapp=TRAPP, t0=0.0, t_end=t_end, h0=1e-9, adaptive=1, rtol=rtol, atol=atol,
+            max_steps=1 << 40, mode=1, hist_cap=200000)
+        assert nh > 0
+        # the same run through the reference's own step() must land on the same state
+        p0, v0, ctrl0, _, _ = oracle.ref_dp45_run(
+            c.pos, c.vel, c.mass, c.charge, trap=1, tof=0, coulomb=1, coulomb_scale=1.0,
+            trapp=TRAPP, t0=0.0, t_end=t_end, h0=1e-9, adaptive=1, rtol=rtol, atol=atol,
+            max_steps=1 << 40, mode=0)
+        assert np.array_equal(p0, p) and np.array_equal(v0, v) and np.array_equal(ctrl0, ctrl)
+        runs.update({f"{tag}_pos0": c.pos, f"{tag}_vel0": c.vel, f"{tag}_mass": c.mass,
+                     f"{tag}_charge": c.charge, f"{tag}_pos": p, f"{tag}_vel": v,
+                     f"{tag}_ctrl": ctrl, f"{tag}_hist": hist,
+                     f"{tag}_cfg": np.array([rtol, atol, t_end, 1e-9])})
+        out[f"dp45_{tag}"] = (len(hist), int((hist[:, 3] == 0).sum()))
+    np.savez_compressed(os.path.join(HERE, "dp45_adaptive.npz"), **runs)
+
+    # 5. fixed step, 40 steps of 2 ns
+    c = cloud(64, 7)
+    p, v, ctrl, hist, nh = oracle.ref_dp45_run(
+        c.pos, c.vel, c.mass, c.charge, trap=1, tof=0, coulomb=1, coulomb_scale=1.0, trapp=TRAPP,
+        t0=0.0, t_end=1.0, h0=2e-9, adaptive=0, rtol=1e-7, atol=1e-7, max_steps=40, mode=1,
+        hist_cap=100)
+    np.savez_compressed(os.path.join(HERE, "dp45_fixed.npz"), pos0=c.pos, vel0=c.vel,
+                        mass=c.mass, charge=c.charge, pos=p, vel=v, ctrl=ctrl, hist=hist)
+    out["dp45_fixed"] = len(hist)
+    print(out)
+
+
+if __name__ == "__main__":
+    main()

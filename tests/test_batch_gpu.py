@@ -1,0 +1,90 @@
+"""Many independent clouds of uneven size in one batch: every cloud matches its own
+oracle run; per-cloud controllers, statuses and end times stay independent."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from simbuca_gb300 import configs
+from simbuca_gb300.abi import SG_PREC_FP32C, SG_PREC_FP64
+from simbuca_gb300.api import Batch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _oracle():
+    oracle.build()
+    oracle.set_threads(os.cpu_count() or 4)
+
+
+def small_scan(n_clouds=6, sim_time=0.3e-6):
+    w = configs.scan_512(n_clouds=n_clouds, sim_time=sim_time)
+    # keep the clouds small for the oracle: 33..700 ions
+    counts = [33, 700, 64, 257, 128, 511][:n_clouds]
+    rng = configs.rng_for(77)
+    w.clouds = [configs.gaussian_cloud(rng, n, 0.5e-3, 300.0, np.full(n, 132.905)) for n in counts]
+    return w
+
+
+@pytest.mark.parametrize("prec", [SG_PREC_FP64, SG_PREC_FP32C])
+def test_batch_matches_single_runs(ctx, prec):
+    w = small_scan()
+    allc = w.concat()
+    b = Batch(ctx, w.counts, w.fields, w.odes, prec)
+    b.upload(allc.pos, allc.vel, allc.mass, allc.charge)
+    info, st = b.run()
+    assert st == 0
+    p, v = b.download()
+    off = 0
+    for k, c in enumerate(w.clouds):
+        n = len(c.mass)
+        o = w.odes[k]
+        pr, vr, cr, _, _ = oracle.dp45_run(c.pos, c.vel, c.mass, c.charge, w.fields[k],
+                                           rtol=o.rtol, atol=o.atol, h0=o.h0, t0=0.0,
+                                           t_end=o.t_end)
+        assert info[k]["done"] == 1 and info[k]["status"] == 0
+        if prec == SG_PREC_FP64:
+            assert info[k]["steps"] == cr.steps and info[k]["rejects"] == cr.rejects
+            tol = 1e-9
+        else:
+            tol = 2e-6
+        assert np.abs(p[off:off + n] - pr).max() <= tol * np.abs(c.pos).max(), k
+        assert np.abs(v[off:off + n] - vr).max() <= tol * np.abs(c.vel).max(), k
+        off += n
+
+
+def test_one_step_each(ctx):
+    w = small_scan()
+    allc = w.concat()
+    b = Batch(ctx, w.counts, w.fields, w.odes, SG_PREC_FP64)
+    b.upload(allc.pos, allc.vel, allc.mass, allc.charge)
+    for k in range(1, 3):
+        info, st = b.step()
+        assert all(s["steps"] == k for s in info)
+
+
+def test_independent_end_times(ctx):
+    w = small_scan(4)
+    allc = w.concat()
+    b = Batch(ctx, w.counts, w.fields, w.odes, SG_PREC_FP64)
+    b.upload(allc.pos, allc.vel, allc.mass, allc.charge)
+    b.set_t_end(1, 0.1e-6)
+    info, _ = b.run()
+    assert info[1]["t"] < info[0]["t"]
+    assert 0.1e-6 <= info[1]["t"] < 0.2e-6
+    assert all(s["done"] for s in info)
+
+
+def test_moments(ctx):
+    w = small_scan(3)
+    allc = w.concat()
+    b = Batch(ctx, w.counts, w.fields, w.odes, SG_PREC_FP64)
+    b.upload(allc.pos, allc.vel, allc.mass, allc.charge)
+    m = b.moments()
+    off = 0
+    for k, c in enumerate(w.clouds):
+        ref = oracle.moments(c.pos, c.vel, c.mass)
+        np.testing.assert_allclose(m[k], ref, rtol=1e-9, atol=1e-15)
+        off += len(c.mass)

@@ -1,0 +1,201 @@
+"""Dormand-Prince integration on the device against the reference's goldens and the
+oracle: attempt histories (h, err, accept), fixed-step trajectories, Penning runs
+with stage times t + c_s h, and the failure statuses."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from simbuca_gb300 import abi, configs
+from simbuca_gb300.abi import SG_PREC_FP32C, SG_PREC_FP64
+from simbuca_gb300.api import Batch
+from helpers import TRAPP, paul_fp
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _oracle():
+    oracle.build()
+    oracle.set_threads(os.cpu_count() or 4)
+
+
+def one_cloud(ctx, pos, vel, mass, charge, fp, rtol, atol, h0, t_end, prec, adaptive=True,
+              max_rejects=0):
+    op = configs.ode(rtol, atol, h0, t_end, adaptive=adaptive, max_rejects=max_rejects)
+    b = Batch(ctx, [len(mass)], [fp], [op], prec)
+    b.upload(pos, vel, mass, charge)
+    return b
+
+
+def attempt_history(b, max_attempts=100000):
+    """Run attempt by attempt, recording (t_start, h, err, accepted) like the golden."""
+    hist = []
+    prev = b.info()[0]
+    for _ in range(max_attempts):
+        if prev["done"]:
+            break
+        b.attempts(1)
+        cur = b.info()[0]
+        acc = cur["steps"] > prev["steps"]
+        hist.append((prev["t"], prev["h"], cur["err"], 1.0 if acc else 0.0))
+        prev = cur
+    return np.array(hist), prev
+
+
+@pytest.mark.parametrize("tag", ["tight", "default"])
+def test_golden_adaptive_fp64(ctx, tag):
+    g = np.load(os.path.join(GOLD, "dp45_adaptive.npz"))
+    rtol, atol, t_end, h0 = g[f"{tag}_cfg"]
+    fp = paul_fp(TRAPP)
+    b = one_cloud(ctx, g[f"{tag}_pos0"], g[f"{tag}_vel0"], g[f"{tag}_mass"], g[f"{tag}_charge"],
+                  fp, rtol, atol, h0, t_end, SG_PREC_FP64)
+    hist, last = attempt_history(b)
+    gh = g[f"{tag}_hist"]
+    assert hist.shape == gh.shape
+    assert np.array_equal(hist[:, 3], gh[:, 3])          # same accept/reject sequence
+    np.testing.assert_allclose(hist[:, :2], gh[:, :2], rtol=1e-11)   # t, h
+    np.testing.assert_allclose(hist[:, 2], gh[:, 2], rtol=1e-8)      # error norms
+    p, v = b.download()
+    np.testing.assert_allclose(p, g[f"{tag}_pos"], rtol=1e-9, atol=1e-15)
+    np.testing.assert_allclose(v, g[f"{tag}_vel"], rtol=1e-9, atol=1e-9)
+    assert last["steps"] == int(g[f"{tag}_ctrl"][5])
+
+
+def test_golden_adaptive_fp32c(ctx):
+    g = np.load(os.path.join(GOLD, "dp45_adaptive.npz"))
+    tag = "tight"
+    rtol, atol, t_end, h0 = g[f"{tag}_cfg"]
+    b = one_cloud(ctx, g[f"{tag}_pos0"], g[f"{tag}_vel0"], g[f"{tag}_mass"], g[f"{tag}_charge"],
+                  paul_fp(TRAPP), rtol, atol, h0, t_end, SG_PREC_FP32C)
+    info, _ = b.run()
+    p, v = b.download()
+    assert info[0]["status"] == 0
+    np.testing.assert_allclose(p, g[f"{tag}_pos"], rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(v, g[f"{tag}_vel"], rtol=1e-5, atol=1e-6)
+
+
+def test_golden_fixed_step(ctx):
+    g = np.load(os.path.join(GOLD, "dp45_fixed.npz"))
+    b = one_cloud(ctx, g["pos0"], g["vel0"], g["mass"], g["charge"], paul_fp(TRAPP), 1e-7, 1e-7,
+                  2e-9, 1.0, SG_PREC_FP64, adaptive=False)
+    info, _ = b.run(max_attempts=40)
+    assert info[0]["steps"] == 40 and info[0]["rejects"] == 0
+    p, v = b.download()
+    np.testing.assert_allclose(p, g["pos"], rtol=1e-10, atol=1e-16)
+    np.testing.assert_allclose(v, g["vel"], rtol=1e-10, atol=1e-10)
+
+
+@pytest.mark.parametrize("prec", [SG_PREC_FP64, SG_PREC_FP32C])
+def test_penning_drive_vs_oracle(ctx, prec):
+    """Penning trap + quadrupole + dipole drive + friction, stage times t + c_s h."""
+    w = configs.penning_1k(n=300, seed=9)
+    c = w.clouds[0]
+    fp = configs.penning_field(quad=(0.5, configs.nu_c(132.905), 0.0, 0.0, 1.0),
+                               dipole=(0.1, 1138.4, 0.0, 0.0, 1.0), delta=1e3)
+    t_end = 0.5e-6
+    p_ref, v_ref, cr, hist, nh = oracle.dp45_run(c.pos, c.vel, c.mass, c.charge, fp, rtol=1e-9,
+                                                 atol=1e-15, h0=1e-9, t0=0.0, t_end=t_end,
+                                                 hist_cap=100000)
+    assert cr.status == 0
+    b = one_cloud(ctx, c.pos, c.vel, c.mass, c.charge, fp, 1e-9, 1e-15, 1e-9, t_end, prec)
+    info, _ = b.run()
+    p, v = b.download()
+    tol = 1e-9 if prec == SG_PREC_FP64 else 2e-6
+    if prec == SG_PREC_FP64:
+        assert info[0]["steps"] == cr.steps and info[0]["rejects"] == cr.rejects
+        assert info[0]["t"] == pytest.approx(cr.t, rel=1e-12)
+    scale_p = np.abs(c.pos).max()
+    scale_v = np.abs(c.vel).max()
+    assert np.abs(p - p_ref).max() <= tol * scale_p
+    assert np.abs(v - v_ref).max() <= tol * scale_v
+
+
+def test_graph_and_direct_identical(ctx):
+    w = configs.penning_1k(n=500, seed=3)
+    c = w.clouds[0]
+    fp = configs.penning_field()
+    out = []
+    for graph in (True, False):
+        ctx.set_use_graph(graph)
+        b = one_cloud(ctx, c.pos, c.vel, c.mass, c.charge, fp, 1e-9, 1e-15, 1e-9, 1e-6,
+                      SG_PREC_FP32C)
+        b.run()
+        out.append(b.download())
+    ctx.set_use_graph(True)
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_step_takes_one_step(ctx):
+    w = configs.penning_1k(n=200, seed=4)
+    c = w.clouds[0]
+    b = one_cloud(ctx, c.pos, c.vel, c.mass, c.charge, configs.penning_field(), 1e-9, 1e-15,
+                  1e-9, 1.0, SG_PREC_FP64)
+    for k in range(1, 4):
+        info, st = b.step()
+        assert st == 0 and info[0]["steps"] == k
+
+
+def test_underflow_status(ctx):
+    g = np.load(os.path.join(GOLD, "force_edges.npz"))
+    pos = g["pos2"].copy()
+    pos[1] = pos[0] + 1e-13
+    b = one_cloud(ctx, pos, g["vel2"], g["mass2"], g["charge2"], paul_fp(TRAPP), 1e-15, 1e-30,
+                  1e-9, 1e-6, SG_PREC_FP64)
+    info, st = b.run(raise_on_error=False)
+    assert st == 0 and info[0]["status"] == abi.SG_H_UNDERFLOW and info[0]["done"] == 1
+    # the mirror of step() raises what the reference throws
+    from simbuca_gb300 import ode
+    cl = ode.IonCloud(pos, g["vel2"], g["mass2"], g["charge2"])
+    od = ode.OdeVars()
+    od.Init_ode(5, 1e-9, True)
+    od.rk_rtol, od.rk_atol = 1e-15, 1e-30
+    od.forcev.coulomb_interaction = True
+    od.forcev.trap_param.E_kick = 0.0
+    with pytest.raises(RuntimeError, match="stepsize underflow created"):
+        for _ in range(100000):
+            ode.step(cl, od)
+
+
+def test_nonfinite_status(ctx):
+    """Two ions at exactly the same place: the FP64 sum is 0/0 as in the reference, and
+    the controller stops the cloud with SG_NONFINITE instead of looping."""
+    g = np.load(os.path.join(GOLD, "force_edges.npz"))
+    pos = g["pos3"].copy()
+    pos[2] = pos[1]
+    b = one_cloud(ctx, pos, g["vel3"], g["mass3"], g["charge3"], paul_fp(TRAPP), 1e-9, 1e-15,
+                  1e-9, 1e-6, SG_PREC_FP64)
+    info, st = b.run(max_attempts=5, raise_on_error=False)
+    assert info[0]["status"] == abi.SG_NONFINITE
+
+
+def test_too_many_rejects(ctx):
+    w = configs.penning_1k(n=100, seed=5)
+    c = w.clouds[0]
+    # h0 far too large for rtol 1e-12: the first step needs several rejects
+    b = one_cloud(ctx, c.pos, c.vel, c.mass, c.charge, configs.penning_field(), 1e-12, 1e-18,
+                  1e-6, 1.0, SG_PREC_FP64, max_rejects=2)
+    info, st = b.run(max_attempts=10, raise_on_error=False)
+    assert info[0]["status"] == abi.SG_TOO_MANY_REJECTS
+
+
+def test_reference_mirror_step_and_force(ctx):
+    """The IonCloud/_ode_vars/step()/force() mirror drives the same device path."""
+    from simbuca_gb300 import ode
+    g = np.load(os.path.join(GOLD, "dp45_adaptive.npz"))
+    tag = "tight"
+    rtol, atol, t_end, h0 = g[f"{tag}_cfg"]
+    cl = ode.IonCloud(g[f"{tag}_pos0"], g[f"{tag}_vel0"], g[f"{tag}_mass"], g[f"{tag}_charge"])
+    od = ode.OdeVars()
+    od.Init_ode(5, h0, True)
+    od.rk_rtol, od.rk_atol = rtol, atol
+    od.forcev.coulomb_interaction = True
+    od.forcev.trap_param.E_kick = 0.0
+    acc = ode.force(cl, od)
+    ref = oracle.force(cl.pos2, cl.vel2, cl.mass, cl.charge, 0.0, paul_fp(TRAPP))
+    np.testing.assert_allclose(acc, ref, rtol=1e-12)
+    while cl.lifetime < t_end:
+        ode.step(cl, od)
+    np.testing.assert_allclose(cl.pos, g[f"{tag}_pos"], rtol=1e-9, atol=1e-15)
