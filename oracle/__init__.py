@@ -82,6 +82,8 @@ def lib():
         L.orc_dp45_run.restype = ctypes.c_int64
         L.orc_error_succes.argtypes = [ctypes.c_double, ctypes.POINTER(OrcCtrl)]
         L.orc_moments.argtypes = [ctypes.c_int, _dp, _dp, _dp, _dp]
+        L.orc_dp45_replay.argtypes = [ctypes.c_int, _dp, _dp, _dp, _ip, ctypes.c_void_p, _dp,
+                                      _dp, ctypes.c_int]
         _orc = L
     return _orc
 
@@ -147,6 +149,20 @@ def dp45_run(pos, vel, mass, charge, fp, *, rtol, atol, h0, t0, t_end, adaptive=
                             int(hist_cap))
     n_rec = min(max(nh, 0), hist_cap)
     return pos, vel, c, hist[:n_rec], nh
+
+
+def dp45_replay(pos, vel, mass, charge, fp, ts, hs):
+    """Fixed steps with the schedule (ts[k], hs[k]); returns (pos, vel)."""
+    pos = np.array(pos, np.float64, order="C")
+    vel = np.array(vel, np.float64, order="C")
+    mass = np.ascontiguousarray(mass, np.float64)
+    charge = np.ascontiguousarray(charge, np.int32)
+    ts = np.ascontiguousarray(ts, np.float64)
+    hs = np.ascontiguousarray(hs, np.float64)
+    st = lib().orc_dp45_replay(len(mass), _d(pos), _d(vel), _d(mass), _i(charge),
+                               ctypes.byref(fp), _d(ts), _d(hs), len(ts))
+    assert st == 0
+    return pos, vel
 
 
 def moments(pos, vel, mass):

@@ -471,6 +471,31 @@ out:
     return nh;
 }
 
+int orc_dp45_replay(int n, double* pos, double* vel, const double* mass, const int* charge,
+                    const sg_field_params* fp, const double* ts, const double* hs, int nsteps) {
+    double* k = (double*)malloc(sizeof(double) * 7 * 6 * (size_t)n);
+    double* pos2 = (double*)malloc(sizeof(double) * 3 * (size_t)n);
+    double* vel2 = (double*)malloc(sizeof(double) * 3 * (size_t)n);
+    double* derivs = (double*)malloc(sizeof(double) * 3 * (size_t)n);
+    if (!k || !pos2 || !vel2 || !derivs) {
+        free(k); free(pos2); free(vel2); free(derivs);
+        return SG_BAD_ARG;
+    }
+    orc_ctrl c;
+    memset(&c, 0, sizeof c);
+    c.rtol = 1e-9;
+    c.atol = 1e-15;
+    for (int s = 0; s < nsteps; s++) {
+        c.t = ts[s];
+        c.h = hs[s];
+        orc_dp45_attempt(n, pos, vel, mass, charge, fp, &c, pos2, vel2, k, derivs);
+        memcpy(pos, pos2, sizeof(double) * 3 * (size_t)n);
+        memcpy(vel, vel2, sizeof(double) * 3 * (size_t)n);
+    }
+    free(k); free(pos2); free(vel2); free(derivs);
+    return SG_OK;
+}
+
 /* Cloud moments.  Temperature restates IonCloud::Temperature (bin/ioncloud.cpp:316-335):
  * T_r = (0.5/N sum m (vx^2+vy^2)) * 2/(3 kb), T_z = (0.5/N sum m vz^2) * 2/(3 kb). */
 void orc_moments(int n, const double* pos, const double* vel, const double* mass,

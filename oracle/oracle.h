@@ -87,6 +87,12 @@ int64_t orc_dp45_run(int n, double* pos, double* vel, const double* mass,
                      const int* charge, const sg_field_params* fp, orc_ctrl* c,
                      int64_t max_steps, double* hist, int64_t hist_cap);
 
+/* Fixed steps with a given schedule: step k starts at ts[k] with size hs[k] (no error
+ * control), as the reference's step() does with change_stepsize false.  Used to
+ * replay the step sequence another implementation accepted. */
+int orc_dp45_replay(int n, double* pos, double* vel, const double* mass, const int* charge,
+                    const sg_field_params* fp, const double* ts, const double* hs, int nsteps);
+
 /* Moments of one cloud: out[12] as sg_batch_moments. */
 void orc_moments(int n, const double* pos, const double* vel, const double* mass,
                  double* out);

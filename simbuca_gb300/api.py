@@ -28,6 +28,7 @@ class Context:
         h = ctypes.c_void_p()
         check(self._L.sg_create(int(device), ctypes.byref(h)), "sg_create")
         self._h = h
+        self._batch_gen = 0  # a context holds one batch; older Batch objects go stale
 
     @property
     def handle(self):
@@ -103,11 +104,17 @@ class Context:
 
 
 class Batch:
-    """Resident clouds advanced on the device by the Dormand-Prince loop."""
+    """Resident clouds advanced on the device by the Dormand-Prince loop.
+
+    A Context holds one batch at a time: creating a new Batch on the same Context
+    releases the previous one, whose methods then raise.  Use one Context per batch
+    to keep several alive."""
 
     def __init__(self, ctx: Context, counts, fields, odes, precision=abi.SG_PREC_FP64):
         self.ctx = ctx
         self._L = ctx._L
+        ctx._batch_gen += 1
+        self._gen = ctx._batch_gen
         self.counts = np.ascontiguousarray(counts, dtype=np.int32)
         self.n_clouds = len(self.counts)
         self.n = int(self.counts.sum())
@@ -119,7 +126,12 @@ class Batch:
                                       self.precision), "sg_batch_create")
         self._info = (StepInfo * self.n_clouds)()
 
+    def _live(self):
+        if self.ctx._batch_gen != self._gen:
+            raise RuntimeError("this Batch was replaced by a newer Batch on the same Context")
+
     def upload(self, pos, vel, mass, charge):
+        self._live()
         pos, vel, mass = _f64(pos), _f64(vel), _f64(mass)
         charge = np.ascontiguousarray(charge, dtype=np.int32)
         assert pos.shape == (self.n, 3) and vel.shape == (self.n, 3)
@@ -127,11 +139,13 @@ class Batch:
                                       iptr(charge)), "sg_batch_upload")
 
     def set_state(self, pos, vel):
+        self._live()
         pos, vel = _f64(pos), _f64(vel)
         check(self._L.sg_batch_set_state(self.ctx.handle, dptr(pos), dptr(vel)),
               "sg_batch_set_state")
 
     def download(self, pos=None, vel=None):
+        self._live()
         pos = np.empty((self.n, 3)) if pos is None else pos
         vel = np.empty((self.n, 3)) if vel is None else vel
         check(self._L.sg_batch_download(self.ctx.handle, dptr(pos), dptr(vel)),
@@ -139,33 +153,40 @@ class Batch:
         return pos, vel
 
     def attempts(self, n: int):
+        self._live()
         check(self._L.sg_batch_attempts(self.ctx.handle, int(n)), "sg_batch_attempts")
 
     def step(self, raise_on_error=True):
+        self._live()
         st = self._L.sg_dp45_step(self.ctx.handle, self._info)
         if raise_on_error:
             check(st, "sg_dp45_step")
         return [s.as_dict() for s in self._info], st
 
     def run(self, max_attempts: int = 1 << 62, raise_on_error=True):
+        self._live()
         st = self._L.sg_batch_run(self.ctx.handle, int(max_attempts), self._info)
         if raise_on_error:
             check(st, "sg_batch_run")
         return [s.as_dict() for s in self._info], st
 
     def info(self):
+        self._live()
         check(self._L.sg_batch_info(self.ctx.handle, self._info), "sg_batch_info")
         return [s.as_dict() for s in self._info]
 
     def moments(self):
+        self._live()
         out = np.empty((self.n_clouds, 12))
         check(self._L.sg_batch_moments(self.ctx.handle, dptr(out)), "sg_batch_moments")
         return out
 
     def set_field(self, cloud: int, fp: FieldParams):
+        self._live()
         check(self._L.sg_batch_set_field(self.ctx.handle, int(cloud), ctypes.byref(fp)),
               "sg_batch_set_field")
 
     def set_t_end(self, cloud: int, t_end: float):
+        self._live()
         check(self._L.sg_batch_set_t_end(self.ctx.handle, int(cloud), float(t_end)),
               "sg_batch_set_t_end")

@@ -30,10 +30,10 @@ struct Problem {
     SgRowBlock* drows = nullptr;
     SgWorkItem* ditems = nullptr;
     double *y = nullptr, *ys = nullptr, *k = nullptr, *part = nullptr, *coul1 = nullptr,
-           *coul7 = nullptr, *kq = nullptr, *qm = nullptr, *qd = nullptr, *mass = nullptr,
+           *coul7 = nullptr, *coulS = nullptr, *kq = nullptr, *qm = nullptr, *qd = nullptr, *mass = nullptr,
            *c64 = nullptr, *err_part = nullptr, *mom = nullptr, *stage = nullptr;
     float* c32 = nullptr;
-    int* flags = nullptr;  // [0] error word, [1] hold-on-accept
+    int* flags = nullptr;  // [0] error word, [1] hold-on-accept, [2] FP32c fix-up count
     SgCtrl* hctrl = nullptr;  // pinned mirror of dctrl
     double interactions = 0.0;  // per Coulomb evaluation, all clouds
     std::vector<double> cloud_inter;
@@ -91,7 +91,7 @@ void free_problem(Problem& P) {
     cudaFree(P.dctrl);
     cudaFree(P.drows);
     cudaFree(P.ditems);
-    double* ds[] = {P.y, P.ys, P.k, P.part, P.coul1, P.coul7, P.kq, P.qm,
+    double* ds[] = {P.y, P.ys, P.k, P.part, P.coul1, P.coul7, P.coulS, P.kq, P.qm,
                     P.qd, P.mass, P.c64, P.err_part, P.mom, P.stage};
     for (double* d : ds) cudaFree(d);
     cudaFree(P.c32);
@@ -238,7 +238,8 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(dalloc(&P.y, 6 * N));
     CK(dalloc(&P.ys, 6 * N));
     CK(dalloc(&P.k, 42 * N));
-    CK(dalloc(&P.part, (size_t)std::max(P.max_slots, 1) * 3 * NP));
+    CK(dalloc(&P.part, (size_t)std::max(P.max_slots, 1) * 4 * NP));
+    CK(dalloc(&P.coulS, 3 * N));
     CK(dalloc(&P.coul1, 3 * N));
     CK(dalloc(&P.coul7, 3 * N));
     CK(dalloc(&P.kq, N));
@@ -253,7 +254,8 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(dalloc(&P.flags, 4));
     CK(cudaMemset(P.flags, 0, 4 * sizeof(int)));
     CK(cudaMemset(P.coul1, 0, 3 * N * sizeof(double)));
-    CK(cudaMemset(P.part, 0, (size_t)std::max(P.max_slots, 1) * 3 * NP * sizeof(double)));
+    CK(cudaMemset(P.part, 0, (size_t)std::max(P.max_slots, 1) * 4 * NP * sizeof(double)));
+    CK(cudaMemset(P.coulS, 0, 3 * N * sizeof(double)));
     CK(cudaMallocHost((void**)&P.hctrl, sizeof(SgCtrl) * (size_t)std::max(P.n_clouds, 1)));
     CK(cudaMemcpy(P.drows, P.hrows.data(), sizeof(SgRowBlock) * P.hrows.size(),
                   cudaMemcpyHostToDevice));
@@ -271,7 +273,7 @@ SgDpArgs dp_args(Problem& P) {
     a.y = P.y;
     a.ys = P.ys;
     a.k = P.k;
-    a.part = P.part;
+    a.coulS = P.coulS;
     a.coul1 = P.coul1;
     a.coul7 = P.coul7;
     a.kq = P.kq;
@@ -311,7 +313,10 @@ void flush_timing(sg_ctx* ctx) {
     ctx->pending.clear();
 }
 
-int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter) {
+// Coulomb sums of the current Coulomb inputs into out[3][N]: the pair kernel over the
+// work items, then the per-ion reduction of the partial-sum slots (with the FP32c
+// conditioning fix-up).
+int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter, double* out) {
     if (!P.any_coulomb || P.n_items == 0) return SG_OK;
     SgCoulombArgs ca;
     ca.c32 = P.c32;
@@ -329,7 +334,8 @@ int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter) {
         tl.b = take_event(ctx);
         CK(cudaEventRecord(tl.a, ctx->stream));
     }
-    if (P.precision == SG_PREC_FP32C)
+    const bool f32 = P.precision == SG_PREC_FP32C;
+    if (f32)
         CK(sg_launch_coulomb_fp32c(ca, ctx->stream));
     else
         CK(sg_launch_coulomb_fp64(ca, ctx->stream));
@@ -337,6 +343,8 @@ int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter) {
         CK(cudaEventRecord(tl.b, ctx->stream));
         ctx->pending.push_back(tl);
     }
+    CK(sg_launch_coulomb_reduce(ca, P.drows, P.n_rows, f32 ? 1 : 0, out, P.n, P.flags + 2,
+                                ctx->stream));
     return SG_OK;
 }
 
@@ -354,7 +362,7 @@ int enqueue_attempt(sg_ctx* ctx, Problem& P) {
     const double inter = ctx->timing ? active_interactions(P) : 0.0;
     CK(sg_dp_stage(a, 1, P.n_rows, ctx->stream));
     for (int s = 2; s <= 7; s++) {
-        int st = launch_coulomb(ctx, P, true, inter);
+        int st = launch_coulomb(ctx, P, true, inter, P.coulS);
         if (st != SG_OK) return st;
         CK(sg_dp_stage(a, s, P.n_rows, ctx->stream));
     }
@@ -586,7 +594,7 @@ int sg_coulomb_accel(sg_ctx* ctx, int precision, int n, const double* pos, const
     CK(cudaMemcpyAsync(P.kq, kq, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     st = upload_state(ctx, P, pos, nullptr);
     if (st != SG_OK) return st;
-    st = launch_coulomb(ctx, P, false, (double)n * (n - 1));
+    st = launch_coulomb(ctx, P, false, (double)n * (n - 1), P.coulS);
     if (st != SG_OK) return st;
     SgDpArgs a = dp_args(P);
     CK(sg_force_finish(a, 0.0, 0, P.stage, P.n_rows, ctx->stream));
@@ -617,7 +625,7 @@ int sg_force(sg_ctx* ctx, int precision, int n, const double* pos, const double*
     st = upload_state(ctx, P, pos, vel);
     if (st != SG_OK) return st;
     if (fp->flags & SG_F_COULOMB) {
-        st = launch_coulomb(ctx, P, false, (double)n * (n - 1));
+        st = launch_coulomb(ctx, P, false, (double)n * (n - 1), P.coulS);
         if (st != SG_OK) return st;
     }
     SgDpArgs a = dp_args(P);
@@ -700,10 +708,8 @@ int sg_batch_upload(sg_ctx* ctx, const double* pos, const double* vel, const dou
     int st = upload_state(ctx, P, pos, vel);
     if (st != SG_OK) return st;
     // stage-1 Coulomb sum of the initial state
-    st = launch_coulomb(ctx, P, true, active_interactions(P));
+    st = launch_coulomb(ctx, P, true, active_interactions(P), P.coul1);
     if (st != SG_OK) return st;
-    SgDpArgs a = dp_args(P);
-    CK(sg_reduce_slots(a, P.coul1, P.n_rows, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     flush_timing(ctx);
     P.uploaded = true;
@@ -719,10 +725,8 @@ int sg_batch_set_state(sg_ctx* ctx, const double* pos, const double* vel) {
     CK(cudaSetDevice(ctx->device));
     int st = upload_state(ctx, P, pos, vel);
     if (st != SG_OK) return st;
-    st = launch_coulomb(ctx, P, true, active_interactions(P));
+    st = launch_coulomb(ctx, P, true, active_interactions(P), P.coul1);
     if (st != SG_OK) return st;
-    SgDpArgs a = dp_args(P);
-    CK(sg_reduce_slots(a, P.coul1, P.n_rows, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     flush_timing(ctx);
     return SG_OK;

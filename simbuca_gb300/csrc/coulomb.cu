@@ -260,7 +260,6 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
     const float* X = c32;
     const float* Y = c32 + npad_total;
     const float* Z = c32 + 2 * (size_t)npad_total;
-    const float* Q = c32 + 3 * (size_t)npad_total;
     const float* XL = c32 + 4 * (size_t)npad_total;
     const float* YL = c32 + 5 * (size_t)npad_total;
     const float* ZL = c32 + 6 * (size_t)npad_total;
@@ -284,11 +283,13 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
         corr[1][li] = 0.0;
         corr[2][li] = 0.0;
     }
-    float ks[IPT][3], kc[IPT][3];
+    float ks[IPT][3], kc[IPT][3], s2[IPT];
 #pragma unroll
-    for (int k = 0; k < IPT; k++)
+    for (int k = 0; k < IPT; k++) {
+        s2[k] = 0.f;
 #pragma unroll
         for (int c = 0; c < 3; c++) ks[k][c] = kc[k][c] = 0.f;
+    }
 
     const int ntiles = (it.nj + T - 1) / T;
     bool ok = true;
@@ -356,11 +357,16 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
         for (int k = 0; k < IPT; k++) {
             float a, b;
             upk(ax[k], a, b);
-            kahan_add(ks[k][0], kc[k][0], __fadd_rn(a, b));
+            const float tx_ = __fadd_rn(a, b);
             upk(ay[k], a, b);
-            kahan_add(ks[k][1], kc[k][1], __fadd_rn(a, b));
+            const float ty_ = __fadd_rn(a, b);
             upk(az[k], a, b);
-            kahan_add(ks[k][2], kc[k][2], __fadd_rn(a, b));
+            const float tz_ = __fadd_rn(a, b);
+            kahan_add(ks[k][0], kc[k][0], tx_);
+            kahan_add(ks[k][1], kc[k][1], ty_);
+            kahan_add(ks[k][2], kc[k][2], tz_);
+            // sum of squared tile sums: estimates sum_j |f_ij|^2 for the conditioning test
+            s2[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2[k])));
         }
         // close pairs of this tile: FP64 term in, capped FP32 term out
 #pragma unroll
@@ -384,12 +390,13 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
         }
     }
     if (!ok) return;
-    double* P = part + (size_t)it.slot * 3 * npad_total;
+    double* P = part + (size_t)it.slot * 4 * npad_total;
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
         if (ipad[k] < 0) continue;
         const int li = tid + k * NT;
         const int ig = ipad[k];
+        P[3 * (size_t)npad_total + ig] = (double)s2[k];
         // P_i = sum q_j (x_i - x_j)/r^3 = -invL^2 sum w (u_j - u_i) + close-pair terms
         P[ig] = -invL2 * ((double)ks[k][0] - (double)kc[k][0]) + corr[0][li];
         P[npad_total + ig] = -invL2 * ((double)ks[k][1] - (double)kc[k][1]) + corr[1][li];
@@ -463,13 +470,115 @@ __global__ void __launch_bounds__(NT) coulomb_fp64_kernel(const double* __restri
             }
         }
     }
-    double* P = part + (size_t)it.slot * 3 * npad_total;
+    double* P = part + (size_t)it.slot * 4 * npad_total;
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
         if (ipad[k] < 0) continue;
+        P[3 * (size_t)npad_total + ipad[k]] = 0.0;
         P[ipad[k]] = ax[k];
         P[npad_total + ipad[k]] = ay[k];
         P[2 * (size_t)npad_total + ipad[k]] = az[k];
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// Sum of the partial-sum slots of every ion into out[3][N] (SI, m^-2).
+//
+// FP32c only: the conditioning test.  sqrt(s2) estimates sqrt(sum_j |f_ij|^2) of the
+// FP32 terms; the rounding of those terms is random, so the error of P_i is about
+// 2.5e-7 * sqrt(s2).  An ion whose FP32 terms cancel strongly (sqrt(s2) > 1.5 |P_i|,
+// e.g. near the centre of a cloud) gets its dominant pairs -- those with
+// |f_ij| > 0.1 |P_i| that the main kernel did not already take in FP64 -- re-evaluated
+// in FP64 here, one warp per flagged ion over the cloud's j-range.
+// ---------------------------------------------------------------------------
+constexpr double kKappa2 = 2.25;
+
+template <bool F32>
+__global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
+    const SgRowBlock* __restrict__ rows, const SgCloud* __restrict__ clouds,
+    const SgCtrl* __restrict__ ctrl, const double* __restrict__ part,
+    const float* __restrict__ c32, const double* __restrict__ c64, int npad_total,
+    double* __restrict__ out, int n_total, int* __restrict__ counters) {
+    __shared__ int list[SG_ROWS];
+    __shared__ int nl;
+    __shared__ double cx[SG_ROWS], cy[SG_ROWS], cz[SG_ROWS], pm[SG_ROWS];
+    const SgRowBlock rb = rows[blockIdx.x];
+    if (ctrl != nullptr &&
+        (ctrl[rb.cloud].done || ctrl[rb.cloud].hold || ctrl[rb.cloud].status != SG_OK))
+        return;
+    const SgCloud& cl = clouds[rb.cloud];
+    if (!(cl.fp.flags & SG_F_COULOMB)) return;
+    const int li = threadIdx.x;
+    if (li == 0) nl = 0;
+    __syncthreads();
+    const bool act = li < rb.n;
+    const int i = rb.i0 + (act ? li : 0);
+    const int ig = cl.poff + (i - cl.off);
+    const size_t NP = (size_t)npad_total;
+    double px = 0.0, py = 0.0, pz = 0.0, s2 = 0.0;
+    if (act) {
+        for (int sl = 0; sl < cl.nslots; sl++) {
+            const double* P = part + (size_t)sl * 4 * NP;
+            px += P[ig];
+            py += P[NP + ig];
+            pz += P[2 * NP + ig];
+            s2 += P[3 * NP + ig];
+        }
+    }
+    if (F32) {
+        cx[li] = cy[li] = cz[li] = 0.0;
+        const double pf = sqrt(px * px + py * py + pz * pz) * (cl.L * cl.L);  // frame units
+        pm[li] = pf;
+        if (act && s2 > kKappa2 * pf * pf) list[atomicAdd(&nl, 1)] = li;
+        __syncthreads();
+        const int warp = li >> 5, lane = li & 31;
+        const double invL2 = cl.invL * cl.invL;
+        const float wc = cl.wc;
+        for (int k = warp; k < nl; k += SG_ROWS / 32) {
+            const int lk = list[k];
+            const int igk = cl.poff + (rb.i0 + lk - cl.off);
+            const float thr3 = (float)pow(0.1 * pm[lk], 1.5);
+            const float xih = c32[igk], yih = c32[NP + igk], zih = c32[2 * NP + igk];
+            const float xil = c32[4 * NP + igk], yil = c32[5 * NP + igk], zil = c32[6 * NP + igk];
+            const double xi = c64[igk], yi = c64[NP + igk], zi = c64[2 * NP + igk];
+            double ax = 0.0, ay = 0.0, az = 0.0;
+            for (int j = lane; j < cl.npad; j += 32) {
+                const int jg = cl.poff + j;
+                const PairF p = pair_f32(c32[jg], c32[NP + jg], c32[2 * NP + jg], c32[4 * NP + jg],
+                                         c32[5 * NP + jg], c32[6 * NP + jg], xih, yih, zih, xil,
+                                         yil, zil);
+                if (p.y3 > thr3 && p.y3 <= wc && jg != igk) {
+                    const float wf = __fmul_rn(c32[3 * NP + jg], p.y3);
+                    const double rx = xi - c64[jg], ry = yi - c64[NP + jg], rz = zi - c64[2 * NP + jg];
+                    const double inv = 1.0 / sqrt(rx * rx + ry * ry + rz * rz);
+                    const double wq = c64[3 * NP + jg] * inv * inv * inv;
+                    ax += wq * rx + invL2 * ((double)wf * (double)p.dx);
+                    ay += wq * ry + invL2 * ((double)wf * (double)p.dy);
+                    az += wq * rz + invL2 * ((double)wf * (double)p.dz);
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                ax += __shfl_down_sync(0xffffffffu, ax, o);
+                ay += __shfl_down_sync(0xffffffffu, ay, o);
+                az += __shfl_down_sync(0xffffffffu, az, o);
+            }
+            if (lane == 0) {
+                cx[lk] = ax;
+                cy[lk] = ay;
+                cz[lk] = az;
+            }
+        }
+        __syncthreads();
+        if (li == 0 && nl > 0 && counters != nullptr) atomicAdd(counters, nl);
+        px += cx[li];
+        py += cy[li];
+        pz += cz[li];
+    }
+    if (act) {
+        out[i] = px;
+        out[(size_t)n_total + i] = py;
+        out[2 * (size_t)n_total + i] = pz;
     }
 }
 
@@ -487,5 +596,20 @@ cudaError_t sg_launch_coulomb_fp64(const SgCoulombArgs& a, cudaStream_t s) {
     if (a.n_items <= 0) return cudaSuccess;
     coulomb_fp64_kernel<SG_C64_THREADS, SG_C64_IPT><<<a.n_items, SG_C64_THREADS, 0, s>>>(
         a.c64, a.items, a.ctrl, a.part, a.npad_total);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* rows, int n_rows,
+                                     int fp32c, double* out, int n_total, int* counters,
+                                     cudaStream_t s) {
+    if (n_rows <= 0) return cudaSuccess;
+    if (fp32c)
+        coulomb_reduce_kernel<true><<<n_rows, SG_ROWS, 0, s>>>(rows, a.clouds, a.ctrl, a.part, a.c32,
+                                                              a.c64, a.npad_total, out, n_total,
+                                                              counters);
+    else
+        coulomb_reduce_kernel<false><<<n_rows, SG_ROWS, 0, s>>>(rows, a.clouds, a.ctrl, a.part,
+                                                               a.c32, a.c64, a.npad_total, out,
+                                                               n_total, counters);
     return cudaGetLastError();
 }

@@ -91,12 +91,9 @@ __global__ void __launch_bounds__(SG_ROWS) dp_stage_kernel(DpArgs a) {
                 cy = a.coul1[N + i];
                 cz = a.coul1[2 * N + i];
             } else {
-                for (int sl = 0; sl < cl.nslots; sl++) {
-                    const double* P = a.part + (size_t)sl * 3 * a.npad;
-                    cx += P[ig];
-                    cy += P[a.npad + ig];
-                    cz += P[2 * (size_t)a.npad + ig];
-                }
+                cx = a.coulS[i];
+                cy = a.coulS[N + i];
+                cz = a.coulS[2 * N + i];
                 if (S == 7) {
                     a.coul7[i] = cx;
                     a.coul7[N + i] = cy;
@@ -287,27 +284,6 @@ __global__ void __launch_bounds__(SG_ROWS) coords_from_state_kernel(DpArgs a,
     }
 }
 
-// Sum of the partial-sum slots into dst[3][N] (stage-1 Coulomb sum after set-up).
-__global__ void __launch_bounds__(SG_ROWS) reduce_slots_kernel(DpArgs a, double* dst) {
-    const SgRowBlock rb = a.rows[blockIdx.x];
-    const SgCloud& cl = a.clouds[rb.cloud];
-    const int li = threadIdx.x;
-    if (li >= rb.n) return;
-    const int i = rb.i0 + li;
-    const int ig = cl.poff + (i - cl.off);
-    const size_t N = (size_t)a.n;
-    double cx = 0.0, cy = 0.0, cz = 0.0;
-    for (int sl = 0; sl < cl.nslots; sl++) {
-        const double* P = a.part + (size_t)sl * 3 * a.npad;
-        cx += P[ig];
-        cy += P[a.npad + ig];
-        cz += P[2 * (size_t)a.npad + ig];
-    }
-    dst[i] = cx;
-    dst[N + i] = cy;
-    dst[2 * N + i] = cz;
-}
-
 // Stand-alone force: out[i][c] (AoS) = field(t) + kq_i * sum_slots P (if Coulomb).
 __global__ void __launch_bounds__(SG_ROWS) force_finish_kernel(DpArgs a, double t,
                                                                int with_field,
@@ -317,16 +293,12 @@ __global__ void __launch_bounds__(SG_ROWS) force_finish_kernel(DpArgs a, double 
     const int li = threadIdx.x;
     if (li >= rb.n) return;
     const int i = rb.i0 + li;
-    const int ig = cl.poff + (i - cl.off);
     const size_t N = (size_t)a.n;
     double cx = 0.0, cy = 0.0, cz = 0.0;
     if (cl.fp.flags & SG_F_COULOMB) {
-        for (int sl = 0; sl < cl.nslots; sl++) {
-            const double* P = a.part + (size_t)sl * 3 * a.npad;
-            cx += P[ig];
-            cy += P[a.npad + ig];
-            cz += P[2 * (size_t)a.npad + ig];
-        }
+        cx = a.coulS[i];
+        cy = a.coulS[N + i];
+        cz = a.coulS[2 * N + i];
     }
     double fx = 0.0, fy = 0.0, fz = 0.0;
     if (with_field)
@@ -433,11 +405,6 @@ cudaError_t sg_dp_commit(const SgDpArgs& a, int n_rows, cudaStream_t st) {
 
 cudaError_t sg_coords_from_state(const SgDpArgs& a, const double* q, int n_rows, cudaStream_t st) {
     coords_from_state_kernel<<<n_rows, SG_ROWS, 0, st>>>(a, q);
-    return cudaGetLastError();
-}
-
-cudaError_t sg_reduce_slots(const SgDpArgs& a, double* dst, int n_rows, cudaStream_t st) {
-    reduce_slots_kernel<<<n_rows, SG_ROWS, 0, st>>>(a, dst);
     return cudaGetLastError();
 }
 

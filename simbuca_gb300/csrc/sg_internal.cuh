@@ -135,7 +135,7 @@ struct SgDpArgs {
     double* y;            // [6][N]
     double* ys;           // [6][N]
     double* k;            // [7][6][N]
-    const double* part;   // [slots][3][Npad]
+    const double* coulS;  // [3][N] Coulomb sum of the stage being finished
     double* coul1;        // [3][N]
     double* coul7;        // [3][N]
     const double* kq;     // [N]
@@ -157,7 +157,6 @@ cudaError_t sg_clear_hold(SgCtrl* ctrl, int n_clouds, cudaStream_t st);
 int sg_probe_iters(int which);
 cudaError_t sg_dp_commit(const SgDpArgs& a, int n_rows, cudaStream_t st);
 cudaError_t sg_coords_from_state(const SgDpArgs& a, const double* q, int n_rows, cudaStream_t st);
-cudaError_t sg_reduce_slots(const SgDpArgs& a, double* dst, int n_rows, cudaStream_t st);
 cudaError_t sg_force_finish(const SgDpArgs& a, double t, int with_field, double* out, int n_rows,
                             cudaStream_t st);
 cudaError_t sg_aos_to_soa(const double* pos, const double* vel, double* y, int n, cudaStream_t st);
@@ -175,10 +174,13 @@ struct SgCoulombArgs {
     int n_items;
     const SgCloud* clouds;
     const SgCtrl* ctrl;      // may be null (stand-alone calls)
-    double* part;            // [slots][3][Npad]
+    double* part;            // [slots][4][Npad]: x, y, z sums and the FP32c s2 estimate
     int npad_total;
     int* errword;
 };
 
 cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s);
 cudaError_t sg_launch_coulomb_fp64(const SgCoulombArgs& a, cudaStream_t s);
+cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* rows, int n_rows,
+                                     int fp32c, double* out, int n_total, int* counters,
+                                     cudaStream_t s);

@@ -31,3 +31,32 @@ def rel_err_per_ion(a, ref):
 def summary(e):
     return {"max": float(e.max()), "p99": float(np.percentile(e, 99)),
             "median": float(np.median(e))}
+
+
+def run_recording(batch, max_calls=100000):
+    """Advance a Batch one accepted step per cloud at a time (sg_dp45_step) until every
+    cloud is done; returns per-cloud arrays of accepted (t_start, h) and the last info."""
+    n = batch.n_clouds
+    ts = [[] for _ in range(n)]
+    hs = [[] for _ in range(n)]
+    prev = batch.info()
+    for _ in range(max_calls):
+        if all(s["done"] for s in prev):
+            break
+        cur, st = batch.step(raise_on_error=False)
+        for c in range(n):
+            if cur[c]["steps"] > prev[c]["steps"]:
+                ts[c].append(prev[c]["t"])
+                hs[c].append(cur[c]["h_last"])
+        prev = cur
+        if st != 0:
+            break
+    return [np.array(x) for x in ts], [np.array(x) for x in hs], prev
+
+
+def replay_error(cloud, fp, ts, hs, pos, vel):
+    """Relative max difference of (pos, vel) against the oracle replaying (ts, hs)."""
+    pr, vr = oracle.dp45_replay(cloud.pos, cloud.vel, cloud.mass, cloud.charge, fp, ts, hs)
+    ep = np.abs(pos - pr).max() / np.abs(pr).max()
+    ev = np.abs(vel - vr).max() / np.abs(vr).max()
+    return ep, ev
