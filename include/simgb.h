@@ -180,6 +180,12 @@ int sg_batch_set_t_end(sg_ctx* ctx, int cloud, double t_end);
 int sg_set_kernel_timing(sg_ctx* ctx, int on);
 int sg_kernel_timing(sg_ctx* ctx, double* coulomb_ms, int64_t* coulomb_launches,
                      double* coulomb_interactions);
+/* FP32c conditioning fix-ups (ions whose dominant pairs were re-evaluated in FP64 by
+ * the reduction kernel) since the last call; resets the count. */
+int sg_fixup_count(sg_ctx* ctx, int64_t* count);
+/* Launch shape of the FP32c Coulomb kernel for batches and calls created afterwards:
+ * 0 = 128 threads x 4 ions (default), 1 = 128 x 2, 2 = 256 x 2, 3 = 64 x 4. */
+int sg_set_coulomb_variant(sg_ctx* ctx, int variant);
 /* Capture the attempt sequence in a CUDA graph (1) or launch it directly (0). */
 int sg_set_use_graph(sg_ctx* ctx, int on);
 /* Host-side timer on the context stream (CUDA events). */

@@ -99,6 +99,14 @@ class Context:
                                        ctypes.byref(inter)), "sg_kernel_timing")
         return {"coulomb_ms": ms.value, "coulomb_launches": n.value, "interactions": inter.value}
 
+    def fixup_count(self) -> int:
+        c = ctypes.c_int64()
+        check(self._L.sg_fixup_count(self._h, ctypes.byref(c)), "sg_fixup_count")
+        return c.value
+
+    def set_coulomb_variant(self, v: int):
+        check(self._L.sg_set_coulomb_variant(self._h, int(v)), "sg_set_coulomb_variant")
+
     def set_use_graph(self, on: bool):
         check(self._L.sg_set_use_graph(self._h, int(bool(on))), "sg_set_use_graph")
 

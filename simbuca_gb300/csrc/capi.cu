@@ -18,6 +18,7 @@ namespace {
 // ---------------------------------------------------------------------------
 struct Problem {
     int n_clouds = 0, n = 0, npad = 0, precision = 0, n_rows = 0, n_items = 0, max_slots = 0;
+    int variant = 0;  // FP32c launch shape the items were planned for
     bool any_coulomb = false;
     bool uploaded = false;
     std::vector<SgCloud> hc;
@@ -51,6 +52,7 @@ struct sg_ctx {
     cudaStream_t stream = nullptr;
     int last_err = 0;
     int n_sm = 148;
+    int c32_variant = 0;
     Problem batch;
     Problem solo;
     bool timing = false;
@@ -141,8 +143,8 @@ void plan(Problem& P, int n_sm) {
     P.n_rows = (int)P.hrows.size();
 
     const bool f32 = P.precision == SG_PREC_FP32C;
-    const int ib = f32 ? SG_C32_IB : SG_C64_IB;
-    const int per_sm = f32 ? 3 : 4;
+    const int ib = f32 ? sg_coulomb_fp32c_ib(P.variant) : SG_C64_IB;
+    const int per_sm = f32 ? std::max(1, 2048 / ib) : 4;
     const double conc = (double)n_sm * per_sm;
     double total = 0.0;
     for (int c = 0; c < C; c++)
@@ -328,6 +330,7 @@ int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter, double
     ca.part = P.part;
     ca.npad_total = P.npad;
     ca.errword = P.flags;
+    ca.variant = P.variant;
     TimedLaunch tl{nullptr, nullptr, inter};
     if (ctx->timing) {
         tl.a = take_event(ctx);
@@ -482,12 +485,14 @@ int check_fp(const sg_field_params* fp) {
 int solo_prepare(sg_ctx* ctx, int n, int precision, const sg_field_params& fp) {
     Problem& P = ctx->solo;
     const bool same = P.n_clouds == 1 && P.n == n && P.precision == precision &&
+                      P.variant == ctx->c32_variant &&
                       ((P.hc[0].fp.flags & SG_F_COULOMB) == (fp.flags & SG_F_COULOMB));
     if (!same) {
         free_problem(P);
         P.n_clouds = 1;
         P.counts.assign(1, n);
         P.precision = precision;
+        P.variant = ctx->c32_variant;
         P.hc.assign(1, SgCloud());
         P.hc[0].fp = fp;
         plan(P, ctx->n_sm);
@@ -658,6 +663,7 @@ int sg_batch_create(sg_ctx* ctx, int n_clouds, const int* counts, const sg_field
     P.n_clouds = n_clouds;
     P.counts.assign(counts, counts + n_clouds);
     P.precision = precision;
+    P.variant = ctx->c32_variant;
     P.hc.assign(n_clouds, SgCloud());
     for (int c = 0; c < n_clouds; c++) P.hc[c].fp = fp[c];
     plan(P, ctx->n_sm);
@@ -868,6 +874,27 @@ int sg_kernel_timing(sg_ctx* ctx, double* coulomb_ms, int64_t* launches, double*
     if (coulomb_ms) *coulomb_ms = ctx->coul_ms;
     if (launches) *launches = ctx->coul_launches;
     if (inter) *inter = ctx->coul_inter;
+    return SG_OK;
+}
+
+int sg_fixup_count(sg_ctx* ctx, int64_t* count) {
+    if (!ctx || !count) return SG_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    *count = 0;
+    Problem* ps[2] = {&ctx->batch, &ctx->solo};
+    for (Problem* P : ps) {
+        if (!P->flags) continue;
+        int v = 0;
+        CK(cudaMemcpy(&v, P->flags + 2, sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemset(P->flags + 2, 0, sizeof(int)));
+        *count += v;
+    }
+    return SG_OK;
+}
+
+int sg_set_coulomb_variant(sg_ctx* ctx, int variant) {
+    if (!ctx || variant < 0 || variant >= SG_C32_VARIANTS) return SG_BAD_ARG;
+    ctx->c32_variant = variant;
     return SG_OK;
 }
 

@@ -147,23 +147,20 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 }
 
 
-// Re-evaluates the close pairs of ion ig against one shared-memory tile: pairs whose
-// FP32 1/r^3 exceeded wc get their exact FP64 term, minus the capped FP32 term the
-// main loop already summed (a product of two floats, exact in FP64).
-__device__ __noinline__ void close_pairs(const float (*tl)[SG_TILE], int len, int j0, int ig,
-                                         f2 xh, f2 yh, f2 zh, f2 xl, f2 yl, f2 zl, float wc,
-                                         double invL2, const double* __restrict__ c64,
-                                         int npad_total, double* ox, double* oy, double* oz) {
-    float xih, yih, zih, xil, yil, zil, dummy;
-    upk(xh, xih, dummy);
-    upk(yh, yih, dummy);
-    upk(zh, zih, dummy);
-    upk(xl, xil, dummy);
-    upk(yl, yil, dummy);
-    upk(zl, zil, dummy);
+// Close pairs of one flagged ion against one shared-memory tile, evaluated by the
+// whole warp (lanes stride over the tile): pairs whose FP32 1/r^3 exceeded wc get their
+// exact FP64 term, minus the capped FP32 term the main loop already summed (a product
+// of two floats, exact in FP64).  Returns the warp-reduced correction (all lanes).
+__device__ __forceinline__ void close_pairs_warp(const float (*tl)[SG_TILE], int len, int j0,
+                                                 int ig, float xih, float yih, float zih,
+                                                 float xil, float yil, float zil, float wc,
+                                                 double invL2, const double* __restrict__ c64,
+                                                 int npad_total, double& ox, double& oy,
+                                                 double& oz) {
+    const int lane = threadIdx.x & 31;
     const double xi = c64[ig], yi = c64[npad_total + ig], zi = c64[2 * (size_t)npad_total + ig];
     double cx = 0.0, cy = 0.0, cz = 0.0;
-    for (int jj = 0; jj < len; jj++) {
+    for (int jj = lane; jj < len; jj += 32) {
         const PairF p = pair_f32(tl[0][jj], tl[1][jj], tl[2][jj], tl[4][jj], tl[5][jj],
                                  tl[6][jj], xih, yih, zih, xil, yil, zil);
         const int jg = j0 + jj;
@@ -180,11 +177,15 @@ __device__ __noinline__ void close_pairs(const float (*tl)[SG_TILE], int len, in
             cz += wq * rz + invL2 * ((double)wf * (double)p.dz);
         }
     }
-    *ox += cx;
-    *oy += cy;
-    *oz += cz;
+    for (int o = 16; o > 0; o >>= 1) {
+        cx += __shfl_xor_sync(0xffffffffu, cx, o);
+        cy += __shfl_xor_sync(0xffffffffu, cy, o);
+        cz += __shfl_xor_sync(0xffffffffu, cz, o);
+    }
+    ox = cx;
+    oy = cy;
+    oz = cz;
 }
-
 
 // Main loop over one shared-memory j-tile for the IPT ions of a thread: packed FP32x2
 // over consecutive j pairs.  DIAG: the tile contains the thread's own ions, whose self
@@ -192,12 +193,13 @@ __device__ __noinline__ void close_pairs(const float (*tl)[SG_TILE], int len, in
 template <int IPT, bool DIAG>
 __device__ __forceinline__ void tile_pairs(const float* tx, const float* ty, const float* tz,
                                            const float* tq, const float* txl, const float* tyl,
-                                           const float* tzl, int len, int j0, const int* ipad,
+                                           const float* tzl, int jb, int je, int j0,
+                                           const int* ipad,
                                            const f2* xh, const f2* yh, const f2* zh,
                                            const f2* xl, const f2* yl, const f2* zl, f2 tiny2,
                                            float wc, f2* ax, f2* ay, f2* az, float* y3max) {
 #pragma unroll 2
-    for (int jj = 0; jj < len; jj += 2) {
+    for (int jj = jb; jj < je; jj += 2) {
         const f2 Xj = *reinterpret_cast<const f2*>(tx + jj);
         const f2 Yj = *reinterpret_cast<const f2*>(ty + jj);
         const f2 Zj = *reinterpret_cast<const f2*>(tz + jj);
@@ -311,6 +313,9 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
     }
 
     const f2 tiny2 = pk(kTiny, kTiny);
+    // Small clouds fold partial sums every 16 j-ions so that the squared partial sums
+    // still estimate sum_j |f_ij|^2 when the whole cloud is one or two tiles.
+    const int flush_len = (cl.npad <= 2048) ? 16 : SG_TILE;
     for (int t = 0; t < ntiles; t++) {
         const int s = t % SG_STAGES;
         const uint32_t parity = (uint32_t)((t / SG_STAGES) & 1);
@@ -329,13 +334,9 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
             break;
         }
 
-        f2 ax[IPT], ay[IPT], az[IPT];
         float y3max[IPT];
 #pragma unroll
-        for (int k = 0; k < IPT; k++) {
-            ax[k] = ay[k] = az[k] = 0ull;
-            y3max[k] = 0.f;
-        }
+        for (int k = 0; k < IPT; k++) y3max[k] = 0.f;
         const float* tx = tile[s][0];
         const float* ty = tile[s][1];
         const float* tz = tile[s][2];
@@ -346,36 +347,64 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
         // The tile holding this block's own ions takes the variant that keeps the self
         // pair (dx = 0, contributes nothing) out of the close-pair flag.
         const bool diag = (j0 < it.i0 + it.ni) && (j0 + len > it.i0);
-        if (!diag)
-            tile_pairs<IPT, false>(tx, ty, tz, tq, txl, tyl, tzl, len, j0, ipad, xh, yh, zh, xl,
-                                   yl, zl, tiny2, wc, ax, ay, az, y3max);
-        else
-            tile_pairs<IPT, true>(tx, ty, tz, tq, txl, tyl, tzl, len, j0, ipad, xh, yh, zh, xl,
-                                  yl, zl, tiny2, wc, ax, ay, az, y3max);
-        // fold the tile sums into the compensated accumulators
+        for (int jb = 0; jb < len; jb += flush_len) {
+            const int je = min(len, jb + flush_len);
+            f2 ax[IPT], ay[IPT], az[IPT];
 #pragma unroll
-        for (int k = 0; k < IPT; k++) {
-            float a, b;
-            upk(ax[k], a, b);
-            const float tx_ = __fadd_rn(a, b);
-            upk(ay[k], a, b);
-            const float ty_ = __fadd_rn(a, b);
-            upk(az[k], a, b);
-            const float tz_ = __fadd_rn(a, b);
-            kahan_add(ks[k][0], kc[k][0], tx_);
-            kahan_add(ks[k][1], kc[k][1], ty_);
-            kahan_add(ks[k][2], kc[k][2], tz_);
-            // sum of squared tile sums: estimates sum_j |f_ij|^2 for the conditioning test
-            s2[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2[k])));
+            for (int k = 0; k < IPT; k++) ax[k] = ay[k] = az[k] = 0ull;
+            if (!diag)
+                tile_pairs<IPT, false>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh, zh,
+                                       xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
+            else
+                tile_pairs<IPT, true>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh, zh,
+                                      xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
+            // fold the partial sums into the compensated accumulators
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                float a, b;
+                upk(ax[k], a, b);
+                const float tx_ = __fadd_rn(a, b);
+                upk(ay[k], a, b);
+                const float ty_ = __fadd_rn(a, b);
+                upk(az[k], a, b);
+                const float tz_ = __fadd_rn(a, b);
+                kahan_add(ks[k][0], kc[k][0], tx_);
+                kahan_add(ks[k][1], kc[k][1], ty_);
+                kahan_add(ks[k][2], kc[k][2], tz_);
+                // sum of squared partial sums: estimates sum_j |f_ij|^2 (conditioning test)
+                s2[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2[k])));
+            }
         }
-        // close pairs of this tile: FP64 term in, capped FP32 term out
+        // close pairs of this tile, one flagged ion at a time by the whole warp
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
-            if (y3max[k] > wc && ipad[k] >= 0) {
-                const int li = tid + k * NT;
-                close_pairs(tile[s], len, j0, ipad[k], xh[k], yh[k], zh[k], xl[k], yl[k], zl[k],
-                            wc, invL2, c64, npad_total, &corr[0][li], &corr[1][li],
-                            &corr[2][li]);
+            unsigned m = __ballot_sync(0xffffffffu, y3max[k] > wc && ipad[k] >= 0);
+            while (m) {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                float a, dummy;
+                upk(xh[k], a, dummy);
+                const float xih = __shfl_sync(0xffffffffu, a, src);
+                upk(yh[k], a, dummy);
+                const float yih = __shfl_sync(0xffffffffu, a, src);
+                upk(zh[k], a, dummy);
+                const float zih = __shfl_sync(0xffffffffu, a, src);
+                upk(xl[k], a, dummy);
+                const float xil = __shfl_sync(0xffffffffu, a, src);
+                upk(yl[k], a, dummy);
+                const float yil = __shfl_sync(0xffffffffu, a, src);
+                upk(zl[k], a, dummy);
+                const float zil = __shfl_sync(0xffffffffu, a, src);
+                const int igs = __shfl_sync(0xffffffffu, ipad[k], src);
+                double ox, oy, oz;
+                close_pairs_warp(tile[s], len, j0, igs, xih, yih, zih, xil, yil, zil, wc, invL2,
+                                 c64, npad_total, ox, oy, oz);
+                if ((tid & 31) == src) {
+                    const int li = tid + k * NT;
+                    corr[0][li] += ox;
+                    corr[1][li] += oy;
+                    corr[2][li] += oz;
+                }
             }
         }
         __syncthreads();  // every thread is done with ring slot s
@@ -584,11 +613,34 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
 
 }  // namespace
 
+// Launch shapes of the FP32c kernel (threads per block, ions per thread); the work
+// planner sizes i-blocks as threads x ions.  Variant 0 is the default.
+static const int kC32Shapes[SG_C32_VARIANTS][2] = {{128, 4}, {128, 2}, {256, 2}, {64, 4}};
+
+int sg_coulomb_fp32c_ib(int variant) {
+    if (variant < 0 || variant >= SG_C32_VARIANTS) variant = 0;
+    return kC32Shapes[variant][0] * kC32Shapes[variant][1];
+}
+
 cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s) {
     if (a.n_items <= 0) return cudaSuccess;
-    coulomb_fp32c_kernel<SG_C32_THREADS, SG_C32_IPT><<<a.n_items, SG_C32_THREADS, 0, s>>>(
-        a.c32, a.c64, a.items,
-        a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
+    switch (a.variant) {
+        case 1:
+            coulomb_fp32c_kernel<128, 2><<<a.n_items, 128, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
+            break;
+        case 2:
+            coulomb_fp32c_kernel<256, 2><<<a.n_items, 256, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
+            break;
+        case 3:
+            coulomb_fp32c_kernel<64, 4><<<a.n_items, 64, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
+            break;
+        default:
+            coulomb_fp32c_kernel<128, 4><<<a.n_items, 128, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
+    }
     return cudaGetLastError();
 }
 

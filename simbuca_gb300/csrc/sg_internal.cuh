@@ -177,8 +177,11 @@ struct SgCoulombArgs {
     double* part;            // [slots][4][Npad]: x, y, z sums and the FP32c s2 estimate
     int npad_total;
     int* errword;
+    int variant;             // FP32c launch shape (sg_coulomb_fp32c_ib)
 };
 
+#define SG_C32_VARIANTS 4
+int sg_coulomb_fp32c_ib(int variant);
 cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s);
 cudaError_t sg_launch_coulomb_fp64(const SgCoulombArgs& a, cudaStream_t s);
 cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* rows, int n_rows,

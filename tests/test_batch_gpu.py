@@ -50,7 +50,10 @@ def test_batch_matches_single_runs(ctx, prec):
         _, _, cr, _, _ = oracle.dp45_run(c.pos, c.vel, c.mass, c.charge, w.fields[k],
                                          rtol=o.rtol, atol=o.atol, h0=o.h0, t0=0.0,
                                          t_end=o.t_end)
-        assert abs(info[k]["steps"] - cr.steps) <= 1, k
+        if prec == SG_PREC_FP64:
+            assert abs(info[k]["steps"] - cr.steps) <= 1, k
+        else:  # FP32c force noise moves the step sizes (see test_dp45_gpu)
+            assert abs(info[k]["steps"] - cr.steps) <= max(2, cr.steps // 10), k
         off += n
 
 
