@@ -184,7 +184,8 @@ int sg_kernel_timing(sg_ctx* ctx, double* coulomb_ms, int64_t* coulomb_launches,
  * the reduction kernel) since the last call; resets the count. */
 int sg_fixup_count(sg_ctx* ctx, int64_t* count);
 /* Launch shape of the FP32c Coulomb kernel for batches and calls created afterwards:
- * 0 = 128 threads x 4 ions (default), 1 = 128 x 2, 2 = 256 x 2, 3 = 64 x 4. */
+ * -1 = chosen from the cloud sizes (default), 0 = 128 threads x 4 ions,
+ * 1 = 128 x 2, 2 = 256 x 2, 3 = 64 x 4. */
 int sg_set_coulomb_variant(sg_ctx* ctx, int variant);
 /* Capture the attempt sequence in a CUDA graph (1) or launch it directly (0). */
 int sg_set_use_graph(sg_ctx* ctx, int on);

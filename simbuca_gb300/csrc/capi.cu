@@ -52,7 +52,7 @@ struct sg_ctx {
     cudaStream_t stream = nullptr;
     int last_err = 0;
     int n_sm = 148;
-    int c32_variant = 0;
+    int c32_variant = -1;  // -1: chosen per batch from the cloud sizes
     Problem batch;
     Problem solo;
     bool timing = false;
@@ -103,6 +103,17 @@ void free_problem(Problem& P) {
 }
 
 inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
+
+// Launch shape for a set of clouds when the context has no explicit choice: the
+// cloud carrying the most pair work decides.  Measured on GB300 (simbuca_gb300/tune.py):
+// 128 threads x 2 ions is fastest up to a few thousand ions per cloud (more blocks,
+// less padding of small i-ranges), 128 x 4 from ~16k ions on.
+int auto_variant(const std::vector<int>& counts, int requested) {
+    if (requested >= 0) return requested;
+    int big = 0;
+    for (int n : counts) big = std::max(big, n);
+    return big <= 8192 ? 1 : 0;
+}
 
 // Partition clouds into row blocks and Coulomb work items.  Items are sized so that
 // (a) there are several waves of blocks on the device and (b) no single item is a
@@ -485,14 +496,14 @@ int check_fp(const sg_field_params* fp) {
 int solo_prepare(sg_ctx* ctx, int n, int precision, const sg_field_params& fp) {
     Problem& P = ctx->solo;
     const bool same = P.n_clouds == 1 && P.n == n && P.precision == precision &&
-                      P.variant == ctx->c32_variant &&
+                      P.variant == auto_variant(std::vector<int>(1, n), ctx->c32_variant) &&
                       ((P.hc[0].fp.flags & SG_F_COULOMB) == (fp.flags & SG_F_COULOMB));
     if (!same) {
         free_problem(P);
         P.n_clouds = 1;
         P.counts.assign(1, n);
         P.precision = precision;
-        P.variant = ctx->c32_variant;
+        P.variant = auto_variant(P.counts, ctx->c32_variant);
         P.hc.assign(1, SgCloud());
         P.hc[0].fp = fp;
         plan(P, ctx->n_sm);
@@ -663,7 +674,7 @@ int sg_batch_create(sg_ctx* ctx, int n_clouds, const int* counts, const sg_field
     P.n_clouds = n_clouds;
     P.counts.assign(counts, counts + n_clouds);
     P.precision = precision;
-    P.variant = ctx->c32_variant;
+    P.variant = auto_variant(P.counts, ctx->c32_variant);
     P.hc.assign(n_clouds, SgCloud());
     for (int c = 0; c < n_clouds; c++) P.hc[c].fp = fp[c];
     plan(P, ctx->n_sm);
@@ -893,7 +904,7 @@ int sg_fixup_count(sg_ctx* ctx, int64_t* count) {
 }
 
 int sg_set_coulomb_variant(sg_ctx* ctx, int variant) {
-    if (!ctx || variant < 0 || variant >= SG_C32_VARIANTS) return SG_BAD_ARG;
+    if (!ctx || variant < -1 || variant >= SG_C32_VARIANTS) return SG_BAD_ARG;
     ctx->c32_variant = variant;
     return SG_OK;
 }
