@@ -37,7 +37,8 @@ enum {
     SG_TIMEOUT = 5,          /* a bounded device-side wait ran out                     */
     SG_NO_DEVICE = 6,        /* no usable CUDA device                                  */
     SG_TOO_MANY_REJECTS = 7, /* a step exceeded its reject budget                      */
-    SG_NOT_READY = 8         /* call order violated (e.g. step before upload)          */
+    SG_NOT_READY = 8,        /* call order violated (e.g. step before upload)          */
+    SG_TOO_LARGE = 9         /* size beyond a fixed capacity                           */
 };
 
 /* ---- arithmetic of the Coulomb sum ----------------------------------------- */
@@ -145,6 +146,19 @@ int sg_coulomb_accel(sg_ctx* ctx, int precision, int n, const double* pos,
 int sg_force(sg_ctx* ctx, int precision, int n, const double* pos, const double* vel,
              const double* mass, const int* charge, double t,
              const sg_field_params* fp, double* acc);
+
+/* Coulomb accelerations without any device allocation (no counterpart in the
+ * reference).  For callers that must not call cudaMalloc -- applications that
+ * allocate all device memory up front, or plug-ins that only receive device pointers
+ * from a host framework's pool.  pos [n][3], q [n], kq [n] and acc [n][3] are DEVICE
+ * buffers owned by the caller; the result is the FP64 form of sg_coulomb_accel.  Work
+ * is queued on `stream` (a cudaStream_t, NULL = legacy default stream) of the current
+ * device and the call returns without waiting.  Scratch lives in a fixed 1.8 MB device
+ * array of the library: n <= 8192, else SG_TOO_LARGE.  The first call on a device looks
+ * up that array's device address (make it before capturing any stream).  Calls share
+ * the array: calls that overlap on the GPU race. */
+int sg_coulomb_accel_noalloc(int n, const double* pos, const double* q, const double* kq,
+                             double* acc, void* stream);
 
 /* ---- resident clouds: Dormand-Prince integration on the device -------------- */
 

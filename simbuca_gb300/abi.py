@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(PKG, "libsimgb.so")
 
 # status codes
 SG_OK, SG_BAD_ARG, SG_CUDA_ERR, SG_H_UNDERFLOW, SG_NONFINITE, SG_TIMEOUT, SG_NO_DEVICE, \
-    SG_TOO_MANY_REJECTS, SG_NOT_READY = range(9)
+    SG_TOO_MANY_REJECTS, SG_NOT_READY, SG_TOO_LARGE = range(10)
 SG_PREC_FP64, SG_PREC_FP32C = 0, 1
 
 # field flags
@@ -77,7 +77,8 @@ _vp = ctypes.c_void_p
 # every extern "C" symbol declared in include/simgb.h
 EXPORTED = [
     "sg_create", "sg_destroy", "sg_status_string", "sg_last_cuda_error", "sg_sync",
-    "sg_version", "sg_coulomb_accel", "sg_force", "sg_batch_create", "sg_batch_upload",
+    "sg_version", "sg_coulomb_accel", "sg_force", "sg_coulomb_accel_noalloc",
+    "sg_batch_create", "sg_batch_upload",
     "sg_batch_set_state", "sg_batch_download", "sg_batch_attempts", "sg_dp45_step",
     "sg_batch_run", "sg_batch_info", "sg_batch_set_field", "sg_batch_set_t_end",
     "sg_set_kernel_timing", "sg_kernel_timing", "sg_fixup_count", "sg_set_coulomb_variant",
@@ -107,6 +108,7 @@ def _declare(L):
     L.sg_coulomb_accel.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp]
     L.sg_force.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _ip,
                            ctypes.c_double, ctypes.POINTER(FieldParams), _dp]
+    L.sg_coulomb_accel_noalloc.argtypes = [ctypes.c_int, _vp, _vp, _vp, _vp, _vp]
     L.sg_batch_create.argtypes = [_vp, ctypes.c_int, _ip, ctypes.POINTER(FieldParams),
                                   ctypes.POINTER(OdeParams), ctypes.c_int]
     L.sg_batch_upload.argtypes = [_vp, _dp, _dp, _dp, _ip]

@@ -535,6 +535,7 @@ const char* sg_status_string(int s) {
         case SG_NO_DEVICE: return "no CUDA device";
         case SG_TOO_MANY_REJECTS: return "too many rejected attempts";
         case SG_NOT_READY: return "state not uploaded";
+        case SG_TOO_LARGE: return "size exceeds the fixed capacity";
         default: return "unknown status";
     }
 }
