@@ -222,15 +222,20 @@ def run_ours(args, dist: Dist):
     vel_h = torch.empty((w.n_total, 3), dtype=torch.float64, pin_memory=True).numpy()
     batch.download(pos_h, vel_h)
     e2e_ms = []
+    parts = np.zeros(3)
     e_before = info0()
     dist.barrier()
     for _ in range(args.steps):
         l2_flush()
         t0 = time.perf_counter()
         batch.set_state(pos_h, vel_h)      # H2D of the step's input state
+        t1 = time.perf_counter()
         batch.step()
+        t2 = time.perf_counter()
         batch.download(pos_h, vel_h)       # D2H of the step's result
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        t3 = time.perf_counter()
+        e2e_ms.append((t3 - t0) * 1e3)
+        parts += np.array([t1 - t0, t2 - t1, t3 - t2]) * 1e3
     e_after = info0()
     e2e_sim = dist.sum(sum(a["t"] - b["t"] for a, b in zip(e_after, e_before)) * 1e6)
     e2e_val = e2e_sim / (dist.max(sum(e2e_ms)) * 1e-3)
@@ -274,7 +279,11 @@ def run_ours(args, dist: Dist):
                    "l2": "flushed (256 MB write) between timed steps",
                    "settle_steps": settle_steps, "h_settled": snap[0]["h"]},
         "e2e": {"value": e2e_val, "unit": "sim-us/wall-s", "h2d_bytes_per_step": bytes_state,
-                "d2h_bytes_per_step": bytes_state},
+                "d2h_bytes_per_step": bytes_state, "ms_per_step": sum(e2e_ms) / args.steps,
+                "ms_upload_step_download": (parts / args.steps).tolist(),
+                "mean_h": sum(a["t"] - b["t"] for a, b in zip(e_after, e_before)) /
+                max(1, sum(a["steps"] - b["steps"] for a, b in zip(e_after, e_before)))},
+        "mean_h": sim_us * 1e-6 / max(1, sum(a["steps"] - b["steps"] for a, b in zip(s_after, s_before))),
         "gpu_launches": int(attempts * 21),
         "attempts": int(attempts),
         "interactions_per_s": kt["interactions"] / (kt["coulomb_ms"] * 1e-3) if kt["coulomb_ms"] else None,

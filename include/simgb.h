@@ -213,6 +213,30 @@ int sg_timer_stop(sg_ctx* ctx, double* ms);
  * with per-ion masses); number of ions. */
 int sg_batch_moments(sg_ctx* ctx, double* out);
 
+/* ---- learned step-size proposer ---------------------------------------------
+ * An MLP 16 -> 64 -> 64 -> 1 (SiLU; BF16 weights, FP32 accumulation) proposes each
+ * accepted step's successor from 16 features of the cloud (moments, last step size,
+ * last error norm, excitation phase).  Weights are a flat float array of
+ * sg_mlp_param_count() values: W1[64][16], b1[64], W2[64][64], b2[64], W3[64], b3.
+ * Every attempt is still accepted or rejected by the Dormand-Prince error estimate. */
+int sg_mlp_param_count(void);
+/* out[i] = MLP(X[i]) for n feature rows X[n][16]. */
+int sg_mlp_forward(sg_ctx* ctx, int n, const float* X, const float* w, float* out);
+/* Gradient of the MSE loss (1/n) sum (MLP(X_i) - Y_i)^2 w.r.t. the weights. */
+int sg_mlp_grad(sg_ctx* ctx, int n, const float* X, const float* Y, const float* w,
+                float* grad, float* loss);
+/* Adam (lr, beta 0.9/0.999) on minibatches of `batch` rows for `iters` iterations;
+ * w is the initial FP32 master copy on input and the trained one on output. */
+int sg_mlp_train(sg_ctx* ctx, int n, const float* X, const float* Y, int iters, int batch,
+                 float lr, uint64_t seed, float* w, float* loss_hist);
+/* Use the MLP (w != NULL) with step-size safety factor `safety` in (0, 1] for the
+ * clouds of the batch, or the reference's controller (w == NULL). */
+int sg_batch_set_proposer(sg_ctx* ctx, const float* w, double safety);
+/* Record up to `capacity` accepted steps per cloud: features at the step start and
+ * (h_prev, h, err, t_end_of_step). */
+int sg_batch_set_log(sg_ctx* ctx, int capacity);
+int sg_batch_read_log(sg_ctx* ctx, int cloud, float* feat, double* num, int cap, int* count);
+
 /* ---- measurement probes ----------------------------------------------------- */
 /* Issue-rate probes: FP32 FFMA, packed FP32x2 FFMA2 and FP64 DFMA throughput of the
  * device in GFLOP/s (2 flops per FMA lane), measured with CUDA events. */

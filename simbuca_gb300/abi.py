@@ -85,6 +85,8 @@ EXPORTED = [
     "sg_set_use_graph",
     "sg_timer_start",
     "sg_timer_stop", "sg_batch_moments", "sg_probe_peaks",
+    "sg_mlp_param_count", "sg_mlp_forward", "sg_mlp_grad", "sg_mlp_train",
+    "sg_batch_set_proposer", "sg_batch_set_log", "sg_batch_read_log",
     "cunbody1_force", "cunbody1_force_begin", "cunbody1_force_end",
 ]
 
@@ -129,6 +131,15 @@ def _declare(L):
     L.sg_timer_stop.argtypes = [_vp, _dp]
     L.sg_batch_moments.argtypes = [_vp, _dp]
     L.sg_probe_peaks.argtypes = [_vp, _dp, _dp, _dp]
+    _fp = ctypes.POINTER(ctypes.c_float)
+    L.sg_mlp_forward.argtypes = [_vp, ctypes.c_int, _fp, _fp, _fp]
+    L.sg_mlp_grad.argtypes = [_vp, ctypes.c_int, _fp, _fp, _fp, _fp, _fp]
+    L.sg_mlp_train.argtypes = [_vp, ctypes.c_int, _fp, _fp, ctypes.c_int, ctypes.c_int,
+                               ctypes.c_float, ctypes.c_uint64, _fp, _fp]
+    L.sg_batch_set_proposer.argtypes = [_vp, _fp, ctypes.c_double]
+    L.sg_batch_set_log.argtypes = [_vp, ctypes.c_int]
+    L.sg_batch_read_log.argtypes = [_vp, ctypes.c_int, _fp, _dp, ctypes.c_int,
+                                    ctypes.POINTER(ctypes.c_int)]
     for name in ("cunbody1_force", "cunbody1_force_begin", "cunbody1_force_end"):
         f = getattr(L, name)
         f.argtypes = [_dp, _dp, _dp, ctypes.c_double, _dp, ctypes.c_int, ctypes.c_int]
@@ -157,6 +168,11 @@ def check(status: int, where: str) -> None:
 def dptr(a: np.ndarray):
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data_as(_dp)
+
+
+def fptr(a: np.ndarray):
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
 def iptr(a: np.ndarray):

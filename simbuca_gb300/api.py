@@ -107,6 +107,35 @@ class Context:
     def set_coulomb_variant(self, v: int):
         check(self._L.sg_set_coulomb_variant(self._h, int(v)), "sg_set_coulomb_variant")
 
+    # ---- step-size proposer MLP (BF16 weights, FP32 accumulation) ------------------
+    def mlp_forward(self, X, w):
+        X = np.ascontiguousarray(X, np.float32)
+        w = np.ascontiguousarray(w, np.float32)
+        out = np.empty(len(X), np.float32)
+        check(self._L.sg_mlp_forward(self._h, len(X), abi.fptr(X), abi.fptr(w), abi.fptr(out)),
+              "sg_mlp_forward")
+        return out
+
+    def mlp_grad(self, X, Y, w):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.ascontiguousarray(Y, np.float32)
+        w = np.ascontiguousarray(w, np.float32)
+        g = np.empty(self._L.sg_mlp_param_count(), np.float32)
+        loss = np.zeros(1, np.float32)
+        check(self._L.sg_mlp_grad(self._h, len(Y), abi.fptr(X), abi.fptr(Y), abi.fptr(w),
+                                  abi.fptr(g), abi.fptr(loss)), "sg_mlp_grad")
+        return float(loss[0]), g
+
+    def mlp_train(self, X, Y, w0, iters=2000, batch=256, lr=1e-3, seed=0):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.ascontiguousarray(Y, np.float32)
+        w = np.array(w0, np.float32, order="C")
+        hist = np.zeros(max(iters, 1), np.float32)
+        check(self._L.sg_mlp_train(self._h, len(Y), abi.fptr(X), abi.fptr(Y), int(iters),
+                                   int(batch), float(lr), int(seed), abi.fptr(w), abi.fptr(hist)),
+              "sg_mlp_train")
+        return w, hist[:iters]
+
     def set_use_graph(self, on: bool):
         check(self._L.sg_set_use_graph(self._h, int(bool(on))), "sg_set_use_graph")
 
@@ -193,6 +222,36 @@ class Batch:
         self._live()
         check(self._L.sg_batch_set_field(self.ctx.handle, int(cloud), ctypes.byref(fp)),
               "sg_batch_set_field")
+
+    def set_proposer(self, w=None, safety: float = 0.9):
+        """Learned step-size proposer (weights w) or, with w None, the reference's
+        controller."""
+        self._live()
+        if w is None:
+            check(self._L.sg_batch_set_proposer(self.ctx.handle, None, float(safety)),
+                  "sg_batch_set_proposer")
+        else:
+            w = np.ascontiguousarray(w, np.float32)
+            self._w = w
+            check(self._L.sg_batch_set_proposer(self.ctx.handle, abi.fptr(w), float(safety)),
+                  "sg_batch_set_proposer")
+
+    def set_log(self, capacity: int):
+        self._live()
+        check(self._L.sg_batch_set_log(self.ctx.handle, int(capacity)), "sg_batch_set_log")
+        self._log_cap = int(capacity)
+
+    def read_log(self, cloud: int = 0):
+        """(features [m,16] float32, h_prev, h, err, t) of the logged accepted steps."""
+        self._live()
+        cap = getattr(self, "_log_cap", 0)
+        feat = np.zeros((max(cap, 1), 16), np.float32)
+        num = np.zeros((max(cap, 1), 4))
+        cnt = ctypes.c_int()
+        check(self._L.sg_batch_read_log(self.ctx.handle, int(cloud), abi.fptr(feat), dptr(num),
+                                        cap, ctypes.byref(cnt)), "sg_batch_read_log")
+        m = cnt.value
+        return feat[:m], num[:m, 0], num[:m, 1], num[:m, 2], num[:m, 3]
 
     def set_t_end(self, cloud: int, t_end: float):
         self._live()

@@ -38,6 +38,14 @@ struct Problem {
     SgCtrl* hctrl = nullptr;  // pinned mirror of dctrl
     double interactions = 0.0;  // per Coulomb evaluation, all clouds
     std::vector<double> cloud_inter;
+    // learned step-size proposer and step-history log
+    SgProposerState* pst = nullptr;
+    void* wbf = nullptr;           // BF16 MLP weights
+    float* log_feat = nullptr;     // [clouds][log_cap][16]
+    double* log_num = nullptr;     // [clouds][log_cap][4]: h_prev, h, err, t
+    int log_cap = 0;
+    int use_mlp = 0;
+    double safety = 0.9;
 };
 
 struct TimedLaunch {
@@ -62,8 +70,19 @@ struct sg_ctx {
     long long coul_launches = 0;
     bool use_graph = true;
     cudaGraphExec_t graph = nullptr;
+    // timed graph: the same attempt with an event pair around each Coulomb launch
+    cudaGraphExec_t graph_timed = nullptr;
+    cudaEvent_t gev[16] = {nullptr};
+    int capture_events = -1;  // next event pair while capturing the timed graph, else -1
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     float* probe_sink = nullptr;
+    // MLP training buffers
+    float *mlp_wm = nullptr, *mlp_m1 = nullptr, *mlp_m2 = nullptr, *mlp_grad = nullptr,
+          *mlp_gpart = nullptr, *mlp_lpart = nullptr, *mlp_loss = nullptr, *mlp_X = nullptr,
+          *mlp_Y = nullptr, *mlp_out = nullptr;
+    int* mlp_idx = nullptr;
+    void* mlp_wbf = nullptr;
+    int mlp_cap = 0;
     // CUNBODY slot buffers
     double *cb_xj = nullptr, *cb_mj = nullptr, *cb_xi = nullptr, *cb_ai = nullptr;
     double* cb_host = nullptr;
@@ -98,6 +117,10 @@ void free_problem(Problem& P) {
     for (double* d : ds) cudaFree(d);
     cudaFree(P.c32);
     cudaFree(P.flags);
+    cudaFree(P.pst);
+    cudaFree(P.wbf);
+    cudaFree(P.log_feat);
+    cudaFree(P.log_num);
     if (P.hctrl) cudaFreeHost(P.hctrl);
     P = Problem();
 }
@@ -266,6 +289,10 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(dalloc(&P.stage, 6 * N));
     CK(dalloc(&P.flags, 4));
     CK(cudaMemset(P.flags, 0, 4 * sizeof(int)));
+    CK(dalloc(&P.pst, (size_t)std::max(P.n_clouds, 1)));
+    CK(cudaMemset(P.pst, 0, sizeof(SgProposerState) * (size_t)std::max(P.n_clouds, 1)));
+    CK(cudaMalloc(&P.wbf, SG_MLP_NP * 2));
+    CK(cudaMemset(P.wbf, 0, SG_MLP_NP * 2));
     CK(cudaMemset(P.coul1, 0, 3 * N * sizeof(double)));
     CK(cudaMemset(P.part, 0, (size_t)std::max(P.max_slots, 1) * 4 * NP * sizeof(double)));
     CK(cudaMemset(P.coulS, 0, 3 * N * sizeof(double)));
@@ -343,7 +370,11 @@ int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter, double
     ca.errword = P.flags;
     ca.variant = P.variant;
     TimedLaunch tl{nullptr, nullptr, inter};
-    if (ctx->timing) {
+    const int cap = ctx->capture_events;
+    if (cap >= 0) {
+        // external event nodes: recorded by each replay and readable from the host
+        CK(cudaEventRecordWithFlags(ctx->gev[2 * cap], ctx->stream, cudaEventRecordExternal));
+    } else if (ctx->timing) {
         tl.a = take_event(ctx);
         tl.b = take_event(ctx);
         CK(cudaEventRecord(tl.a, ctx->stream));
@@ -353,7 +384,10 @@ int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter, double
         CK(sg_launch_coulomb_fp32c(ca, ctx->stream));
     else
         CK(sg_launch_coulomb_fp64(ca, ctx->stream));
-    if (ctx->timing) {
+    if (cap >= 0) {
+        CK(cudaEventRecordWithFlags(ctx->gev[2 * cap + 1], ctx->stream, cudaEventRecordExternal));
+        ctx->capture_events = cap + 1;
+    } else if (ctx->timing) {
         CK(cudaEventRecord(tl.b, ctx->stream));
         ctx->pending.push_back(tl);
     }
@@ -382,6 +416,23 @@ int enqueue_attempt(sg_ctx* ctx, Problem& P) {
     }
     CK(sg_dp_control(P.dc, P.dctrl, P.err_part, P.y, P.n_clouds, P.flags + 1, ctx->stream));
     CK(sg_dp_commit(a, P.n_rows, ctx->stream));
+    if (P.log_cap > 0 || P.use_mlp) {
+        CK(sg_moments(a, P.mass, P.mom, P.n_rows, ctx->stream));
+        CK(sg_proposer_launch(P.dc, P.dctrl, P.mom, P.pst, P.wbf, P.log_feat, P.log_num,
+                              P.log_cap, P.use_mlp, P.safety, P.n_clouds, ctx->stream));
+    }
+    return SG_OK;
+}
+
+// Proposer state of a freshly uploaded state: features of the first step.
+int proposer_reset(sg_ctx* ctx, Problem& P) {
+    CK(cudaMemsetAsync(P.pst, 0, sizeof(SgProposerState) * P.n_clouds, ctx->stream));
+    if (P.log_cap > 0 || P.use_mlp) {
+        SgDpArgs a = dp_args(P);
+        CK(sg_moments(a, P.mass, P.mom, P.n_rows, ctx->stream));
+        CK(sg_proposer_launch(P.dc, P.dctrl, P.mom, P.pst, P.wbf, P.log_feat, P.log_num,
+                              P.log_cap, P.use_mlp, P.safety, P.n_clouds, ctx->stream));
+    }
     return SG_OK;
 }
 
@@ -390,24 +441,62 @@ int drop_graph(sg_ctx* ctx) {
         cudaGraphExecDestroy(ctx->graph);
         ctx->graph = nullptr;
     }
+    if (ctx->graph_timed) {
+        cudaGraphExecDestroy(ctx->graph_timed);
+        ctx->graph_timed = nullptr;
+    }
+    return SG_OK;
+}
+
+int capture_attempt(sg_ctx* ctx, Problem& P, bool timed, cudaGraphExec_t* out) {
+    cudaGraph_t g = nullptr;
+    if (timed)
+        for (int k = 0; k < 12; k++)
+            if (!ctx->gev[k]) CK(cudaEventCreate(&ctx->gev[k]));
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    ctx->capture_events = timed ? 0 : -1;
+    int st = enqueue_attempt(ctx, P);
+    ctx->capture_events = -1;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (st != SG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    CK(e);
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    CK(e);
     return SG_OK;
 }
 
 int run_attempts(sg_ctx* ctx, Problem& P, int n) {
-    if (ctx->use_graph && !ctx->timing) {
-        if (!ctx->graph) {
-            cudaGraph_t g = nullptr;
-            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-            int st = enqueue_attempt(ctx, P);
-            cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
-            if (st != SG_OK) {
-                if (g) cudaGraphDestroy(g);
-                return st;
+    if (ctx->use_graph && ctx->timing) {
+        // graph replays one at a time, reading the Coulomb event pairs after each
+        if (!ctx->graph_timed) {
+            int st = capture_attempt(ctx, P, true, &ctx->graph_timed);
+            if (st != SG_OK) return st;
+        }
+        const int pairs = P.any_coulomb ? 6 : 0;
+        for (int i = 0; i < n; i++) {
+            const double inter = active_interactions(P);
+            CK(cudaGraphLaunch(ctx->graph_timed, ctx->stream));
+            if (pairs) {
+                CK(cudaEventSynchronize(ctx->gev[2 * pairs - 1]));
+                for (int k = 0; k < pairs; k++) {
+                    float ms = 0.f;
+                    CK(cudaEventElapsedTime(&ms, ctx->gev[2 * k], ctx->gev[2 * k + 1]));
+                    ctx->coul_ms += ms;
+                    ctx->coul_launches += 1;
+                    ctx->coul_inter += inter;
+                }
             }
-            CK(e);
-            e = cudaGraphInstantiate(&ctx->graph, g, 0);
-            cudaGraphDestroy(g);
-            CK(e);
+        }
+        return SG_OK;
+    }
+    if (ctx->use_graph) {
+        if (!ctx->graph) {
+            int st = capture_attempt(ctx, P, false, &ctx->graph);
+            if (st != SG_OK) return st;
         }
         for (int i = 0; i < n; i++) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
         return SG_OK;
@@ -476,7 +565,14 @@ int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel) 
         CK(cudaMemcpyAsync(P.stage + 3 * N, vel, 3 * N * sizeof(double), cudaMemcpyHostToDevice,
                            ctx->stream));
     CK(sg_aos_to_soa(P.stage, vel ? P.stage + 3 * N : nullptr, P.y, P.n, ctx->stream));
-    for (int c = 0; c < P.n_clouds; c++) set_frame(P.hc[c], pos, P.hc[c].off);
+    for (int c = 0; c < P.n_clouds; c++) {
+        set_frame(P.hc[c], pos, P.hc[c].off);
+        double v2 = 0.0;
+        if (vel)
+            for (int i = P.hc[c].off; i < P.hc[c].off + P.hc[c].n; i++)
+                for (int k = 0; k < 3; k++) v2 += vel[3 * (size_t)i + k] * vel[3 * (size_t)i + k];
+        P.hc[c].vref = P.hc[c].n ? std::sqrt(v2 / (3.0 * P.hc[c].n)) : 0.0;
+    }
     CK(cudaMemcpyAsync(P.dc, P.hc.data(), sizeof(SgCloud) * P.n_clouds, cudaMemcpyHostToDevice,
                        ctx->stream));
     SgDpArgs a = dp_args(P);
@@ -572,9 +668,16 @@ int sg_destroy(sg_ctx* ctx) {
     free_problem(ctx->batch);
     free_problem(ctx->solo);
     for (cudaEvent_t e : ctx->free_ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->gev)
+        if (e) cudaEventDestroy(e);
     cudaEventDestroy(ctx->t0);
     cudaEventDestroy(ctx->t1);
     cudaFree(ctx->probe_sink);
+    float* mf[] = {ctx->mlp_wm, ctx->mlp_m1, ctx->mlp_m2, ctx->mlp_grad, ctx->mlp_gpart,
+                   ctx->mlp_lpart, ctx->mlp_loss, ctx->mlp_X, ctx->mlp_Y, ctx->mlp_out};
+    for (float* f : mf) cudaFree(f);
+    cudaFree(ctx->mlp_idx);
+    cudaFree(ctx->mlp_wbf);
     cudaFree(ctx->cb_xj);
     cudaFree(ctx->cb_mj);
     cudaFree(ctx->cb_xi);
@@ -728,6 +831,8 @@ int sg_batch_upload(sg_ctx* ctx, const double* pos, const double* vel, const dou
     // stage-1 Coulomb sum of the initial state
     st = launch_coulomb(ctx, P, true, active_interactions(P), P.coul1);
     if (st != SG_OK) return st;
+    st = proposer_reset(ctx, P);
+    if (st != SG_OK) return st;
     CK(cudaStreamSynchronize(ctx->stream));
     flush_timing(ctx);
     P.uploaded = true;
@@ -744,6 +849,8 @@ int sg_batch_set_state(sg_ctx* ctx, const double* pos, const double* vel) {
     int st = upload_state(ctx, P, pos, vel);
     if (st != SG_OK) return st;
     st = launch_coulomb(ctx, P, true, active_interactions(P), P.coul1);
+    if (st != SG_OK) return st;
+    st = proposer_reset(ctx, P);
     if (st != SG_OK) return st;
     CK(cudaStreamSynchronize(ctx->stream));
     flush_timing(ctx);
@@ -989,6 +1096,201 @@ int sg_probe_peaks(sg_ctx* ctx, double* fp32, double* fp32x2, double* fp64) {
         }
         *outs[w] = best;
     }
+    return SG_OK;
+}
+
+}  // extern "C"
+
+
+// ---- learned step-size proposer --------------------------------------------------
+namespace {
+int mlp_reserve(sg_ctx* ctx, int n) {
+    if (!ctx->mlp_wm) {
+        CK(dalloc(&ctx->mlp_wm, SG_MLP_NP));
+        CK(dalloc(&ctx->mlp_m1, SG_MLP_NP));
+        CK(dalloc(&ctx->mlp_m2, SG_MLP_NP));
+        CK(dalloc(&ctx->mlp_grad, SG_MLP_NP));
+        CK(dalloc(&ctx->mlp_gpart, (size_t)SG_MLP_NP * 64));
+        CK(dalloc(&ctx->mlp_lpart, 64));
+        CK(dalloc(&ctx->mlp_loss, 1));
+        CK(cudaMalloc(&ctx->mlp_wbf, SG_MLP_NP * 2));
+    }
+    if (n > ctx->mlp_cap) {
+        cudaFree(ctx->mlp_X);
+        cudaFree(ctx->mlp_Y);
+        cudaFree(ctx->mlp_out);
+        cudaFree(ctx->mlp_idx);
+        ctx->mlp_X = ctx->mlp_Y = ctx->mlp_out = nullptr;
+        ctx->mlp_idx = nullptr;
+        CK(dalloc(&ctx->mlp_X, (size_t)n * SG_MLP_IN));
+        CK(dalloc(&ctx->mlp_Y, (size_t)n));
+        CK(dalloc(&ctx->mlp_out, (size_t)n));
+        CK(dalloc(&ctx->mlp_idx, (size_t)n));
+        ctx->mlp_cap = n;
+    }
+    return SG_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int sg_mlp_param_count(void) { return SG_MLP_NP; }
+
+int sg_mlp_forward(sg_ctx* ctx, int n, const float* X, const float* w, float* out) {
+    if (!ctx || n < 0 || (n > 0 && (!X || !w || !out))) return SG_BAD_ARG;
+    if (n == 0) return SG_OK;
+    CK(cudaSetDevice(ctx->device));
+    int st = mlp_reserve(ctx, n);
+    if (st != SG_OK) return st;
+    CK(cudaMemcpyAsync(ctx->mlp_wm, w, SG_MLP_NP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    CK(sg_mlp_to_bf16_launch(ctx->mlp_wm, ctx->mlp_wbf, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->mlp_X, X, sizeof(float) * n * SG_MLP_IN, cudaMemcpyHostToDevice, ctx->stream));
+    CK(sg_mlp_forward_launch(ctx->mlp_wbf, ctx->mlp_X, n, ctx->mlp_out, ctx->stream));
+    CK(cudaMemcpyAsync(out, ctx->mlp_out, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
+int sg_mlp_grad(sg_ctx* ctx, int n, const float* X, const float* Y, const float* w, float* grad,
+                float* loss) {
+    if (!ctx || n <= 0 || !X || !Y || !w || !grad || !loss) return SG_BAD_ARG;
+    CK(cudaSetDevice(ctx->device));
+    int st = mlp_reserve(ctx, n);
+    if (st != SG_OK) return st;
+    CK(cudaMemcpyAsync(ctx->mlp_wm, w, SG_MLP_NP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    CK(sg_mlp_to_bf16_launch(ctx->mlp_wm, ctx->mlp_wbf, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->mlp_X, X, sizeof(float) * n * SG_MLP_IN, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->mlp_Y, Y, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream));
+    const int nb = std::min(64, std::max(1, n / 32));
+    CK(sg_mlp_grad_launch(ctx->mlp_wbf, ctx->mlp_X, ctx->mlp_Y, nullptr, n, ctx->mlp_gpart,
+                          ctx->mlp_lpart, nb, ctx->mlp_grad, ctx->mlp_loss, ctx->stream));
+    CK(cudaMemcpyAsync(grad, ctx->mlp_grad, SG_MLP_NP * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(loss, ctx->mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
+int sg_mlp_train(sg_ctx* ctx, int n, const float* X, const float* Y, int iters, int batch,
+                 float lr, uint64_t seed, float* w, float* loss_hist) {
+    if (!ctx || n <= 0 || !X || !Y || !w || iters < 0 || batch <= 0) return SG_BAD_ARG;
+    CK(cudaSetDevice(ctx->device));
+    batch = std::min(batch, n);
+    int st = mlp_reserve(ctx, n);
+    if (st != SG_OK) return st;
+    CK(cudaMemcpyAsync(ctx->mlp_wm, w, SG_MLP_NP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(ctx->mlp_m1, 0, SG_MLP_NP * sizeof(float), ctx->stream));
+    CK(cudaMemsetAsync(ctx->mlp_m2, 0, SG_MLP_NP * sizeof(float), ctx->stream));
+    CK(sg_mlp_to_bf16_launch(ctx->mlp_wm, ctx->mlp_wbf, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->mlp_X, X, sizeof(float) * n * SG_MLP_IN, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->mlp_Y, Y, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream));
+    // minibatches: a seeded permutation per epoch (splitmix64), uploaded per iteration
+    std::vector<int> perm(n), idx(batch);
+    for (int i = 0; i < n; i++) perm[i] = i;
+    uint64_t s = seed;
+    auto next = [&s]() {
+        s += 0x9E3779B97F4A7C15ull;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    int pos = n;
+    std::vector<float> losses(iters > 0 ? iters : 1);
+    const int nb = std::min(64, std::max(1, batch / 32));
+    for (int it = 0; it < iters; it++) {
+        for (int b = 0; b < batch; b++) {
+            if (pos >= n) {
+                for (int i = n - 1; i > 0; i--) std::swap(perm[i], perm[next() % (uint64_t)(i + 1)]);
+                pos = 0;
+            }
+            idx[b] = perm[pos++];
+        }
+        CK(cudaMemcpyAsync(ctx->mlp_idx, idx.data(), sizeof(int) * batch, cudaMemcpyHostToDevice,
+                           ctx->stream));
+        CK(sg_mlp_grad_launch(ctx->mlp_wbf, ctx->mlp_X, ctx->mlp_Y, ctx->mlp_idx, batch,
+                              ctx->mlp_gpart, ctx->mlp_lpart, nb, ctx->mlp_grad, ctx->mlp_loss,
+                              ctx->stream));
+        CK(sg_mlp_adam_launch(ctx->mlp_wm, ctx->mlp_wbf, ctx->mlp_m1, ctx->mlp_m2, ctx->mlp_grad, lr,
+                              it + 1, ctx->stream));
+        if (loss_hist)
+            CK(cudaMemcpyAsync(&losses[it], ctx->mlp_loss, sizeof(float), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+        // the index buffer is reused next iteration: wait for this one's upload to land
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    CK(cudaMemcpyAsync(w, ctx->mlp_wm, SG_MLP_NP * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (loss_hist)
+        for (int it = 0; it < iters; it++) loss_hist[it] = losses[it];
+    return SG_OK;
+}
+
+int sg_batch_set_proposer(sg_ctx* ctx, const float* w, double safety) {
+    if (!ctx || !(safety > 0.0 && safety <= 1.0)) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    drop_graph(ctx);
+    if (w) {
+        int st = mlp_reserve(ctx, 1);
+        if (st != SG_OK) return st;
+        CK(cudaMemcpyAsync(ctx->mlp_wm, w, SG_MLP_NP * sizeof(float), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        CK(sg_mlp_to_bf16_launch(ctx->mlp_wm, P.wbf, ctx->stream));
+    }
+    const bool was_active = P.log_cap > 0 || P.use_mlp;
+    P.use_mlp = w ? 1 : 0;
+    P.safety = safety;
+    if (!was_active && P.uploaded) {
+        int st = proposer_reset(ctx, P);
+        if (st != SG_OK) return st;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
+int sg_batch_set_log(sg_ctx* ctx, int capacity) {
+    if (!ctx || capacity < 0) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    drop_graph(ctx);
+    cudaFree(P.log_feat);
+    cudaFree(P.log_num);
+    P.log_feat = nullptr;
+    P.log_num = nullptr;
+    P.log_cap = 0;
+    if (capacity > 0) {
+        CK(dalloc(&P.log_feat, (size_t)P.n_clouds * capacity * SG_MLP_IN));
+        CK(dalloc(&P.log_num, (size_t)P.n_clouds * capacity * 4));
+        P.log_cap = capacity;
+    }
+    if (P.uploaded) {
+        int st = proposer_reset(ctx, P);
+        if (st != SG_OK) return st;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
+int sg_batch_read_log(sg_ctx* ctx, int cloud, float* feat, double* num, int cap, int* count) {
+    if (!ctx || !count) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (cloud < 0 || cloud >= P.n_clouds || P.log_cap == 0) return SG_BAD_ARG;
+    CK(cudaSetDevice(ctx->device));
+    SgProposerState ps;
+    CK(cudaMemcpyAsync(&ps, P.pst + cloud, sizeof ps, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const int m = std::min(std::min(ps.logged, P.log_cap), cap);
+    if (m > 0 && feat)
+        CK(cudaMemcpy(feat, P.log_feat + (size_t)cloud * P.log_cap * SG_MLP_IN,
+                      sizeof(float) * m * SG_MLP_IN, cudaMemcpyDeviceToHost));
+    if (m > 0 && num)
+        CK(cudaMemcpy(num, P.log_num + (size_t)cloud * P.log_cap * 4, sizeof(double) * m * 4,
+                      cudaMemcpyDeviceToHost));
+    *count = m;
     return SG_OK;
 }
 

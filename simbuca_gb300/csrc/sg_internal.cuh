@@ -62,6 +62,7 @@ struct SgCloud {
     int32_t pad;
     double cx, cy, cz;   // centre of the FP32 frame (m)
     double L, invL;      // scale of the FP32 frame (m)
+    double vref;         // RMS velocity per axis at upload (m/s), proposer features
     float wc;            // FP32c close-pair threshold on 1/r^3 (frame units)
     float pad2;
     sg_field_params fp;
@@ -72,6 +73,27 @@ struct SgCtrl {
     double t, h, hnext, errold, err, t_end, rtol, atol, h_last;
     int32_t reject, adaptive, max_rejects, status, done, accepted, rejects_here, hold;
     long long steps, rejects, force_evals, coulomb_evals;
+};
+
+// ---- learned step-size proposer (proposer.cu) -------------------------------------
+#define SG_MLP_IN 16
+#define SG_MLP_H 64
+#define SG_MLP_W1 0
+#define SG_MLP_B1 (SG_MLP_W1 + SG_MLP_H * SG_MLP_IN)
+#define SG_MLP_W2 (SG_MLP_B1 + SG_MLP_H)
+#define SG_MLP_B2 (SG_MLP_W2 + SG_MLP_H * SG_MLP_H)
+#define SG_MLP_W3 (SG_MLP_B2 + SG_MLP_H)
+#define SG_MLP_B3 (SG_MLP_W3 + SG_MLP_H)
+#define SG_MLP_NP (SG_MLP_B3 + 1)
+
+// Per-cloud proposer state: features of the current step start and step history.
+struct SgProposerState {
+    float feat[SG_MLP_IN];
+    double h_prev;          // accepted step size before the last accepted step
+    int32_t init;           // features computed since the last upload
+    int32_t logged;         // log records written
+    int32_t rejects_in_step;
+    int32_t pad;
 };
 
 // ---- field terms ---------------------------------------------------------------
@@ -166,6 +188,18 @@ cudaError_t sg_moments(const SgDpArgs& a, const double* mass, double* out, int n
 cudaError_t sg_cunbody_launch(const double* xj, const double* mj, const double* xi, double eps2,
                               double* ai, int ni, int nj, cudaStream_t st);
 cudaError_t sg_probe_launch(int which, int blocks, int threads, float* sink, cudaStream_t st);
+cudaError_t sg_proposer_launch(const SgCloud* clouds, SgCtrl* ctrl, const double* mom,
+                               SgProposerState* pst, const void* wbf, float* log_feat,
+                               double* log_num, int log_cap, int use_mlp, double safety,
+                               int n_clouds, cudaStream_t st);
+cudaError_t sg_mlp_grad_launch(const void* wbf, const float* X, const float* Y, const int* idx,
+                               int B, float* gpart, float* lpart, int nb, float* grad, float* loss,
+                               cudaStream_t st);
+cudaError_t sg_mlp_adam_launch(float* wm, void* wbf, float* m1, float* m2, const float* grad,
+                               float lr, int step, cudaStream_t st);
+cudaError_t sg_mlp_to_bf16_launch(const float* wm, void* wbf, cudaStream_t st);
+cudaError_t sg_mlp_forward_launch(const void* wbf, const float* X, int n, float* out,
+                                  cudaStream_t st);
 
 struct SgCoulombArgs {
     const float* c32;        // [7][Npad] frame coords hi x,y,z, charge, lo x,y,z (FP32c)

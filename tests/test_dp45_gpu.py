@@ -224,3 +224,25 @@ def test_reference_mirror_step_and_force(ctx):
     while cl.lifetime < t_end:
         ode.step(cl, od)
     np.testing.assert_allclose(cl.pos, g[f"{tag}_pos"], rtol=1e-9, atol=1e-15)
+
+
+def test_kernel_timing_in_graph_and_direct(ctx):
+    """Coulomb launches are timed with CUDA events both inside the attempt graph and with
+    direct launches; both count 6 Coulomb sums per attempt."""
+    w = configs.penning_1k(n=700, seed=8)
+    c = w.clouds[0]
+    for graph in (True, False):
+        ctx.set_use_graph(graph)
+        b = one_cloud(ctx, c.pos, c.vel, c.mass, c.charge, configs.penning_field(), 1e-9, 1e-15,
+                      1e-9, 1.0, SG_PREC_FP32C)
+        ctx.set_kernel_timing(True)
+        i0 = b.info()[0]
+        for _ in range(3):
+            b.step()
+        i1 = b.info()[0]
+        kt = ctx.kernel_timing()
+        ctx.set_kernel_timing(False)
+        attempts = (i1["steps"] + i1["rejects"]) - (i0["steps"] + i0["rejects"])
+        assert kt["coulomb_launches"] == 6 * attempts
+        assert kt["coulomb_ms"] > 0 and kt["interactions"] == 6 * attempts * 700 * 699
+    ctx.set_use_graph(True)
