@@ -103,6 +103,9 @@ typedef struct sg_ode_params {
     double t_end;        /* the cloud stops advancing once t >= t_end                    */
     int32_t adaptive;    /* 1: step-size control on (ode.cpp:478); 0: fixed step h0     */
     int32_t max_rejects; /* reject budget per step (0 = unlimited)                      */
+    int32_t method;      /* Init_ode order (ode.cpp:556-583): 5 Dormand-Prince (0 = 5),
+                            4 Cash-Karp, the reference's "RungaKutta4" (ode.cpp:220-345) */
+    int32_t pad;
 } sg_ode_params;
 
 /* State of one cloud after a call. */
@@ -199,7 +202,8 @@ int sg_kernel_timing(sg_ctx* ctx, double* coulomb_ms, int64_t* coulomb_launches,
 int sg_fixup_count(sg_ctx* ctx, int64_t* count);
 /* Launch shape of the FP32c Coulomb kernel for batches and calls created afterwards:
  * -1 = chosen from the cloud sizes (default), 0 = 128 threads x 4 ions,
- * 1 = 128 x 2, 2 = 256 x 2, 3 = 64 x 4. */
+ * 1 = 128 x 2, 2 = 256 x 2, 3 = 64 x 4, 4 = 128 x 4 with the ions kept in k-d tree
+ * order and far tile pairs summed from the high parts of the coordinates. */
 int sg_set_coulomb_variant(sg_ctx* ctx, int variant);
 /* Capture the attempt sequence in a CUDA graph (1) or launch it directly (0). */
 int sg_set_use_graph(sg_ctx* ctx, int on);

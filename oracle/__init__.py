@@ -80,10 +80,13 @@ def lib():
                                    ctypes.POINTER(OrcCtrl), ctypes.c_int64, _dp,
                                    ctypes.c_int64]
         L.orc_dp45_run.restype = ctypes.c_int64
+        L.orc_rk_run.argtypes = [ctypes.c_int] + L.orc_dp45_run.argtypes
+        L.orc_rk_run.restype = ctypes.c_int64
         L.orc_error_succes.argtypes = [ctypes.c_double, ctypes.POINTER(OrcCtrl)]
         L.orc_moments.argtypes = [ctypes.c_int, _dp, _dp, _dp, _dp]
         L.orc_dp45_replay.argtypes = [ctypes.c_int, _dp, _dp, _dp, _ip, ctypes.c_void_p, _dp,
                                       _dp, ctypes.c_int]
+        L.orc_rk_replay.argtypes = [ctypes.c_int] + L.orc_dp45_replay.argtypes
         _orc = L
     return _orc
 
@@ -134,8 +137,9 @@ def field(pos, vel, mass, charge, t, fp):
 
 
 def dp45_run(pos, vel, mass, charge, fp, *, rtol, atol, h0, t0, t_end, adaptive=True,
-             max_steps=1 << 62, hist_cap=0, max_rejects=0):
-    """Run the restated step loop; returns (pos, vel, ctrl, hist[attempts, 4])."""
+             max_steps=1 << 62, hist_cap=0, max_rejects=0, method=5):
+    """Run the restated step loop (method 5 Dormand-Prince, 4 Cash-Karp); returns
+    (pos, vel, ctrl, hist[attempts, 4], n_attempts)."""
     pos = np.array(pos, np.float64, order="C")
     vel = np.array(vel, np.float64, order="C")
     mass = np.ascontiguousarray(mass, np.float64)
@@ -144,23 +148,24 @@ def dp45_run(pos, vel, mass, charge, fp, *, rtol, atol, h0, t0, t_end, adaptive=
     c.rtol, c.atol, c.h, c.hnext, c.errold = rtol, atol, h0, h0, 1e-4
     c.t, c.t_end, c.adaptive, c.max_rejects = t0, t_end, int(adaptive), int(max_rejects)
     hist = np.zeros((max(hist_cap, 1), 4))
-    nh = lib().orc_dp45_run(len(mass), _d(pos), _d(vel), _d(mass), _i(charge),
-                            ctypes.byref(fp), ctypes.byref(c), int(max_steps), _d(hist),
-                            int(hist_cap))
+    nh = lib().orc_rk_run(int(method), len(mass), _d(pos), _d(vel), _d(mass), _i(charge),
+                          ctypes.byref(fp), ctypes.byref(c), int(max_steps), _d(hist),
+                          int(hist_cap))
     n_rec = min(max(nh, 0), hist_cap)
     return pos, vel, c, hist[:n_rec], nh
 
 
-def dp45_replay(pos, vel, mass, charge, fp, ts, hs):
-    """Fixed steps with the schedule (ts[k], hs[k]); returns (pos, vel)."""
+def dp45_replay(pos, vel, mass, charge, fp, ts, hs, method=5):
+    """Fixed steps with the schedule (ts[k], hs[k]); returns (pos, vel).
+    method 5 = Dormand-Prince, 4 = Cash-Karp."""
     pos = np.array(pos, np.float64, order="C")
     vel = np.array(vel, np.float64, order="C")
     mass = np.ascontiguousarray(mass, np.float64)
     charge = np.ascontiguousarray(charge, np.int32)
     ts = np.ascontiguousarray(ts, np.float64)
     hs = np.ascontiguousarray(hs, np.float64)
-    st = lib().orc_dp45_replay(len(mass), _d(pos), _d(vel), _d(mass), _i(charge),
-                               ctypes.byref(fp), _d(ts), _d(hs), len(ts))
+    st = lib().orc_rk_replay(int(method), len(mass), _d(pos), _d(vel), _d(mass), _i(charge),
+                             ctypes.byref(fp), _d(ts), _d(hs), len(ts))
     assert st == 0
     return pos, vel
 
@@ -196,7 +201,7 @@ def ref_lib():
                                    ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_longlong, ctypes.c_int, _dp, ctypes.c_longlong,
-                                   _dp]
+                                   _dp, ctypes.c_int]
         L.ref_dp45_run.restype = ctypes.c_longlong
         _ref = L
     return _ref
@@ -216,7 +221,7 @@ def ref_force(pos, vel, mass, charge, t, *, trap, tof, coulomb, coulomb_scale, t
 
 
 def ref_dp45_run(pos, vel, mass, charge, *, trap, tof, coulomb, coulomb_scale, trapp, t0,
-                 t_end, h0, adaptive, rtol, atol, max_steps, mode, hist_cap=0):
+                 t_end, h0, adaptive, rtol, atol, max_steps, mode, hist_cap=0, method=5):
     pos = np.array(pos, np.float64, order="C")
     vel = np.array(vel, np.float64, order="C")
     mass = np.ascontiguousarray(mass, np.float64)
@@ -228,5 +233,5 @@ def ref_dp45_run(pos, vel, mass, charge, *, trap, tof, coulomb, coulomb_scale, t
                                 int(tof), int(coulomb), float(coulomb_scale), _d(trapp),
                                 float(t0), float(t_end), float(h0), int(adaptive), float(rtol),
                                 float(atol), int(max_steps), int(mode), _d(hist), int(hist_cap),
-                                _d(ctrl))
+                                _d(ctrl), int(method))
     return pos, vel, ctrl, hist[:min(max(nh, 0), hist_cap)], nh

@@ -380,6 +380,121 @@ double orc_dp45_attempt(int n, const double* pos, const double* vel, const doubl
     return err;
 }
 
+
+/* ---------------------------------------------------------------------------
+ * Cash-Karp 5(4), bin/ode.cpp:220-345 (the reference calls it RungaKutta4).
+ * ------------------------------------------------------------------------- */
+static const double RKb21 = 0.2, RKb31 = 3.0 / 40.0, RKb32 = 9.0 / 40.0, RKb41 = 0.3,
+                    RKb42 = -0.9, RKb43 = 1.2, RKb51 = -11.0 / 54.0, RKb52 = 2.5,
+                    RKb53 = -70.0 / 27.0, RKb54 = 35.0 / 27.0, RKb61 = 1631.0 / 55296.0,
+                    RKb62 = 175.0 / 512.0, RKb63 = 575.0 / 13824.0, RKb64 = 44275.0 / 110592.0,
+                    RKb65 = 253.0 / 4096.0, RKc1 = 37.0 / 378.0, RKc3 = 250.0 / 621.0,
+                    RKc4 = 125.0 / 594.0, RKc6 = 512.0 / 1771.0;
+#define RKdc5 (-277.00 / 14336.0)
+#define RKdc1 (RKc1 - 2825.0 / 27648.0)
+#define RKdc3 (RKc3 - 18575.0 / 48384.0)
+#define RKdc4 (RKc4 - 13525.0 / 55296.0)
+#define RKdc6 (RKc6 - 0.25)
+
+double orc_ck45_attempt(int n, const double* pos, const double* vel, const double* mass,
+                        const int* charge, const sg_field_params* fp, orc_ctrl* cs,
+                        double* pos2, double* vel2, double* k, double* derivs) {
+    const double h = cs->h;
+    const int frozen = (fp->flags & SG_F_FROZEN_T) != 0;
+    const double t0 = cs->t;
+    /* stage times of the Cash-Karp nodes c = 0, 1/5, 3/10, 3/5, 1, 7/8 */
+    const double cc[6] = {0.0, 0.2, 0.3, 0.6, 1.0, 0.875};
+    double ts[6];
+    for (int s = 0; s < 6; s++) ts[s] = frozen ? t0 : t0 + cc[s] * h;
+    double err = cs->err;  /* not reset, as in the reference */
+    double sk;
+    for (int j = 0; j < n; j++) {
+        KS(0, j, 0) = vel[3 * j + 0];
+        KS(0, j, 1) = vel[3 * j + 1];
+        KS(0, j, 2) = vel[3 * j + 2];
+    }
+    memcpy(pos2, pos, sizeof(double) * 3 * (size_t)n);
+    memcpy(vel2, vel, sizeof(double) * 3 * (size_t)n);
+    orc_force(n, pos2, vel2, mass, charge, ts[0], fp, derivs);
+    for (int j = 0; j < n; j++) {
+        for (int c = 0; c < 3; c++) KS(0, j, 3 + c) = derivs[3 * j + c];
+        for (int c = 0; c < 3; c++) pos2[3 * j + c] = pos[3 * j + c] + h * (RKb21 * KS(0, j, c));
+        for (int c = 0; c < 3; c++)
+            KS(1, j, c) = vel2[3 * j + c] = vel[3 * j + c] + h * (RKb21 * KS(0, j, 3 + c));
+    }
+    orc_force(n, pos2, vel2, mass, charge, ts[1], fp, derivs);
+    for (int j = 0; j < n; j++) {
+        for (int c = 0; c < 3; c++) KS(1, j, 3 + c) = derivs[3 * j + c];
+        for (int c = 0; c < 3; c++)
+            pos2[3 * j + c] = pos[3 * j + c] + h * (RKb31 * KS(0, j, c) + RKb32 * KS(1, j, c));
+        for (int c = 0; c < 3; c++)
+            KS(2, j, c) = vel2[3 * j + c] =
+                vel[3 * j + c] + h * (RKb31 * KS(0, j, 3 + c) + RKb32 * KS(1, j, 3 + c));
+    }
+    orc_force(n, pos2, vel2, mass, charge, ts[2], fp, derivs);
+    for (int j = 0; j < n; j++) {
+        for (int c = 0; c < 3; c++) KS(2, j, 3 + c) = derivs[3 * j + c];
+        for (int c = 0; c < 3; c++)
+            pos2[3 * j + c] = pos[3 * j + c] + h * (RKb41 * KS(0, j, c) + RKb42 * KS(1, j, c) +
+                                                    RKb43 * KS(2, j, c));
+        for (int c = 0; c < 3; c++)
+            KS(3, j, c) = vel2[3 * j + c] =
+                vel[3 * j + c] + h * (RKb41 * KS(0, j, 3 + c) + RKb42 * KS(1, j, 3 + c) +
+                                      RKb43 * KS(2, j, 3 + c));
+    }
+    orc_force(n, pos2, vel2, mass, charge, ts[3], fp, derivs);
+    for (int j = 0; j < n; j++) {
+        for (int c = 0; c < 3; c++) KS(3, j, 3 + c) = derivs[3 * j + c];
+        for (int c = 0; c < 3; c++)
+            pos2[3 * j + c] = pos[3 * j + c] + h * (RKb51 * KS(0, j, c) + RKb52 * KS(1, j, c) +
+                                                    RKb53 * KS(2, j, c) + RKb54 * KS(3, j, c));
+        for (int c = 0; c < 3; c++)
+            KS(4, j, c) = vel2[3 * j + c] =
+                vel[3 * j + c] + h * (RKb51 * KS(0, j, 3 + c) + RKb52 * KS(1, j, 3 + c) +
+                                      RKb53 * KS(2, j, 3 + c) + RKb54 * KS(3, j, 3 + c));
+    }
+    orc_force(n, pos2, vel2, mass, charge, ts[4], fp, derivs);
+    for (int j = 0; j < n; j++) {
+        for (int c = 0; c < 3; c++) KS(4, j, 3 + c) = derivs[3 * j + c];
+        for (int c = 0; c < 3; c++)
+            pos2[3 * j + c] =
+                pos[3 * j + c] + h * (RKb61 * KS(0, j, c) + RKb62 * KS(1, j, c) +
+                                      RKb63 * KS(2, j, c) + RKb64 * KS(3, j, c) +
+                                      RKb65 * KS(4, j, c));
+        for (int c = 0; c < 3; c++)
+            KS(5, j, c) = vel2[3 * j + c] =
+                vel[3 * j + c] + h * (RKb61 * KS(0, j, 3 + c) + RKb62 * KS(1, j, 3 + c) +
+                                      RKb63 * KS(2, j, 3 + c) + RKb64 * KS(3, j, 3 + c) +
+                                      RKb65 * KS(4, j, 3 + c));
+    }
+    orc_force(n, pos2, vel2, mass, charge, ts[5], fp, derivs);
+    for (int j = 0; j < n; j++) {
+        double yerr[6];
+        for (int c = 0; c < 3; c++) KS(5, j, 3 + c) = derivs[3 * j + c];
+        for (int c = 0; c < 3; c++)
+            pos2[3 * j + c] = pos[3 * j + c] + h * (RKc1 * KS(0, j, c) + RKc3 * KS(2, j, c) +
+                                                    RKc4 * KS(3, j, c) + RKc6 * KS(5, j, c));
+        for (int c = 0; c < 3; c++)
+            vel2[3 * j + c] = vel[3 * j + c] + h * (RKc1 * KS(0, j, 3 + c) + RKc3 * KS(2, j, 3 + c) +
+                                                    RKc4 * KS(3, j, 3 + c) + RKc6 * KS(5, j, 3 + c));
+        for (int i = 0; i < 6; i++)
+            yerr[i] = h * (RKdc1 * KS(0, j, i) + RKdc3 * KS(2, j, i) + RKdc4 * KS(3, j, i) +
+                           RKdc5 * KS(4, j, i) + RKdc6 * KS(5, j, i));
+        for (int c = 0; c < 3; c++) {
+            sk = cs->atol + cs->rtol * ref_max(fabs(pos[3 * j + c]), fabs(pos2[3 * j + c]));
+            err = err + (yerr[c] / sk) * (yerr[c] / sk);
+        }
+        for (int c = 0; c < 3; c++) {
+            sk = cs->atol + cs->rtol * ref_max(fabs(vel[3 * j + c]), fabs(vel2[3 * j + c]));
+            err = err + (yerr[3 + c] / sk) * (yerr[3 + c] / sk);
+        }
+    }
+    err = sqrt(err / (6 * n));
+    cs->err = err;
+    cs->force_evals += 6;
+    return err;
+}
+
 /* error_succes, bin/ode.cpp:426-457 (beta = 0, alpha = 0.2, safe = 0.9,
  * minscale = 0.2, maxscale = 10). */
 int orc_error_succes(double err, orc_ctrl* c) {
@@ -415,6 +530,12 @@ int orc_error_succes(double err, orc_ctrl* c) {
 int64_t orc_dp45_run(int n, double* pos, double* vel, const double* mass,
                      const int* charge, const sg_field_params* fp, orc_ctrl* c,
                      int64_t max_steps, double* hist, int64_t hist_cap) {
+    return orc_rk_run(5, n, pos, vel, mass, charge, fp, c, max_steps, hist, hist_cap);
+}
+
+int64_t orc_rk_run(int method, int n, double* pos, double* vel, const double* mass,
+                   const int* charge, const sg_field_params* fp, orc_ctrl* c,
+                   int64_t max_steps, double* hist, int64_t hist_cap) {
     double* k = (double*)malloc(sizeof(double) * 7 * 6 * (size_t)n);
     double* pos2 = (double*)malloc(sizeof(double) * 3 * (size_t)n);
     double* vel2 = (double*)malloc(sizeof(double) * 3 * (size_t)n);
@@ -430,7 +551,9 @@ int64_t orc_dp45_run(int n, double* pos, double* vel, const double* mass,
         int rejects_here = 0;
         for (;;) {
             double tstart = c->t, hs = c->h;
-            double err = orc_dp45_attempt(n, pos, vel, mass, charge, fp, c, pos2, vel2, k, derivs);
+            double err = method == 4
+                             ? orc_ck45_attempt(n, pos, vel, mass, charge, fp, c, pos2, vel2, k, derivs)
+                             : orc_dp45_attempt(n, pos, vel, mass, charge, fp, c, pos2, vel2, k, derivs);
             int acc = 1;
             if (!isfinite(err)) {
                 c->status = SG_NONFINITE;
@@ -473,6 +596,12 @@ out:
 
 int orc_dp45_replay(int n, double* pos, double* vel, const double* mass, const int* charge,
                     const sg_field_params* fp, const double* ts, const double* hs, int nsteps) {
+    return orc_rk_replay(5, n, pos, vel, mass, charge, fp, ts, hs, nsteps);
+}
+
+int orc_rk_replay(int method, int n, double* pos, double* vel, const double* mass,
+                  const int* charge, const sg_field_params* fp, const double* ts,
+                  const double* hs, int nsteps) {
     double* k = (double*)malloc(sizeof(double) * 7 * 6 * (size_t)n);
     double* pos2 = (double*)malloc(sizeof(double) * 3 * (size_t)n);
     double* vel2 = (double*)malloc(sizeof(double) * 3 * (size_t)n);
@@ -488,7 +617,10 @@ int orc_dp45_replay(int n, double* pos, double* vel, const double* mass, const i
     for (int s = 0; s < nsteps; s++) {
         c.t = ts[s];
         c.h = hs[s];
-        orc_dp45_attempt(n, pos, vel, mass, charge, fp, &c, pos2, vel2, k, derivs);
+        if (method == 4)
+            orc_ck45_attempt(n, pos, vel, mass, charge, fp, &c, pos2, vel2, k, derivs);
+        else
+            orc_dp45_attempt(n, pos, vel, mass, charge, fp, &c, pos2, vel2, k, derivs);
         memcpy(pos, pos2, sizeof(double) * 3 * (size_t)n);
         memcpy(vel, vel2, sizeof(double) * 3 * (size_t)n);
     }

@@ -76,6 +76,20 @@ double orc_dp45_attempt(int n, const double* pos, const double* vel, const doubl
                         const int* charge, const sg_field_params* fp, orc_ctrl* c,
                         double* pos2, double* vel2, double* k, double* derivs);
 
+/* One Cash-Karp 5(4) attempt, the reference's "RungaKutta4" (bin/ode.cpp:220-345):
+ * 6 stages, 5th-order solution into pos2/vel2.  As in the reference the error sum
+ * starts from the previous error norm (odev.err is never reset there), carried in
+ * c->err.  k is scratch of 6*n*6 doubles. */
+double orc_ck45_attempt(int n, const double* pos, const double* vel, const double* mass,
+                        const int* charge, const sg_field_params* fp, orc_ctrl* c,
+                        double* pos2, double* vel2, double* k, double* derivs);
+
+/* Step loop with the method of the reference's Init_ode order: 5 = Dormand-Prince,
+ * 4 = Cash-Karp.  Same contract as orc_dp45_run. */
+int64_t orc_rk_run(int method, int n, double* pos, double* vel, const double* mass,
+                   const int* charge, const sg_field_params* fp, orc_ctrl* c,
+                   int64_t max_steps, double* hist, int64_t hist_cap);
+
 /* error_succes (bin/ode.cpp:426-457): 1 = accepted. */
 int orc_error_succes(double err, orc_ctrl* c);
 
@@ -92,6 +106,10 @@ int64_t orc_dp45_run(int n, double* pos, double* vel, const double* mass,
  * replay the step sequence another implementation accepted. */
 int orc_dp45_replay(int n, double* pos, double* vel, const double* mass, const int* charge,
                     const sg_field_params* fp, const double* ts, const double* hs, int nsteps);
+/* The same with method 5 (Dormand-Prince) or 4 (Cash-Karp). */
+int orc_rk_replay(int method, int n, double* pos, double* vel, const double* mass,
+                  const int* charge, const sg_field_params* fp, const double* ts,
+                  const double* hs, int nsteps);
 
 /* Moments of one cloud: out[12] as sg_batch_moments. */
 void orc_moments(int n, const double* pos, const double* vel, const double* mass,

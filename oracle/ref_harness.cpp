@@ -22,6 +22,7 @@
 
 /* defined at global scope in bin/ode.cpp:61 and :426 */
 double Dormand_Prince_5(IonCloud& _cloud, _ode_vars& odev);
+double RungaKutta4(IonCloud& _cloud, _ode_vars& odev);
 bool error_succes(const double err, _ode_vars& odev);
 
 namespace {
@@ -36,7 +37,7 @@ struct RefRun {
 void setup(RefRun& r, int n, const double* pos, const double* vel, const double* mass,
            const int* charge, int trap, int tof, int coulomb, double coulomb_scale,
            const double* trapp, double t0, double h0, int adaptive, double rtol,
-           double atol) {
+           double atol, int method = 5) {
     char tmpl[] = "/tmp/simgb_refXXXXXX";
     char* dir = mkdtemp(tmpl);
     r.prefix = std::string(dir ? dir : "/tmp") + "/run";
@@ -51,7 +52,8 @@ void setup(RefRun& r, int n, const double* pos, const double* vel, const double*
                    vel[3 * i + 2]);
         r.cloud.AddParticle(p, ion);
     }
-    r.odev.Init_ode(5, h0, adaptive != 0);
+    r.odev.Init_ode(method, h0, adaptive != 0);
+    r.odev.err = 0.0;  // the Cash-Karp error sum starts from the previous norm
     r.odev.rk_rtol = rtol;
     r.odev.rk_atol = atol;
     r.odev.Initpoolvectors(n);
@@ -112,7 +114,8 @@ int ref_force(int n, const double* pos, const double* vel, const double* mass,
     return 0;
 }
 
-/* Dormand-Prince run.  mode 0: call the reference step() (bin/ode.cpp:459-494)
+/* Runge-Kutta run, method 5 = Dormand-Prince, 4 = Cash-Karp (Init_ode's order).
+ * mode 0: call the reference step() (bin/ode.cpp:459-494)
  * until lifetime >= t_end or max_steps steps; mode 1: the same loop written out
  * with the reference's Dormand_Prince_5 and error_succes so each attempt can be
  * recorded as (t_start, h, err, accepted) in hist.  ctrl_out receives
@@ -122,10 +125,11 @@ long long ref_dp45_run(int n, double* pos, double* vel, const double* mass,
                        const int* charge, int trap, int tof, int coulomb,
                        double coulomb_scale, const double* trapp, double t0, double t_end,
                        double h0, int adaptive, double rtol, double atol, long long max_steps,
-                       int mode, double* hist, long long hist_cap, double* ctrl_out) {
+                       int mode, double* hist, long long hist_cap, double* ctrl_out,
+                       int method) {
     RefRun* r = new RefRun;
     setup(*r, n, pos, vel, mass, charge, trap, tof, coulomb, coulomb_scale, trapp, t0, h0,
-          adaptive, rtol, atol);
+          adaptive, rtol, atol, method);
     IonCloud& cl = r->cloud;
     _ode_vars& od = r->odev;
     long long nh = 0, steps = 0;
@@ -137,7 +141,7 @@ long long ref_dp45_run(int n, double* pos, double* vel, const double* mass,
             } else {
                 for (;;) {
                     double ts = cl.lifetime, hs = od.h;
-                    double err = Dormand_Prince_5(cl, od);
+                    double err = method == 4 ? RungaKutta4(cl, od) : Dormand_Prince_5(cl, od);
                     bool acc = true;
                     if (od.change_stepsize) {
                         od.countstep++;

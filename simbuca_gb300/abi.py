@@ -54,7 +54,8 @@ class OdeParams(ctypes.Structure):
     """sg_ode_params (include/simgb.h)."""
     _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double), ("h0", ctypes.c_double),
                 ("t0", ctypes.c_double), ("t_end", ctypes.c_double),
-                ("adaptive", ctypes.c_int32), ("max_rejects", ctypes.c_int32)]
+                ("adaptive", ctypes.c_int32), ("max_rejects", ctypes.c_int32),
+                ("method", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 class StepInfo(ctypes.Structure):

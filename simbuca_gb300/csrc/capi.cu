@@ -19,6 +19,7 @@ namespace {
 struct Problem {
     int n_clouds = 0, n = 0, npad = 0, precision = 0, n_rows = 0, n_items = 0, max_slots = 0;
     int variant = 0;  // FP32c launch shape the items were planned for
+    int method = 5;   // 5 Dormand-Prince, 4 Cash-Karp (every cloud of a batch)
     bool any_coulomb = false;
     bool uploaded = false;
     std::vector<SgCloud> hc;
@@ -38,6 +39,14 @@ struct Problem {
     SgCtrl* hctrl = nullptr;  // pinned mirror of dctrl
     double interactions = 0.0;  // per Coulomb evaluation, all clouds
     std::vector<double> cloud_inter;
+    // ion order: device arrays hold ions in k-d tree order when `sorted`; perm maps a
+    // device position to the caller's ion index
+    bool sorted = false;
+    std::vector<int> perm;
+    int* dperm = nullptr;
+    float* bbox = nullptr;        // [ntiles][8]
+    int ntiles = 0;
+    double *kq0 = nullptr, *qm0 = nullptr, *qd0 = nullptr, *mass0 = nullptr;  // caller order
     // learned step-size proposer and step-history log
     SgProposerState* pst = nullptr;
     void* wbf = nullptr;           // BF16 MLP weights
@@ -119,6 +128,12 @@ void free_problem(Problem& P) {
     cudaFree(P.flags);
     cudaFree(P.pst);
     cudaFree(P.wbf);
+    cudaFree(P.dperm);
+    cudaFree(P.bbox);
+    cudaFree(P.kq0);
+    cudaFree(P.qm0);
+    cudaFree(P.qd0);
+    cudaFree(P.mass0);
     cudaFree(P.log_feat);
     cudaFree(P.log_num);
     if (P.hctrl) cudaFreeHost(P.hctrl);
@@ -130,12 +145,13 @@ inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 // Launch shape for a set of clouds when the context has no explicit choice: the
 // cloud carrying the most pair work decides.  Measured on GB300 (simbuca_gb300/tune.py):
 // 128 threads x 2 ions is fastest up to a few thousand ions per cloud (more blocks,
-// less padding of small i-ranges), 128 x 4 from ~16k ions on.
+// less padding of small i-ranges); from ~16k ions on the ions are put in k-d tree order
+// and far tile pairs take the high parts only.
 int auto_variant(const std::vector<int>& counts, int requested) {
     if (requested >= 0) return requested;
     int big = 0;
     for (int n : counts) big = std::max(big, n);
-    return big <= 8192 ? 1 : 0;
+    return big <= 8192 ? 1 : SG_C32_SORTED;
 }
 
 // Partition clouds into row blocks and Coulomb work items.  Items are sized so that
@@ -149,7 +165,7 @@ void plan(Problem& P, int n_sm) {
     P.hrows.clear();
     P.hitems.clear();
     P.cloud_inter.assign(C, 0.0);
-    int off = 0, poff = 0;
+    int off = 0, poff = 0, tiles = 0;
     P.any_coulomb = false;
     for (int c = 0; c < C; c++) {
         SgCloud& cl = P.hc[c];
@@ -159,6 +175,8 @@ void plan(Problem& P, int n_sm) {
         cl.n = P.counts[c];
         cl.poff = poff;
         cl.npad = round_up(cl.n, SG_PAD);
+        cl.tile0 = tiles;
+        tiles += (cl.npad + 127) / 128;
         cl.rb0 = (int)P.hrows.size();
         for (int i = 0; i < cl.n; i += SG_ROWS) {
             SgRowBlock rb;
@@ -174,7 +192,9 @@ void plan(Problem& P, int n_sm) {
     }
     P.n = off;
     P.npad = poff;
+    P.ntiles = tiles;
     P.n_rows = (int)P.hrows.size();
+    P.sorted = P.precision == SG_PREC_FP32C && P.variant == SG_C32_SORTED;
 
     const bool f32 = P.precision == SG_PREC_FP32C;
     const int ib = f32 ? sg_coulomb_fp32c_ib(P.variant) : SG_C64_IB;
@@ -263,6 +283,40 @@ void set_frame(SgCloud& cl, const double* pos_aos, int off) {
     const double spacing = std::cbrt(vol / std::max(n, 1));
     const double rc = 0.6 * spacing;
     cl.wc = (float)(1.0 / (rc * rc * rc));
+    // far tiles (sorted kernel): beyond every capped pair, and far enough that the
+    // high parts alone give the pair distance to ~1e-6
+    cl.dfar = (float)std::max(0.25, 1.01 * rc);
+}
+
+// k-d tree order of one cloud: recursive median splits along the widest axis, the
+// lower part always a multiple of 128 ions, so that every 128-ion tile is a leaf.
+void kd_order(const double* pos, int off, int n, int* out) {
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; i++) idx[i] = off + i;
+    std::vector<std::pair<int, int>> stack;
+    stack.push_back(std::make_pair(0, n));
+    while (!stack.empty()) {
+        const int b = stack.back().first, e = stack.back().second;
+        stack.pop_back();
+        const int len = e - b;
+        if (len <= 128) continue;
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int i = b; i < e; i++)
+            for (int c = 0; c < 3; c++) {
+                const double v = pos[3 * (size_t)idx[i] + c];
+                lo[c] = std::min(lo[c], v);
+                hi[c] = std::max(hi[c], v);
+            }
+        int ax = 0;
+        for (int c = 1; c < 3; c++)
+            if (hi[c] - lo[c] > hi[ax] - lo[ax]) ax = c;
+        const int m = std::min(len - 1, (len / 2 + 127) / 128 * 128);
+        std::nth_element(idx.begin() + b, idx.begin() + b + m, idx.begin() + e,
+                         [pos, ax](int p, int q) { return pos[3 * (size_t)p + ax] < pos[3 * (size_t)q + ax]; });
+        stack.push_back(std::make_pair(b + m, e));
+        stack.push_back(std::make_pair(b, b + m));
+    }
+    for (int i = 0; i < n; i++) out[i] = idx[i];
 }
 
 int alloc_problem(sg_ctx* ctx, Problem& P) {
@@ -293,6 +347,17 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(cudaMemset(P.pst, 0, sizeof(SgProposerState) * (size_t)std::max(P.n_clouds, 1)));
     CK(cudaMalloc(&P.wbf, SG_MLP_NP * 2));
     CK(cudaMemset(P.wbf, 0, SG_MLP_NP * 2));
+    CK(dalloc(&P.dperm, N));
+    CK(dalloc(&P.bbox, (size_t)std::max(P.ntiles, 1) * 8));
+    CK(dalloc(&P.kq0, N));
+    CK(dalloc(&P.qm0, N));
+    CK(dalloc(&P.qd0, N));
+    CK(dalloc(&P.mass0, N));
+    CK(cudaMemset(P.mass0, 0, N * sizeof(double)));
+    CK(cudaMemset(P.qm0, 0, N * sizeof(double)));
+    P.perm.resize(P.n);
+    for (int i = 0; i < P.n; i++) P.perm[i] = i;
+    CK(cudaMemcpy(P.dperm, P.perm.data(), sizeof(int) * P.n, cudaMemcpyHostToDevice));
     CK(cudaMemset(P.coul1, 0, 3 * N * sizeof(double)));
     CK(cudaMemset(P.part, 0, (size_t)std::max(P.max_slots, 1) * 4 * NP * sizeof(double)));
     CK(cudaMemset(P.coulS, 0, 3 * N * sizeof(double)));
@@ -321,6 +386,7 @@ SgDpArgs dp_args(Problem& P) {
     a.c64 = P.c64;
     a.c32 = P.c32;
     a.err_part = P.err_part;
+    a.bbox = P.sorted ? P.bbox : nullptr;
     a.n = P.n;
     a.npad = P.npad;
     a.fp32c = P.precision == SG_PREC_FP32C ? 1 : 0;
@@ -369,6 +435,7 @@ int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter, double
     ca.npad_total = P.npad;
     ca.errword = P.flags;
     ca.variant = P.variant;
+    ca.bbox = P.bbox;
     TimedLaunch tl{nullptr, nullptr, inter};
     const int cap = ctx->capture_events;
     if (cap >= 0) {
@@ -408,11 +475,22 @@ double active_interactions(Problem& P) {
 int enqueue_attempt(sg_ctx* ctx, Problem& P) {
     SgDpArgs a = dp_args(P);
     const double inter = ctx->timing ? active_interactions(P) : 0.0;
-    CK(sg_dp_stage(a, 1, P.n_rows, ctx->stream));
-    for (int s = 2; s <= 7; s++) {
-        int st = launch_coulomb(ctx, P, true, inter, P.coulS);
-        if (st != SG_OK) return st;
-        CK(sg_dp_stage(a, s, P.n_rows, ctx->stream));
+    if (P.method == 4) {
+        // Cash-Karp: the step start is no stage of the previous step, so its Coulomb
+        // inputs are rebuilt and all six stages take a Coulomb sum
+        CK(sg_coords_from_state(a, P.qd, P.n_rows, ctx->stream));
+        for (int s = 1; s <= 6; s++) {
+            int st = launch_coulomb(ctx, P, true, inter, P.coulS);
+            if (st != SG_OK) return st;
+            CK(sg_ck_stage(a, s, P.n_rows, ctx->stream));
+        }
+    } else {
+        CK(sg_dp_stage(a, 1, P.n_rows, ctx->stream));
+        for (int s = 2; s <= 7; s++) {
+            int st = launch_coulomb(ctx, P, true, inter, P.coulS);
+            if (st != SG_OK) return st;
+            CK(sg_dp_stage(a, s, P.n_rows, ctx->stream));
+        }
     }
     CK(sg_dp_control(P.dc, P.dctrl, P.err_part, P.y, P.n_clouds, P.flags + 1, ctx->stream));
     CK(sg_dp_commit(a, P.n_rows, ctx->stream));
@@ -558,13 +636,27 @@ void ion_constants(const Problem& P, const double* mass, const int* charge,
 }
 
 // Uploads positions/velocities (AoS host) into y and rebuilds the Coulomb inputs.
+// Uploads positions/velocities (AoS host, caller's order) into y -- in k-d tree order for
+// the sorted kernel -- brings the per-ion constants into the same order and rebuilds the
+// Coulomb inputs.  The constants in the caller's order (kq0, qm0, qd0, mass0) must be on
+// the device already.
 int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel) {
     const size_t N = (size_t)P.n;
+    if (P.sorted) {
+        for (int c = 0; c < P.n_clouds; c++)
+            kd_order(pos, P.hc[c].off, P.hc[c].n, P.perm.data() + P.hc[c].off);
+        CK(cudaMemcpyAsync(P.dperm, P.perm.data(), sizeof(int) * N, cudaMemcpyHostToDevice,
+                           ctx->stream));
+    }
     CK(cudaMemcpyAsync(P.stage, pos, 3 * N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     if (vel)
         CK(cudaMemcpyAsync(P.stage + 3 * N, vel, 3 * N * sizeof(double), cudaMemcpyHostToDevice,
                            ctx->stream));
-    CK(sg_aos_to_soa(P.stage, vel ? P.stage + 3 * N : nullptr, P.y, P.n, ctx->stream));
+    CK(sg_aos_to_soa(P.stage, vel ? P.stage + 3 * N : nullptr, P.dperm, P.y, P.n, ctx->stream));
+    CK(sg_gather(P.kq0, P.dperm, P.kq, P.n, ctx->stream));
+    CK(sg_gather(P.qm0, P.dperm, P.qm, P.n, ctx->stream));
+    CK(sg_gather(P.qd0, P.dperm, P.qd, P.n, ctx->stream));
+    CK(sg_gather(P.mass0, P.dperm, P.mass, P.n, ctx->stream));
     for (int c = 0; c < P.n_clouds; c++) {
         set_frame(P.hc[c], pos, P.hc[c].off);
         double v2 = 0.0;
@@ -577,6 +669,8 @@ int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel) 
                        ctx->stream));
     SgDpArgs a = dp_args(P);
     CK(sg_coords_from_state(a, P.qd, P.n_rows, ctx->stream));
+    // the host vectors above are read by queued copies: finish before they go away
+    CK(cudaStreamSynchronize(ctx->stream));
     return SG_OK;
 }
 
@@ -710,14 +804,14 @@ int sg_coulomb_accel(sg_ctx* ctx, int precision, int n, const double* pos, const
     int st = solo_prepare(ctx, n, precision, fp);
     if (st != SG_OK) return st;
     Problem& P = ctx->solo;
-    CK(cudaMemcpyAsync(P.qd, q, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(P.kq, kq, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.qd0, q, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.kq0, kq, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     st = upload_state(ctx, P, pos, nullptr);
     if (st != SG_OK) return st;
     st = launch_coulomb(ctx, P, false, (double)n * (n - 1), P.coulS);
     if (st != SG_OK) return st;
     SgDpArgs a = dp_args(P);
-    CK(sg_force_finish(a, 0.0, 0, P.stage, P.n_rows, ctx->stream));
+    CK(sg_force_finish(a, 0.0, 0, P.dperm, P.stage, P.n_rows, ctx->stream));
     CK(cudaMemcpyAsync(acc, P.stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
     int errword = 0;
     CK(cudaMemcpyAsync(&errword, P.flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -739,9 +833,10 @@ int sg_force(sg_ctx* ctx, int precision, int n, const double* pos, const double*
     Problem& P = ctx->solo;
     std::vector<double> kq, qm, qd;
     ion_constants(P, mass, charge, kq, qm, qd);
-    CK(cudaMemcpyAsync(P.qd, qd.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(P.kq, kq.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(P.qm, qm.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.qd0, qd.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.kq0, kq.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.qm0, qm.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.mass0, mass, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     st = upload_state(ctx, P, pos, vel);
     if (st != SG_OK) return st;
     if (fp->flags & SG_F_COULOMB) {
@@ -749,7 +844,7 @@ int sg_force(sg_ctx* ctx, int precision, int n, const double* pos, const double*
         if (st != SG_OK) return st;
     }
     SgDpArgs a = dp_args(P);
-    CK(sg_force_finish(a, t, 1, P.stage, P.n_rows, ctx->stream));
+    CK(sg_force_finish(a, t, 1, P.dperm, P.stage, P.n_rows, ctx->stream));
     CK(cudaMemcpyAsync(acc, P.stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
     int errword = 0;
     CK(cudaMemcpyAsync(&errword, P.flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -766,6 +861,9 @@ int sg_batch_create(sg_ctx* ctx, int n_clouds, const int* counts, const sg_field
     for (int c = 0; c < n_clouds; c++) {
         if (counts[c] <= 0 || check_fp(&fp[c]) != SG_OK) return SG_BAD_ARG;
         if (!(op[c].rtol >= 0.0) || !(op[c].atol >= 0.0) || !(op[c].h0 > 0.0)) return SG_BAD_ARG;
+        const int m = op[c].method == 0 ? 5 : op[c].method;
+        const int m0 = op[0].method == 0 ? 5 : op[0].method;
+        if ((m != 5 && m != 4) || m != m0) return SG_BAD_ARG;
         total += counts[c];
     }
     if (total > (1ll << 30)) return SG_BAD_ARG;
@@ -779,6 +877,7 @@ int sg_batch_create(sg_ctx* ctx, int n_clouds, const int* counts, const sg_field
     P.counts.assign(counts, counts + n_clouds);
     P.precision = precision;
     P.variant = auto_variant(P.counts, ctx->c32_variant);
+    P.method = op[0].method == 0 ? 5 : op[0].method;
     P.hc.assign(n_clouds, SgCloud());
     for (int c = 0; c < n_clouds; c++) P.hc[c].fp = fp[c];
     plan(P, ctx->n_sm);
@@ -795,6 +894,8 @@ int sg_batch_create(sg_ctx* ctx, int n_clouds, const int* counts, const sg_field
         s.atol = op[c].atol;
         s.adaptive = op[c].adaptive;
         s.max_rejects = op[c].max_rejects;
+        s.method = P.method;
+        s.err = 0.0;
         s.status = SG_OK;
         s.done = (s.t >= s.t_end) ? 1 : 0;
     }
@@ -818,10 +919,10 @@ int sg_batch_upload(sg_ctx* ctx, const double* pos, const double* vel, const dou
     std::vector<double> kq, qm, qd;
     ion_constants(P, mass, charge, kq, qm, qd);
     const size_t N = (size_t)P.n;
-    CK(cudaMemcpyAsync(P.kq, kq.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(P.qm, qm.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(P.qd, qd.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(P.mass, mass, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.kq0, kq.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.qm0, qm.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.qd0, qd.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.mass0, mass, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     memcpy(P.hctrl, P.hctrl0.data(), sizeof(SgCtrl) * P.n_clouds);
     CK(cudaMemcpyAsync(P.dctrl, P.hctrl0.data(), sizeof(SgCtrl) * P.n_clouds,
                        cudaMemcpyHostToDevice, ctx->stream));
@@ -863,7 +964,7 @@ int sg_batch_download(sg_ctx* ctx, double* pos, double* vel) {
     if (!P.uploaded) return SG_NOT_READY;
     CK(cudaSetDevice(ctx->device));
     const size_t N = (size_t)P.n;
-    CK(sg_soa_to_aos(P.y, P.stage, P.stage + 3 * N, P.n, ctx->stream));
+    CK(sg_soa_to_aos(P.y, P.dperm, P.stage, P.stage + 3 * N, P.n, ctx->stream));
     CK(cudaMemcpyAsync(pos, P.stage, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(vel, P.stage + 3 * N, 3 * N * sizeof(double), cudaMemcpyDeviceToHost,
                        ctx->stream));

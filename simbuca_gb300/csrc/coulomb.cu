@@ -236,6 +236,68 @@ __device__ __forceinline__ void tile_pairs(const float* tx, const float* ty, con
     }
 }
 
+
+// Pair term from the high parts only (tiles farther apart than SgCloud::dfar): the
+// quantisation of |u| ~ 1 costs ~1e-7 relative only for pairs this far apart.
+struct PairH {
+    float dx, dy, dz, y3;
+};
+__device__ __forceinline__ PairH pair_hi(float xjh, float yjh, float zjh, float xih, float yih,
+                                         float zih) {
+    PairH p;
+    p.dx = __fsub_rn(xjh, xih);
+    p.dy = __fsub_rn(yjh, yih);
+    p.dz = __fsub_rn(zjh, zih);
+    float r2 = __fmaf_rn(p.dx, p.dx, kTiny);
+    r2 = __fmaf_rn(p.dy, p.dy, r2);
+    r2 = __fmaf_rn(p.dz, p.dz, r2);
+    const float y = rsqrt_approx(r2);
+    p.y3 = __fmul_rn(__fmul_rn(y, y), y);
+    return p;
+}
+
+// Squared distance between two tile bounding boxes (frame units).
+__device__ __forceinline__ float box_dist2(const float* a, const float* b) {
+    float d2 = 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const float g = fmaxf(0.f, fmaxf(b[c] - a[3 + c], a[c] - b[3 + c]));
+        d2 = fmaf(g, g, d2);
+    }
+    return d2;
+}
+
+// Far tiles: packed FP32x2 over j pairs, high parts only, no close pairs possible.
+template <int IPT>
+__device__ __forceinline__ void tile_pairs_far(const float* tx, const float* ty, const float* tz,
+                                               const float* tq, int jb, int je, const f2* xh,
+                                               const f2* yh, const f2* zh, f2 tiny2, f2* ax,
+                                               f2* ay, f2* az) {
+#pragma unroll 2
+    for (int jj = jb; jj < je; jj += 2) {
+        const f2 Xj = *reinterpret_cast<const f2*>(tx + jj);
+        const f2 Yj = *reinterpret_cast<const f2*>(ty + jj);
+        const f2 Zj = *reinterpret_cast<const f2*>(tz + jj);
+        const f2 Qj = *reinterpret_cast<const f2*>(tq + jj);
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            const f2 dx = sub2(Xj, xh[k]);
+            const f2 dy = sub2(Yj, yh[k]);
+            const f2 dz = sub2(Zj, zh[k]);
+            f2 r2 = fma2(dx, dx, tiny2);
+            r2 = fma2(dy, dy, r2);
+            r2 = fma2(dz, dz, r2);
+            float ra, rb;
+            upk(r2, ra, rb);
+            const f2 y = pk(rsqrt_approx(ra), rsqrt_approx(rb));
+            const f2 w = mul2(Qj, mul2(mul2(y, y), y));
+            ax[k] = fma2(w, dx, ax[k]);
+            ay[k] = fma2(w, dy, ay[k]);
+            az[k] = fma2(w, dz, az[k]);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // FP32c kernel.  Global layout: c32 = 7 float arrays of npad_total entries
 // (x, y, z, q, xl, yl, zl in frame units); shared tile = the same 7 arrays of SG_TILE.
@@ -434,6 +496,216 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
     }
 }
 
+template <int NT, int IPT>
+__global__ void __launch_bounds__(NT, 4) coulomb_fp32c_sorted_kernel(const float* __restrict__ c32,
+                                                            const double* __restrict__ c64,
+                                                            const SgWorkItem* __restrict__ items,
+                                                            const SgCloud* __restrict__ clouds,
+                                                            const SgCtrl* __restrict__ ctrl,
+                                                            double* __restrict__ part,
+                                                            int npad_total, int* errword,
+                                                            const float* __restrict__ bbox) {
+    constexpr int T = SG_TILE;
+    __shared__ __align__(128) float tile[SG_STAGES][7][T];
+    __shared__ __align__(8) uint64_t full[SG_STAGES];
+    __shared__ double corr[3][NT * IPT];
+
+    const SgWorkItem it = items[blockIdx.x];
+    if (ctrl != nullptr && (ctrl[it.cloud].done || ctrl[it.cloud].hold || ctrl[it.cloud].status != SG_OK)) return;
+    const SgCloud& cl = clouds[it.cloud];
+    const float wc = cl.wc;
+    const double invL2 = cl.invL * cl.invL;
+    const int tid = threadIdx.x;
+    const float* X = c32;
+    const float* Y = c32 + npad_total;
+    const float* Z = c32 + 2 * (size_t)npad_total;
+    const float* XL = c32 + 4 * (size_t)npad_total;
+    const float* YL = c32 + 5 * (size_t)npad_total;
+    const float* ZL = c32 + 6 * (size_t)npad_total;
+
+    // i-ions of this thread: it.i0 + tid + k*NT (clamped into the item for loads)
+    int ipad[IPT];
+    f2 xh[IPT], yh[IPT], zh[IPT], xl[IPT], yl[IPT], zl[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        int li = IPT * tid + k;  // contiguous: warp w holds the 128-ion tile w of the block
+        int ii = it.i0 + (li < it.ni ? li : 0);
+        ipad[k] = li < it.ni ? ii : -1;
+        float a = X[ii], b = Y[ii], c = Z[ii], d = XL[ii], e = YL[ii], f = ZL[ii];
+        xh[k] = pk(a, a);
+        yh[k] = pk(b, b);
+        zh[k] = pk(c, c);
+        xl[k] = pk(d, d);
+        yl[k] = pk(e, e);
+        zl[k] = pk(f, f);
+        corr[0][li] = 0.0;
+        corr[1][li] = 0.0;
+        corr[2][li] = 0.0;
+    }
+    float ks[IPT][3], kc[IPT][3], s2[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        s2[k] = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; c++) ks[k][c] = kc[k][c] = 0.f;
+    }
+
+    const int ntiles = (it.nj + T - 1) / T;
+    bool ok = true;
+    if (tid == 0) {
+        for (int s = 0; s < SG_STAGES; s++) mbar_init(&full[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    // prologue: fill the ring
+    if (tid == 0) {
+        for (int s = 0; s < SG_STAGES && s < ntiles; s++) {
+            const int j0 = it.j0 + s * T;
+            const int len = min(T, it.j0 + it.nj - j0);
+            const uint32_t bytes = (uint32_t)len * 4u;
+            mbar_arrive_tx(&full[s], 7u * bytes);
+            for (int a = 0; a < 7; a++)
+                bulk_g2s(&tile[s][a][0], c32 + (size_t)a * npad_total + j0, bytes, &full[s]);
+        }
+    }
+
+    const f2 tiny2 = pk(kTiny, kTiny);
+    // bounds of this warp's 128 i-ions (a k-d tree leaf after sorting)
+    float wbox[6];
+    {
+        // warps past the cloud's last ion read the last tile (their results are dropped)
+        const int last = (cl.npad + 127) / 128 - 1;
+        const int wt = cl.tile0 + min(last, (it.i0 - cl.poff) / 128 + (tid >> 5) * (32 * IPT) / 128);
+        for (int q = 0; q < 6; q++) wbox[q] = bbox[8 * (size_t)wt + q];
+    }
+    const float dfar2 = cl.dfar * cl.dfar;
+    // Small clouds fold partial sums every 16 j-ions so that the squared partial sums
+    // still estimate sum_j |f_ij|^2 when the whole cloud is one or two tiles.
+    const int flush_len = (cl.npad <= 2048) ? 16 : SG_TILE;
+    for (int t = 0; t < ntiles; t++) {
+        const int s = t % SG_STAGES;
+        const uint32_t parity = (uint32_t)((t / SG_STAGES) & 1);
+        const int j0 = it.j0 + t * T;
+        const int len = min(T, it.j0 + it.nj - j0);
+        const bool arrived = mbar_wait(&full[s], parity);
+        if (!__syncthreads_and(arrived)) {  // block-uniform decision
+            ok = false;
+            if (tid == 0) {
+                atomicExch(errword, SG_TIMEOUT);
+                // drain the copies still in flight (tiles t .. t+STAGES-1), bounded
+                for (int u = t; u < ntiles && u < t + SG_STAGES; u++)
+                    (void)mbar_wait(&full[u % SG_STAGES], (uint32_t)((u / SG_STAGES) & 1));
+            }
+            __syncthreads();
+            break;
+        }
+
+        float y3max[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) y3max[k] = 0.f;
+        const float* tx = tile[s][0];
+        const float* ty = tile[s][1];
+        const float* tz = tile[s][2];
+        const float* tq = tile[s][3];
+        const float* txl = tile[s][4];
+        const float* tyl = tile[s][5];
+        const float* tzl = tile[s][6];
+        // The tile holding this block's own ions takes the variant that keeps the self
+        // pair (dx = 0, contributes nothing) out of the close-pair flag.
+        const bool diag = (j0 < it.i0 + it.ni) && (j0 + len > it.i0);
+        float jbox[6];
+        const int jt = cl.tile0 + (j0 - cl.poff) / 128;
+        for (int q = 0; q < 6; q++) jbox[q] = bbox[8 * (size_t)jt + q];
+        const bool far = !diag && box_dist2(wbox, jbox) > dfar2;  // uniform per warp
+        for (int jb = 0; jb < len; jb += flush_len) {
+            const int je = min(len, jb + flush_len);
+            f2 ax[IPT], ay[IPT], az[IPT];
+#pragma unroll
+            for (int k = 0; k < IPT; k++) ax[k] = ay[k] = az[k] = 0ull;
+            if (far)
+                tile_pairs_far<IPT>(tx, ty, tz, tq, jb, je, xh, yh, zh, tiny2, ax, ay, az);
+            else if (!diag)
+                tile_pairs<IPT, false>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh, zh,
+                                       xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
+            else
+                tile_pairs<IPT, true>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh, zh,
+                                      xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
+            // fold the partial sums into the compensated accumulators
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                float a, b;
+                upk(ax[k], a, b);
+                const float tx_ = __fadd_rn(a, b);
+                upk(ay[k], a, b);
+                const float ty_ = __fadd_rn(a, b);
+                upk(az[k], a, b);
+                const float tz_ = __fadd_rn(a, b);
+                kahan_add(ks[k][0], kc[k][0], tx_);
+                kahan_add(ks[k][1], kc[k][1], ty_);
+                kahan_add(ks[k][2], kc[k][2], tz_);
+                // sum of squared partial sums: estimates sum_j |f_ij|^2 (conditioning test)
+                s2[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2[k])));
+            }
+        }
+        // close pairs of this tile, one flagged ion at a time by the whole warp
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            unsigned m = __ballot_sync(0xffffffffu, y3max[k] > wc && ipad[k] >= 0);
+            while (m) {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                float a, dummy;
+                upk(xh[k], a, dummy);
+                const float xih = __shfl_sync(0xffffffffu, a, src);
+                upk(yh[k], a, dummy);
+                const float yih = __shfl_sync(0xffffffffu, a, src);
+                upk(zh[k], a, dummy);
+                const float zih = __shfl_sync(0xffffffffu, a, src);
+                upk(xl[k], a, dummy);
+                const float xil = __shfl_sync(0xffffffffu, a, src);
+                upk(yl[k], a, dummy);
+                const float yil = __shfl_sync(0xffffffffu, a, src);
+                upk(zl[k], a, dummy);
+                const float zil = __shfl_sync(0xffffffffu, a, src);
+                const int igs = __shfl_sync(0xffffffffu, ipad[k], src);
+                double ox, oy, oz;
+                close_pairs_warp(tile[s], len, j0, igs, xih, yih, zih, xil, yil, zil, wc, invL2,
+                                 c64, npad_total, ox, oy, oz);
+                if ((tid & 31) == src) {
+                    const int li = IPT * tid + k;
+                    corr[0][li] += ox;
+                    corr[1][li] += oy;
+                    corr[2][li] += oz;
+                }
+            }
+        }
+        __syncthreads();  // every thread is done with ring slot s
+        if (tid == 0 && t + SG_STAGES < ntiles) {
+            fence_proxy_async();
+            const int jn = it.j0 + (t + SG_STAGES) * T;
+            const int ln = min(T, it.j0 + it.nj - jn);
+            const uint32_t bytes = (uint32_t)ln * 4u;
+            mbar_arrive_tx(&full[s], 7u * bytes);
+            for (int a = 0; a < 7; a++)
+                bulk_g2s(&tile[s][a][0], c32 + (size_t)a * npad_total + jn, bytes, &full[s]);
+        }
+    }
+    if (!ok) return;
+    double* P = part + (size_t)it.slot * 4 * npad_total;
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        if (ipad[k] < 0) continue;
+        const int li = IPT * tid + k;
+        const int ig = ipad[k];
+        P[3 * (size_t)npad_total + ig] = (double)s2[k];
+        // P_i = sum q_j (x_i - x_j)/r^3 = -invL^2 sum w (u_j - u_i) + close-pair terms
+        P[ig] = -invL2 * ((double)ks[k][0] - (double)kc[k][0]) + corr[0][li];
+        P[npad_total + ig] = -invL2 * ((double)ks[k][1] - (double)kc[k][1]) + corr[1][li];
+        P[2 * (size_t)npad_total + ig] =
+            -invL2 * ((double)ks[k][2] - (double)kc[k][2]) + corr[2][li];
+    }
+}
+
 // ---------------------------------------------------------------------------
 // FP64 kernel (plain form).  c64 = 4 double arrays (x, y, z, q) in SI units.
 // ---------------------------------------------------------------------------
@@ -528,7 +800,8 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     const SgRowBlock* __restrict__ rows, const SgCloud* __restrict__ clouds,
     const SgCtrl* __restrict__ ctrl, const double* __restrict__ part,
     const float* __restrict__ c32, const double* __restrict__ c64, int npad_total,
-    double* __restrict__ out, int n_total, int* __restrict__ counters) {
+    double* __restrict__ out, int n_total, int* __restrict__ counters,
+    const float* __restrict__ bbox) {
     __shared__ int list[SG_ROWS];
     __shared__ int nl;
     __shared__ double cx[SG_ROWS], cy[SG_ROWS], cz[SG_ROWS], pm[SG_ROWS];
@@ -572,11 +845,24 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
             const float xil = c32[4 * NP + igk], yil = c32[5 * NP + igk], zil = c32[6 * NP + igk];
             const double xi = c64[igk], yi = c64[NP + igk], zi = c64[2 * NP + igk];
             double ax = 0.0, ay = 0.0, az = 0.0;
+            const float* ibox = bbox ? bbox + 8 * (size_t)(cl.tile0 + (igk - cl.poff) / 128) : nullptr;
             for (int j = lane; j < cl.npad; j += 32) {
                 const int jg = cl.poff + j;
-                const PairF p = pair_f32(c32[jg], c32[NP + jg], c32[2 * NP + jg], c32[4 * NP + jg],
-                                         c32[5 * NP + jg], c32[6 * NP + jg], xih, yih, zih, xil,
-                                         yil, zil);
+                PairF p = pair_f32(c32[jg], c32[NP + jg], c32[2 * NP + jg], c32[4 * NP + jg],
+                                   c32[5 * NP + jg], c32[6 * NP + jg], xih, yih, zih, xil, yil,
+                                   zil);
+                if (ibox != nullptr) {
+                    // the sorted kernel summed this pair from the high parts if its tiles are far
+                    const float* jbox = bbox + 8 * (size_t)(cl.tile0 + j / 128);
+                    const bool same = (igk - cl.poff) / 128 == j / 128;
+                    if (!same && box_dist2(ibox, jbox) > cl.dfar * cl.dfar) {
+                        const PairH q = pair_hi(c32[jg], c32[NP + jg], c32[2 * NP + jg], xih, yih, zih);
+                        p.dx = q.dx;
+                        p.dy = q.dy;
+                        p.dz = q.dz;
+                        p.y3 = q.y3;
+                    }
+                }
                 if (p.y3 > thr3 && p.y3 <= wc && jg != igk) {
                     const float wf = __fmul_rn(c32[3 * NP + jg], p.y3);
                     const double rx = xi - c64[jg], ry = yi - c64[NP + jg], rz = zi - c64[2 * NP + jg];
@@ -615,7 +901,8 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
 
 // Launch shapes of the FP32c kernel (threads per block, ions per thread); the work
 // planner sizes i-blocks as threads x ions.  Variant 0 is the default.
-static const int kC32Shapes[SG_C32_VARIANTS][2] = {{128, 4}, {128, 2}, {256, 2}, {64, 4}};
+static const int kC32Shapes[SG_C32_VARIANTS][2] = {{128, 4}, {128, 2}, {256, 2}, {64, 4},
+                                                   {128, 4}};
 
 int sg_coulomb_fp32c_ib(int variant) {
     if (variant < 0 || variant >= SG_C32_VARIANTS) variant = 0;
@@ -637,6 +924,10 @@ cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s) {
             coulomb_fp32c_kernel<64, 4><<<a.n_items, 64, 0, s>>>(
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
             break;
+        case SG_C32_SORTED:
+            coulomb_fp32c_sorted_kernel<128, 4><<<a.n_items, 128, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            break;
         default:
             coulomb_fp32c_kernel<128, 4><<<a.n_items, 128, 0, s>>>(
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
@@ -656,12 +947,12 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
                                      cudaStream_t s) {
     if (n_rows <= 0) return cudaSuccess;
     if (fp32c)
-        coulomb_reduce_kernel<true><<<n_rows, SG_ROWS, 0, s>>>(rows, a.clouds, a.ctrl, a.part, a.c32,
-                                                              a.c64, a.npad_total, out, n_total,
-                                                              counters);
+        coulomb_reduce_kernel<true><<<n_rows, SG_ROWS, 0, s>>>(
+            rows, a.clouds, a.ctrl, a.part, a.c32, a.c64, a.npad_total, out, n_total, counters,
+            a.variant == SG_C32_SORTED ? a.bbox : nullptr);
     else
-        coulomb_reduce_kernel<false><<<n_rows, SG_ROWS, 0, s>>>(rows, a.clouds, a.ctrl, a.part,
-                                                               a.c32, a.c64, a.npad_total, out,
-                                                               n_total, counters);
+        coulomb_reduce_kernel<false><<<n_rows, SG_ROWS, 0, s>>>(
+            rows, a.clouds, a.ctrl, a.part, a.c32, a.c64, a.npad_total, out, n_total, counters,
+            nullptr);
     return cudaGetLastError();
 }

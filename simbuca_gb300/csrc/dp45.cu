@@ -43,7 +43,7 @@ __constant__ double c_e[8] = {0,
 typedef SgDpArgs DpArgs;
 
 __device__ __forceinline__ void write_coords(const DpArgs& a, const SgCloud& cl, int ig,
-                                             double x, double y, double z) {
+                                             double x, double y, double z, float* hu = nullptr) {
     a.c64[ig] = x;
     a.c64[a.npad + ig] = y;
     a.c64[2 * (size_t)a.npad + ig] = z;
@@ -58,6 +58,44 @@ __device__ __forceinline__ void write_coords(const DpArgs& a, const SgCloud& cl,
         a.c32[4 * (size_t)a.npad + ig] = __double2float_rn(u - (double)uh);
         a.c32[5 * (size_t)a.npad + ig] = __double2float_rn(v - (double)vh);
         a.c32[6 * (size_t)a.npad + ig] = __double2float_rn(w - (double)wh);
+        if (hu) {
+            hu[0] = uh;
+            hu[1] = vh;
+            hu[2] = wh;
+        }
+    }
+}
+
+
+// Bounds of the 128-ion tiles covered by a row block (256 ions = 2 tiles of the cloud):
+// min/max of the FP32 frame coordinates of the block's real ions.
+__device__ __forceinline__ void tile_bounds(const DpArgs& a, const SgCloud& cl,
+                                            const SgRowBlock& rb, bool active, float u,
+                                            float v, float w) {
+    __shared__ float sb[SG_ROWS / 32][6];
+    float b[6] = {active ? u : INFINITY, active ? v : INFINITY, active ? w : INFINITY,
+                  active ? u : -INFINITY, active ? v : -INFINITY, active ? w : -INFINITY};
+    for (int o = 16; o > 0; o >>= 1)
+        for (int q = 0; q < 6; q++) {
+            const float x = __shfl_xor_sync(0xffffffffu, b[q], o);
+            b[q] = q < 3 ? fminf(b[q], x) : fmaxf(b[q], x);
+        }
+    const int warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int q = 0; q < 6; q++) sb[warp][q] = b[q];
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        const int h = threadIdx.x;                 // tile 0 or 1 of this row block
+        float r[6];
+        for (int q = 0; q < 6; q++) r[q] = sb[4 * h][q];
+        for (int wv = 4 * h + 1; wv < 4 * h + 4; wv++)
+            for (int q = 0; q < 6; q++) r[q] = q < 3 ? fminf(r[q], sb[wv][q]) : fmaxf(r[q], sb[wv][q]);
+        const int local = rb.i0 - cl.off;          // multiple of SG_ROWS
+        const int tile = local / 128 + h;
+        if (local + 128 * h < cl.n) {
+            float* B = a.bbox + 8 * (size_t)(cl.tile0 + tile);
+            for (int q = 0; q < 6; q++) B[q] = r[q];
+        }
     }
 }
 
@@ -80,6 +118,7 @@ __global__ void __launch_bounds__(SG_ROWS) dp_stage_kernel(DpArgs a) {
     const double ts = frozen ? cs.t : cs.t + c_c[S] * h;
 
     double acc2 = 0.0;
+    float hu[3] = {0.f, 0.f, 0.f};
     if (active) {
         const double* st = (S == 1) ? a.y : a.ys;
         const double px = st[i], py = st[N + i], pz = st[2 * N + i];
@@ -124,7 +163,7 @@ __global__ void __launch_bounds__(SG_ROWS) dp_stage_kernel(DpArgs a) {
             }
 #pragma unroll
             for (int c = 0; c < 6; c++) a.ys[c * N + i] = out[c];
-            write_coords(a, cl, ig, out[0], out[1], out[2]);
+            write_coords(a, cl, ig, out[0], out[1], out[2], hu);
         } else {
             // embedded error of the attempt (bin/ode.cpp:189-205); y5 = stage-7 state
             const double rtol = cs.rtol, atol = cs.atol;
@@ -142,6 +181,7 @@ __global__ void __launch_bounds__(SG_ROWS) dp_stage_kernel(DpArgs a) {
             }
         }
     }
+    if (S < 7 && a.fp32c && a.bbox) tile_bounds(a, cl, rb, active, hu[0], hu[1], hu[2]);
     if (S == 7) {
         // deterministic block reduction -> one partial per row block
         for (int o = 16; o > 0; o >>= 1) acc2 += __shfl_down_sync(0xffffffffu, acc2, o);
@@ -151,6 +191,114 @@ __global__ void __launch_bounds__(SG_ROWS) dp_stage_kernel(DpArgs a) {
             double s = 0.0;
             for (int w = 0; w < SG_ROWS / 32; w++) s += red[w];
             a.err_part[blockIdx.x] = s;
+        }
+    }
+}
+
+
+// ---- Cash-Karp 5(4), the reference's "RungaKutta4" (bin/ode.cpp:220-345) ----------
+__constant__ double c_ck_a[7][6] = {
+    {0, 0, 0, 0, 0, 0},
+    {0, 0, 0, 0, 0, 0},
+    {0.2, 0, 0, 0, 0, 0},
+    {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0, 0},
+    {0.3, -0.9, 1.2, 0, 0, 0},
+    {-11.0 / 54.0, 2.5, -70.0 / 27.0, 35.0 / 27.0, 0, 0},
+    {1631.0 / 55296.0, 175.0 / 512.0, 575.0 / 13824.0, 44275.0 / 110592.0, 253.0 / 4096.0, 0}};
+__constant__ double c_ck_c[7] = {0, 0.0, 0.2, 0.3, 0.6, 1.0, 0.875};
+__constant__ double c_ck_b[7] = {0, 37.0 / 378.0, 0.0, 250.0 / 621.0, 125.0 / 594.0, 0.0,
+                                 512.0 / 1771.0};
+__constant__ double c_ck_e[7] = {0,
+                                 37.0 / 378.0 - 2825.0 / 27648.0,
+                                 0.0,
+                                 250.0 / 621.0 - 18575.0 / 48384.0,
+                                 125.0 / 594.0 - 13525.0 / 55296.0,
+                                 -277.00 / 14336.0,
+                                 512.0 / 1771.0 - 0.25};
+
+// Stage S (1..6) of Cash-Karp: finish its force (the Coulomb sum of every stage comes
+// from coulS: no stage coincides with the next step's start), store k_S, build stage
+// S+1, or for S = 6 the 5th-order solution (into ys) and the embedded error.
+template <int S>
+__global__ void __launch_bounds__(SG_ROWS) ck_stage_kernel(DpArgs a) {
+    __shared__ double red[SG_ROWS / 32];
+    const SgRowBlock rb = a.rows[blockIdx.x];
+    const SgCtrl& cs = a.ctrl[rb.cloud];
+    if (cs.done || cs.hold || cs.status != SG_OK) return;
+    const SgCloud& cl = a.clouds[rb.cloud];
+    const int li = threadIdx.x;
+    const bool active = li < rb.n;
+    const int i = rb.i0 + (active ? li : 0);
+    const int ig = cl.poff + (i - cl.off);
+    const size_t N = (size_t)a.n;
+    const double h = cs.h;
+    const bool frozen = (cl.fp.flags & SG_F_FROZEN_T) != 0;
+    const double ts = frozen ? cs.t : cs.t + c_ck_c[S] * h;
+    double acc2 = 0.0;
+    float hu[3] = {0.f, 0.f, 0.f};
+    if (active) {
+        const double* st = (S == 1) ? a.y : a.ys;
+        const double px = st[i], py = st[N + i], pz = st[2 * N + i];
+        const double vx = st[3 * N + i], vy = st[4 * N + i], vz = st[5 * N + i];
+        double cx = 0.0, cy = 0.0, cz = 0.0;
+        if (cl.fp.flags & SG_F_COULOMB) {
+            cx = a.coulS[i];
+            cy = a.coulS[N + i];
+            cz = a.coulS[2 * N + i];
+        }
+        double fx, fy, fz;
+        sg_field_accel(cl.fp, ts, a.qm[i], px, py, pz, vx, vy, vz, fx, fy, fz);
+        const double kqi = a.kq[i];
+        double* kS = a.k + (size_t)(S - 1) * 6 * N;
+        kS[i] = vx;
+        kS[N + i] = vy;
+        kS[2 * N + i] = vz;
+        kS[3 * N + i] = fx + kqi * cx;
+        kS[4 * N + i] = fy + kqi * cy;
+        kS[5 * N + i] = fz + kqi * cz;
+        if (S < 6) {
+            double out[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+                double sum = 0.0;
+#pragma unroll
+                for (int j = 1; j <= S; j++) sum += c_ck_a[S + 1][j - 1] * a.k[((size_t)(j - 1) * 6 + c) * N + i];
+                out[c] = a.y[c * N + i] + h * sum;
+            }
+#pragma unroll
+            for (int c = 0; c < 6; c++) a.ys[c * N + i] = out[c];
+            write_coords(a, cl, ig, out[0], out[1], out[2], hu);
+        } else {
+            const double rtol = cs.rtol, atol = cs.atol;
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+                double b = 0.0, e = 0.0;
+#pragma unroll
+                for (int j = 1; j <= 6; j++) {
+                    const double kj = a.k[((size_t)(j - 1) * 6 + c) * N + i];
+                    b += c_ck_b[j] * kj;
+                    e += c_ck_e[j] * kj;
+                }
+                const double y0 = a.y[c * N + i];
+                const double y5 = y0 + h * b;
+                a.ys[c * N + i] = y5;
+                const double yerr = h * e;
+                const double m0 = fabs(y0), m1 = fabs(y5);
+                const double sk = atol + rtol * ((m0 < m1) ? m1 : m0);
+                const double r = yerr / sk;
+                acc2 += r * r;
+            }
+        }
+    }
+    if (S < 6 && a.fp32c && a.bbox) tile_bounds(a, cl, rb, active, hu[0], hu[1], hu[2]);
+    if (S == 6) {
+        for (int o = 16; o > 0; o >>= 1) acc2 += __shfl_down_sync(0xffffffffu, acc2, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc2;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double sum = 0.0;
+            for (int w = 0; w < SG_ROWS / 32; w++) sum += red[w];
+            a.err_part[blockIdx.x] = sum;
         }
     }
 }
@@ -170,10 +318,12 @@ __global__ void dp_control_kernel(const SgCloud* __restrict__ clouds, SgCtrl* __
         return;
     }
     double s = 0.0;
+    // Cash-Karp: the reference adds to the previous norm, odev.err is never reset there
+    if (cs.method == 4) s = cs.err;
     for (int b = 0; b < cl.nrb; b++) s += err_part[cl.rb0 + b];
     const double err = sqrt(s / (6 * cl.n));
     cs.err = err;
-    cs.force_evals += 7;
+    cs.force_evals += (cs.method == 4) ? 6 : 7;
     cs.coulomb_evals += (cl.fp.flags & SG_F_COULOMB) ? 6 : 0;
     int accepted = 1;
     if (!isfinite(err)) {
@@ -254,13 +404,15 @@ __global__ void __launch_bounds__(SG_ROWS) coords_from_state_kernel(DpArgs a,
     const size_t N = (size_t)a.n;
     // this block also covers the ghost tail of its cloud when it holds the cloud's last row
     const bool last = (rb.i0 + rb.n == cl.off + cl.n);
+    float hu[3] = {0.f, 0.f, 0.f};
     if (li < rb.n) {
         const int i = rb.i0 + li;
         const int ig = cl.poff + (i - cl.off);
-        write_coords(a, cl, ig, a.y[i], a.y[N + i], a.y[2 * N + i]);
+        write_coords(a, cl, ig, a.y[i], a.y[N + i], a.y[2 * N + i], hu);
         a.c64[3 * (size_t)a.npad + ig] = q[i];
         if (a.fp32c) a.c32[3 * (size_t)a.npad + ig] = (float)q[i];
     }
+    if (a.fp32c && a.bbox) tile_bounds(a, cl, rb, li < rb.n, hu[0], hu[1], hu[2]);
     if (last) {
         for (int g = cl.n + li; g < cl.npad; g += blockDim.x) {
             const int ig = cl.poff + g;
@@ -287,6 +439,7 @@ __global__ void __launch_bounds__(SG_ROWS) coords_from_state_kernel(DpArgs a,
 // Stand-alone force: out[i][c] (AoS) = field(t) + kq_i * sum_slots P (if Coulomb).
 __global__ void __launch_bounds__(SG_ROWS) force_finish_kernel(DpArgs a, double t,
                                                                int with_field,
+                                                               const int* __restrict__ perm,
                                                                double* __restrict__ out) {
     const SgRowBlock rb = a.rows[blockIdx.x];
     const SgCloud& cl = a.clouds[rb.cloud];
@@ -305,32 +458,43 @@ __global__ void __launch_bounds__(SG_ROWS) force_finish_kernel(DpArgs a, double 
         sg_field_accel(cl.fp, t, a.qm[i], a.y[i], a.y[N + i], a.y[2 * N + i], a.y[3 * N + i],
                        a.y[4 * N + i], a.y[5 * N + i], fx, fy, fz);
     const double kqi = a.kq[i];
-    out[3 * (size_t)i + 0] = fx + kqi * cx;
-    out[3 * (size_t)i + 1] = fy + kqi * cy;
-    out[3 * (size_t)i + 2] = fz + kqi * cz;
+    const size_t o = 3 * (size_t)(perm ? perm[i] : i);
+    out[o + 0] = fx + kqi * cx;
+    out[o + 1] = fy + kqi * cy;
+    out[o + 2] = fz + kqi * cz;
 }
 
 // AoS host layout -> SoA state (positions and velocities).
+// y[c][k] = pos[perm[k]][c]: the caller's order into the device (sorted) order.
 __global__ void aos_to_soa_kernel(const double* __restrict__ pos, const double* __restrict__ vel,
-                                  double* __restrict__ y, int n) {
+                                  const int* __restrict__ perm, double* __restrict__ y, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const size_t N = (size_t)n;
+    const size_t s = 3 * (size_t)(perm ? perm[i] : i);
     for (int c = 0; c < 3; c++) {
-        y[c * N + i] = pos[3 * (size_t)i + c];
-        y[(3 + c) * N + i] = vel ? vel[3 * (size_t)i + c] : 0.0;
+        y[c * N + i] = pos[s + c];
+        y[(3 + c) * N + i] = vel ? vel[s + c] : 0.0;
     }
 }
 
-__global__ void soa_to_aos_kernel(const double* __restrict__ y, double* __restrict__ pos,
-                                  double* __restrict__ vel, int n) {
+// pos[perm[k]][c] = y[c][k]: back to the caller's order.
+__global__ void soa_to_aos_kernel(const double* __restrict__ y, const int* __restrict__ perm,
+                                  double* __restrict__ pos, double* __restrict__ vel, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const size_t N = (size_t)n;
+    const size_t d = 3 * (size_t)(perm ? perm[i] : i);
     for (int c = 0; c < 3; c++) {
-        pos[3 * (size_t)i + c] = y[c * N + i];
-        vel[3 * (size_t)i + c] = y[(3 + c) * N + i];
+        pos[d + c] = y[c * N + i];
+        vel[d + c] = y[(3 + c) * N + i];
     }
+}
+
+__global__ void gather_kernel(const double* __restrict__ src, const int* __restrict__ perm,
+                              double* __restrict__ dst, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[perm ? perm[i] : i];
 }
 
 // Per-row-block moment partials: sum x, x^2 per axis, v^2 per axis, m(vx^2+vy^2), m vz^2.
@@ -385,6 +549,20 @@ cudaError_t sg_dp_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t s
     return cudaGetLastError();
 }
 
+cudaError_t sg_ck_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t st) {
+    if (n_rows <= 0) return cudaSuccess;
+    switch (stage) {
+        case 1: ck_stage_kernel<1><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        case 2: ck_stage_kernel<2><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        case 3: ck_stage_kernel<3><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        case 4: ck_stage_kernel<4><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        case 5: ck_stage_kernel<5><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        case 6: ck_stage_kernel<6><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t sg_dp_control(const SgCloud* clouds, SgCtrl* ctrl, const double* err_part,
                           const double* y, int n_clouds, const int* hold_on_accept,
                           cudaStream_t st) {
@@ -408,21 +586,29 @@ cudaError_t sg_coords_from_state(const SgDpArgs& a, const double* q, int n_rows,
     return cudaGetLastError();
 }
 
-cudaError_t sg_force_finish(const SgDpArgs& a, double t, int with_field, double* out, int n_rows,
-                            cudaStream_t st) {
-    force_finish_kernel<<<n_rows, SG_ROWS, 0, st>>>(a, t, with_field, out);
+cudaError_t sg_force_finish(const SgDpArgs& a, double t, int with_field, const int* perm,
+                            double* out, int n_rows, cudaStream_t st) {
+    force_finish_kernel<<<n_rows, SG_ROWS, 0, st>>>(a, t, with_field, perm, out);
     return cudaGetLastError();
 }
 
-cudaError_t sg_aos_to_soa(const double* pos, const double* vel, double* y, int n, cudaStream_t st) {
+cudaError_t sg_aos_to_soa(const double* pos, const double* vel, const int* perm, double* y, int n,
+                          cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    aos_to_soa_kernel<<<(n + 255) / 256, 256, 0, st>>>(pos, vel, y, n);
+    aos_to_soa_kernel<<<(n + 255) / 256, 256, 0, st>>>(pos, vel, perm, y, n);
     return cudaGetLastError();
 }
 
-cudaError_t sg_soa_to_aos(const double* y, double* pos, double* vel, int n, cudaStream_t st) {
+cudaError_t sg_soa_to_aos(const double* y, const int* perm, double* pos, double* vel, int n,
+                          cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    soa_to_aos_kernel<<<(n + 255) / 256, 256, 0, st>>>(y, pos, vel, n);
+    soa_to_aos_kernel<<<(n + 255) / 256, 256, 0, st>>>(y, perm, pos, vel, n);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_gather(const double* src, const int* perm, double* dst, int n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    gather_kernel<<<(n + 255) / 256, 256, 0, st>>>(src, perm, dst, n);
     return cudaGetLastError();
 }
 

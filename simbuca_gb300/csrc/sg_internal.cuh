@@ -63,6 +63,8 @@ struct SgCloud {
     double cx, cy, cz;   // centre of the FP32 frame (m)
     double L, invL;      // scale of the FP32 frame (m)
     double vref;         // RMS velocity per axis at upload (m/s), proposer features
+    int32_t tile0;       // first entry of this cloud in the 128-ion tile bounding boxes
+    float dfar;          // FP32c: tiles farther apart than this (frame units) use hi parts only
     float wc;            // FP32c close-pair threshold on 1/r^3 (frame units)
     float pad2;
     sg_field_params fp;
@@ -72,6 +74,7 @@ struct SgCloud {
 struct SgCtrl {
     double t, h, hnext, errold, err, t_end, rtol, atol, h_last;
     int32_t reject, adaptive, max_rejects, status, done, accepted, rejects_here, hold;
+    int32_t method, pad2;  // 5 Dormand-Prince, 4 Cash-Karp
     long long steps, rejects, force_evals, coulomb_evals;
 };
 
@@ -165,6 +168,7 @@ struct SgDpArgs {
     double* c64;          // [4][Npad]
     float* c32;           // [7][Npad]
     double* err_part;     // [rows]
+    float* bbox;          // [tiles][8] frame-unit bounds of each 128-ion tile (FP32c)
     int n;                // ions (unpadded)
     int npad;             // padded ions
     int fp32c;            // write the FP32 frame coordinates
@@ -172,6 +176,7 @@ struct SgDpArgs {
 
 // ---- launchers implemented in the .cu files ------------------------------------
 cudaError_t sg_dp_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t st);
+cudaError_t sg_ck_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t st);
 cudaError_t sg_dp_control(const SgCloud* clouds, SgCtrl* ctrl, const double* err_part,
                           const double* y, int n_clouds, const int* hold_on_accept,
                           cudaStream_t st);
@@ -179,10 +184,14 @@ cudaError_t sg_clear_hold(SgCtrl* ctrl, int n_clouds, cudaStream_t st);
 int sg_probe_iters(int which);
 cudaError_t sg_dp_commit(const SgDpArgs& a, int n_rows, cudaStream_t st);
 cudaError_t sg_coords_from_state(const SgDpArgs& a, const double* q, int n_rows, cudaStream_t st);
-cudaError_t sg_force_finish(const SgDpArgs& a, double t, int with_field, double* out, int n_rows,
-                            cudaStream_t st);
-cudaError_t sg_aos_to_soa(const double* pos, const double* vel, double* y, int n, cudaStream_t st);
-cudaError_t sg_soa_to_aos(const double* y, double* pos, double* vel, int n, cudaStream_t st);
+cudaError_t sg_force_finish(const SgDpArgs& a, double t, int with_field, const int* perm,
+                            double* out, int n_rows, cudaStream_t st);
+// layout changes with the ion order perm (sorted position -> caller's index)
+cudaError_t sg_aos_to_soa(const double* pos, const double* vel, const int* perm, double* y, int n,
+                          cudaStream_t st);
+cudaError_t sg_soa_to_aos(const double* y, const int* perm, double* pos, double* vel, int n,
+                          cudaStream_t st);
+cudaError_t sg_gather(const double* src, const int* perm, double* dst, int n, cudaStream_t st);
 cudaError_t sg_moments(const SgDpArgs& a, const double* mass, double* out, int n_rows,
                        cudaStream_t st);
 cudaError_t sg_cunbody_launch(const double* xj, const double* mj, const double* xi, double eps2,
@@ -212,9 +221,12 @@ struct SgCoulombArgs {
     int npad_total;
     int* errword;
     int variant;             // FP32c launch shape (sg_coulomb_fp32c_ib)
+    const float* bbox;       // [tiles][8] tile bounds (sorted variant)
 };
 
-#define SG_C32_VARIANTS 4
+#define SG_C32_VARIANTS 5
+// variant 4: ions in k-d tree order, far tile pairs from the high parts only
+#define SG_C32_SORTED 4
 int sg_coulomb_fp32c_ib(int variant);
 cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s);
 cudaError_t sg_launch_coulomb_fp64(const SgCoulombArgs& a, cudaStream_t s);

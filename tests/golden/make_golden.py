@@ -94,7 +94,23 @@ def main():
         out[f"dp45_{tag}"] = (len(hist), int((hist[:, 3] == 0).sum()))
     np.savez_compressed(os.path.join(HERE, "dp45_adaptive.npz"), **runs)
 
-    # 5. fixed step, 40 steps of 2 ns
+    # 5. Cash-Karp (the reference's "RungaKutta4", Init_ode order 4), adaptive, with the
+    #    reference's error sum carried over from the previous attempt
+    c = cloud(150, 8)
+    p, v, ctrl, hist, nh = oracle.ref_dp45_run(
+        c.pos, c.vel, c.mass, c.charge, trap=1, tof=0, coulomb=1, coulomb_scale=1.0, trapp=TRAPP,
+        t0=0.0, t_end=4e-7, h0=1e-9, adaptive=1, rtol=1e-9, atol=1e-15, max_steps=1 << 40,
+        mode=1, hist_cap=100000, method=4)
+    p0, v0, ctrl0, _, _ = oracle.ref_dp45_run(
+        c.pos, c.vel, c.mass, c.charge, trap=1, tof=0, coulomb=1, coulomb_scale=1.0, trapp=TRAPP,
+        t0=0.0, t_end=4e-7, h0=1e-9, adaptive=1, rtol=1e-9, atol=1e-15, max_steps=1 << 40,
+        mode=0, method=4)
+    assert np.array_equal(p0, p) and np.array_equal(ctrl0, ctrl)
+    np.savez_compressed(os.path.join(HERE, "ck45_adaptive.npz"), pos0=c.pos, vel0=c.vel,
+                        mass=c.mass, charge=c.charge, pos=p, vel=v, ctrl=ctrl, hist=hist)
+    out["ck45"] = (len(hist), int((hist[:, 3] == 0).sum()))
+
+    # 6. fixed step, 40 steps of 2 ns
     c = cloud(64, 7)
     p, v, ctrl, hist, nh = oracle.ref_dp45_run(
         c.pos, c.vel, c.mass, c.charge, trap=1, tof=0, coulomb=1, coulomb_scale=1.0, trapp=TRAPP,

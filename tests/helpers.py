@@ -54,9 +54,10 @@ def run_recording(batch, max_calls=100000):
     return [np.array(x) for x in ts], [np.array(x) for x in hs], prev
 
 
-def replay_error(cloud, fp, ts, hs, pos, vel):
+def replay_error(cloud, fp, ts, hs, pos, vel, method=5):
     """Relative max difference of (pos, vel) against the oracle replaying (ts, hs)."""
-    pr, vr = oracle.dp45_replay(cloud.pos, cloud.vel, cloud.mass, cloud.charge, fp, ts, hs)
+    pr, vr = oracle.dp45_replay(cloud.pos, cloud.vel, cloud.mass, cloud.charge, fp, ts, hs,
+                                method=method)
     ep = np.abs(pos - pr).max() / np.abs(pr).max()
     ev = np.abs(vel - vr).max() / np.abs(vr).max()
     return ep, ev

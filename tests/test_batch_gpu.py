@@ -107,3 +107,28 @@ def test_moments(ctx):
         ref = oracle.moments(c.pos, c.vel, c.mass)
         np.testing.assert_allclose(m[k], ref, rtol=1e-9, atol=1e-15)
         off += len(c.mass)
+
+
+def test_sorted_order_round_trip(ctx):
+    """A batch in k-d tree order: download returns the caller's order, and the
+    integration matches the oracle replaying the accepted steps."""
+    w = configs.penning_1k(n=3000, seed=21)
+    c = w.clouds[0]
+    fp = configs.penning_field(quad=(0.5, configs.nu_c(132.905), 0.0, 0.0, 1.0), delta=1e3)
+    ctx.set_coulomb_variant(4)
+    try:
+        b = Batch(ctx, [3000], [fp], [configs.ode(1e-9, 1e-15, 1e-9, 1.0)], SG_PREC_FP32C)
+        b.upload(c.pos, c.vel, c.mass, c.charge)
+        p0, v0 = b.download()
+        assert np.array_equal(p0, c.pos) and np.array_equal(v0, c.vel)
+        ts, hs = [], []
+        for _ in range(6):
+            i0 = b.info()[0]
+            info, st = b.step()
+            ts.append(i0["t"])
+            hs.append(info[0]["h_last"])
+        p, v = b.download()
+    finally:
+        ctx.set_coulomb_variant(-1)
+    ep, ev = replay_error(c, fp, np.array(ts), np.array(hs), p, v)
+    assert ep <= 1e-9 and ev <= 1e-9, (ep, ev)

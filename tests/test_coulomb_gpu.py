@@ -101,3 +101,23 @@ def test_bad_arguments(ctx):
     L = abi.load()
     assert L.sg_coulomb_accel(ctx.handle, 7, 3, None, None, None, None) == abi.SG_BAD_ARG
     assert L.sg_coulomb_accel(ctx.handle, 0, -1, None, None, None, None) == abi.SG_BAD_ARG
+
+
+@pytest.mark.parametrize("n", [100, 1000, 5000, 20000])
+def test_sorted_variant(ctx, n):
+    """Ions in k-d tree order, far tile pairs from the high parts only: same accuracy,
+    results returned in the caller's order."""
+    rng = np.random.default_rng(100 + n)
+    pos = rng.normal(0, 6e-4, (n, 3)) + np.array([2e-4, 0.0, -1e-4])
+    q = np.ones(n)
+    q[::11] = 2.0
+    kq = kq_of(np.full(n, 132.905 * oracle.AMU), q)
+    rows = np.unique(rng.choice(n, min(n, 600), replace=False))
+    ref = np.stack([oracle.coulomb_kq_rows(pos, q, kq, int(i), int(i) + 1)[0] for i in rows])
+    ctx.set_coulomb_variant(4)
+    try:
+        a = ctx.coulomb_accel(pos, q, kq, SG_PREC_FP32C)[rows]
+    finally:
+        ctx.set_coulomb_variant(-1)
+    e = rel_err_per_ion(a, ref)
+    assert e.max() <= 1e-6, summary(e)

@@ -30,8 +30,9 @@ def _oracle():
 
 
 def one_cloud(ctx, pos, vel, mass, charge, fp, rtol, atol, h0, t_end, prec, adaptive=True,
-              max_rejects=0):
-    op = configs.ode(rtol, atol, h0, t_end, adaptive=adaptive, max_rejects=max_rejects)
+              max_rejects=0, method=5):
+    op = configs.ode(rtol, atol, h0, t_end, adaptive=adaptive, max_rejects=max_rejects,
+                     method=method)
     b = Batch(ctx, [len(mass)], [fp], [op], prec)
     b.upload(pos, vel, mass, charge)
     return b
@@ -94,6 +95,44 @@ def test_golden_adaptive_fp32c(ctx):
     assert ep <= 1e-9 and ev <= 1e-9, (ep, ev)
     # accepted/rejected counts of the FP64 reference run
     assert abs(last[0]["steps"] - int(g[f"{tag}_ctrl"][5])) <= 1
+
+
+@pytest.mark.parametrize("prec", [SG_PREC_FP64, SG_PREC_FP32C])
+def test_golden_cash_karp(ctx, prec):
+    """Cash-Karp (the reference's RungaKutta4, bin/ode.cpp:220-345) with the error sum
+    that the reference carries from one attempt to the next."""
+    g = np.load(os.path.join(GOLD, "ck45_adaptive.npz"))
+    fp = paul_fp(TRAPP)
+    b = one_cloud(ctx, g["pos0"], g["vel0"], g["mass"], g["charge"], fp, 1e-9, 1e-15, 1e-9,
+                  4e-7, prec, method=4)
+    hist, last = attempt_history(b)
+    gh = g["hist"]
+    p, v = b.download()
+    acc = hist[hist[:, 3] == 1]
+    from simbuca_gb300.configs import Cloud
+    c0 = Cloud(g["pos0"], g["vel0"], g["mass"], g["charge"])
+    ep, ev = replay_error(c0, fp, acc[:, 0], acc[:, 1], p, v, method=4)
+    if prec == SG_PREC_FP64:
+        assert hist.shape == gh.shape
+        assert np.array_equal(hist[:, 3], gh[:, 3])
+        np.testing.assert_allclose(hist[:, :2], gh[:, :2], rtol=1e-8)
+        np.testing.assert_allclose(hist[:, 2], gh[:, 2], rtol=1e-5, atol=1e-9)
+        assert ep <= 1e-12 and ev <= 1e-12, (ep, ev)
+    else:
+        assert last["status"] == 0 and last["done"] == 1
+        assert abs(len(acc) - int((gh[:, 3] == 1).sum())) <= 1
+        assert ep <= 1e-9 and ev <= 1e-9, (ep, ev)
+    # a Cash-Karp attempt takes six force evaluations
+    assert last["force_evals"] == 6 * len(hist)
+
+
+def test_method_mix_rejected(ctx):
+    fp = paul_fp(TRAPP)
+    ops = [configs.ode(1e-9, 1e-15, 1e-9, 1e-7, method=m) for m in (5, 4)]
+    with pytest.raises(abi.SimGBError):
+        Batch(ctx, [8, 8], [fp, fp], ops, SG_PREC_FP64)
+    with pytest.raises(abi.SimGBError):
+        Batch(ctx, [8], [fp], [configs.ode(1e-9, 1e-15, 1e-9, 1e-7, method=3)], SG_PREC_FP64)
 
 
 def test_golden_fixed_step(ctx):

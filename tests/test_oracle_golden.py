@@ -86,6 +86,19 @@ def test_dp45_adaptive_history(tag):
     assert c.steps == int(ctrl[5])
 
 
+def test_ck45_adaptive_history():
+    """Cash-Karp (bin/ode.cpp:220-345), including the error sum that the reference never
+    resets between attempts."""
+    g = np.load(os.path.join(GOLD, "ck45_adaptive.npz"))
+    fp = paul_fp(np.array([50.0, 5.0, 0.001, 0.04, 0.04, 50e5, 100.0]))
+    fp.flags &= ~SG_F_TOF
+    p, v, c, hist, nh = oracle.dp45_run(g["pos0"], g["vel0"], g["mass"], g["charge"], fp,
+                                        rtol=1e-9, atol=1e-15, h0=1e-9, t0=0.0, t_end=4e-7,
+                                        hist_cap=100000, method=4)
+    assert np.array_equal(hist, g["hist"])
+    assert np.array_equal(p, g["pos"]) and np.array_equal(v, g["vel"])
+
+
 def test_dp45_fixed_steps():
     g = np.load(os.path.join(GOLD, "dp45_fixed.npz"))
     fp = paul_fp(np.array([50.0, 5.0, 0.001, 0.04, 0.04, 50e5, 100.0]))
