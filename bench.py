@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="FP32c Coulomb launch shape (-1 automatic, 0..4 fixed)")
+    ap.add_argument("--method", type=int, default=5, choices=[4, 5],
+                    help="5 Dormand-Prince, 4 Cash-Karp")
     ap.add_argument("--settle", type=int, default=60,
                     help="at most this many steps to let the step size settle before warm-up")
     return ap.parse_args()
@@ -167,7 +171,11 @@ def run_ours(args, dist: Dist):
     w = configs.WORKLOADS[args.workload]()
     allc = w.concat()
     prec = abi.SG_PREC_FP32C if args.precision == "fp32c" else abi.SG_PREC_FP64
+    for o in w.odes:
+        o.method = args.method
     ctx = Context(dist.local)
+    if args.variant >= 0:
+        ctx.set_coulomb_variant(args.variant)
     peaks = ctx.probe_peaks()
     batch = Batch(ctx, w.counts, w.fields, w.odes, prec)
     batch.upload(allc.pos, allc.vel, allc.mass, allc.charge)
@@ -277,7 +285,9 @@ def run_ours(args, dist: Dist):
                    "precision": args.precision, "rtol": 1e-9, "atol": 1e-15,
                    "parallelism": f"replicas x{dist.world}",
                    "l2": "flushed (256 MB write) between timed steps",
-                   "settle_steps": settle_steps, "h_settled": snap[0]["h"]},
+                   "settle_steps": settle_steps, "h_settled": snap[0]["h"],
+                   "method": "dormand-prince" if args.method == 5 else "cash-karp",
+                   "coulomb_variant": batch.variant()},
         "e2e": {"value": e2e_val, "unit": "sim-us/wall-s", "h2d_bytes_per_step": bytes_state,
                 "d2h_bytes_per_step": bytes_state, "ms_per_step": sum(e2e_ms) / args.steps,
                 "ms_upload_step_download": (parts / args.steps).tolist(),

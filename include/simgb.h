@@ -104,7 +104,10 @@ typedef struct sg_ode_params {
     int32_t adaptive;    /* 1: step-size control on (ode.cpp:478); 0: fixed step h0     */
     int32_t max_rejects; /* reject budget per step (0 = unlimited)                      */
     int32_t method;      /* Init_ode order (ode.cpp:556-583): 5 Dormand-Prince (0 = 5),
-                            4 Cash-Karp, the reference's "RungaKutta4" (ode.cpp:220-345) */
+                            4 Cash-Karp, the reference's "RungaKutta4" (ode.cpp:220-345),
+                            1 Gear predictor-corrector (ode.cpp:347-424): fixed step h0,
+                            adaptive ignored, history restarted by upload and set_state.
+                            All clouds of a batch use one method.                      */
     int32_t pad;
 } sg_ode_params;
 
@@ -205,6 +208,8 @@ int sg_fixup_count(sg_ctx* ctx, int64_t* count);
  * 1 = 128 x 2, 2 = 256 x 2, 3 = 64 x 4, 4 = 128 x 4 with the ions kept in k-d tree
  * order and far tile pairs summed from the high parts of the coordinates. */
 int sg_set_coulomb_variant(sg_ctx* ctx, int variant);
+/* Launch shape the resident batch was planned with (0..4; 0 for FP64 batches). */
+int sg_batch_variant(sg_ctx* ctx, int* variant);
 /* Capture the attempt sequence in a CUDA graph (1) or launch it directly (0). */
 int sg_set_use_graph(sg_ctx* ctx, int on);
 /* Host-side timer on the context stream (CUDA events). */

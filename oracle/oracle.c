@@ -495,6 +495,64 @@ double orc_ck45_attempt(int n, const double* pos, const double* vel, const doubl
     return err;
 }
 
+
+/* GearMethod, bin/ode.cpp:347-424: fifth-order Gear predictor-corrector in Nordsieck
+ * form, one force evaluation per step.  g holds [4][n][3]: the acceleration of the
+ * last force call (odev.forcev.derivs), and b, c, d (odev.b/c/d).  hf = h^2/2, h^3/6,
+ * h^4/24, h^5/120 as Init_ode computes them from the initial step (bin/ode.cpp:548-552).
+ * The e terms of the reference are computed there but never read; they are left out. */
+#define GEA0 (3.0 / 20.0)
+#define GEA1 (251.0 / 360.0)
+#define GEA3 (11.0 / 18.0)
+#define GEA4 (1.0 / 6.0)
+#define GEA5 (1.0 / 60.0)
+#define GS(s, j, c) g[((size_t)(s) * n + (j)) * 3 + (c)]
+
+void orc_gear_init(int n, double* g) {
+    /* InitAcceleraction, bin/ode.cpp:36-59: constant seeds for every ion but the last,
+     * whose entry the reference leaves as allocated; it is zero here.  b = c = d = 0
+     * (std::vector value-initialised, bin/ode.cpp:599-630). */
+    memset(g, 0, sizeof(double) * 12 * (size_t)n);
+    for (int i = 0; i + 1 < n; i++) {
+        GS(0, i, 0) = 1.6e9;
+        GS(0, i, 1) = 1.1e9;
+        GS(0, i, 2) = -5e8;
+    }
+}
+
+void orc_gear_step(int n, const double* pos, const double* vel, const double* mass,
+                   const int* charge, const sg_field_params* fp, orc_ctrl* cs, const double* hf,
+                   double* pos2, double* vel2, double* g, double* derivs) {
+    const double h = cs->h;
+    const double h2f = hf[0], h3f = hf[1], h4f = hf[2], h5f = hf[3];
+    const int frozen = (fp->flags & SG_F_FROZEN_T) != 0;
+    for (int i = 0; i < n; i++)
+        for (int c = 0; c < 3; c++) {
+            pos2[3 * i + c] = pos[3 * i + c] + vel[3 * i + c] * h + GS(0, i, c) * h2f +
+                              GS(1, i, c) * h3f + GS(2, i, c) * h4f + GS(3, i, c) * h5f;
+            vel2[3 * i + c] = vel[3 * i + c] + GS(0, i, c) * h + GS(1, i, c) * h2f +
+                              GS(2, i, c) * h3f + GS(3, i, c) * h4f;
+        }
+    orc_force(n, pos2, vel2, mass, charge, frozen ? cs->t : cs->t + h, fp, derivs);
+    for (int i = 0; i < n; i++)
+        for (int c = 0; c < 3; c++) {
+            const double a = GS(0, i, c), b = GS(1, i, c), cc = GS(2, i, c), d = GS(3, i, c);
+            const double sug = a + b * h + cc * h2f + d * h3f;
+            const double bn = b + cc * h + d * h2f;
+            const double cn = cc + d * h;
+            const double ad = h2f * (derivs[3 * i + c] - sug);
+            pos2[3 * i + c] += GEA0 * ad;
+            vel2[3 * i + c] += GEA1 * ad / h;
+            GS(0, i, c) = derivs[3 * i + c];
+            GS(1, i, c) = bn + GEA3 * ad / h3f;
+            GS(2, i, c) = cn + GEA4 * ad / h4f;
+            GS(3, i, c) = d + GEA5 * ad / h5f;
+        }
+    cs->err = 0.0;
+    cs->force_evals += 1;
+}
+#undef GS
+
 /* error_succes, bin/ode.cpp:426-457 (beta = 0, alpha = 0.2, safe = 0.9,
  * minscale = 0.2, maxscale = 10). */
 int orc_error_succes(double err, orc_ctrl* c) {
@@ -542,15 +600,35 @@ int64_t orc_rk_run(int method, int n, double* pos, double* vel, const double* ma
     double* derivs = (double*)malloc(sizeof(double) * 3 * (size_t)n);
     int64_t nh = 0;
     int64_t done_steps = 0;
+    /* Gear: step powers fixed at the initial step (bin/ode.cpp:548-552).  The reference
+     * is C++98 code, where pow(double, int) is std::pow's integer overload, evaluated by
+     * repeated multiplication: h^3 = h^2 h, h^4 = h^2 h^2, h^5 = h^3 h^2. */
+    const double h1 = c->h, h2 = h1 * h1, h3 = h2 * h1;
+    const double hf[4] = {h1 * h1 / 2., h3 / 6., h2 * h2 / 24., h3 * h2 / 120.};
     c->status = SG_OK;
     if (!k || !pos2 || !vel2 || !derivs) {
         free(k); free(pos2); free(vel2); free(derivs);
         return -SG_BAD_ARG;
     }
+    if (method == 1) orc_gear_init(n, k);
     while (done_steps < max_steps && c->t < c->t_end) {
         int rejects_here = 0;
         for (;;) {
             double tstart = c->t, hs = c->h;
+            if (method == 1) {
+                /* step() turns error control off for Gear (bin/ode.cpp:473-476) */
+                orc_gear_step(n, pos, vel, mass, charge, fp, c, hf, pos2, vel2, k, derivs);
+                c->attempts++;
+                c->hnext = c->h;
+                if (hist && nh < hist_cap) {
+                    hist[4 * nh + 0] = tstart;
+                    hist[4 * nh + 1] = hs;
+                    hist[4 * nh + 2] = 0.0;
+                    hist[4 * nh + 3] = 1.0;
+                }
+                nh++;
+                break;
+            }
             double err = method == 4
                              ? orc_ck45_attempt(n, pos, vel, mass, charge, fp, c, pos2, vel2, k, derivs)
                              : orc_dp45_attempt(n, pos, vel, mass, charge, fp, c, pos2, vel2, k, derivs);

@@ -9,6 +9,8 @@
  *   - the CPU direct-sum Coulomb loop            bin/force.cpp:147-174
  *   - the trap and TOF field terms               bin/force.cpp:34-82
  *   - Dormand_Prince_5                           bin/ode.cpp:61-218
+ *   - RungaKutta4 (Cash-Karp 5(4))               bin/ode.cpp:220-345
+ *   - GearMethod (5th-order predictor-corrector) bin/ode.cpp:347-424
  *   - error_succes (step-size controller)        bin/ode.cpp:426-457
  *   - step (retry loop, underflow, commit)       bin/ode.cpp:459-494
  *   - IonCloud::Temperature                      bin/ioncloud.cpp:316-335
@@ -84,8 +86,18 @@ double orc_ck45_attempt(int n, const double* pos, const double* vel, const doubl
                         const int* charge, const sg_field_params* fp, orc_ctrl* c,
                         double* pos2, double* vel2, double* k, double* derivs);
 
+/* GearMethod (bin/ode.cpp:347-424), one fixed step from (pos, vel) into pos2/vel2.
+ * g is the Gear state [4][n][3] (acceleration, b, c, d), updated in place; hf the
+ * step powers h^2/2, h^3/6, h^4/24, h^5/120 of the initial step.  orc_gear_init seeds
+ * g as InitAcceleraction does (bin/ode.cpp:36-59). */
+void orc_gear_init(int n, double* g);
+void orc_gear_step(int n, const double* pos, const double* vel, const double* mass,
+                   const int* charge, const sg_field_params* fp, orc_ctrl* c, const double* hf,
+                   double* pos2, double* vel2, double* g, double* derivs);
+
 /* Step loop with the method of the reference's Init_ode order: 5 = Dormand-Prince,
- * 4 = Cash-Karp.  Same contract as orc_dp45_run. */
+ * 4 = Cash-Karp, 1 = Gear (fixed step, error control off).  Same contract as
+ * orc_dp45_run. */
 int64_t orc_rk_run(int method, int n, double* pos, double* vel, const double* mass,
                    const int* charge, const sg_field_params* fp, orc_ctrl* c,
                    int64_t max_steps, double* hist, int64_t hist_cap);

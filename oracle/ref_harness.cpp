@@ -23,6 +23,7 @@
 /* defined at global scope in bin/ode.cpp:61 and :426 */
 double Dormand_Prince_5(IonCloud& _cloud, _ode_vars& odev);
 double RungaKutta4(IonCloud& _cloud, _ode_vars& odev);
+void GearMethod(IonCloud& _cloud, _ode_vars& odev);
 bool error_succes(const double err, _ode_vars& odev);
 
 namespace {
@@ -57,6 +58,9 @@ void setup(RefRun& r, int n, const double* pos, const double* vel, const double*
     r.odev.rk_rtol = rtol;
     r.odev.rk_atol = atol;
     r.odev.Initpoolvectors(n);
+    // InitAcceleraction leaves the last ion's initial acceleration as allocated; zero it
+    // so that Gear runs are defined (the Runge-Kutta methods overwrite it before use)
+    memset(r.odev.forcev.derivs, 0, sizeof(double) * 3 * (size_t)n);
     r.cloud.InitializePoolVectors();
     r.cloud.CopyParticlesToVectors();
     r.odev.forcev.coulomb_interaction = coulomb != 0;
@@ -114,7 +118,7 @@ int ref_force(int n, const double* pos, const double* vel, const double* mass,
     return 0;
 }
 
-/* Runge-Kutta run, method 5 = Dormand-Prince, 4 = Cash-Karp (Init_ode's order).
+/* Integrator run, method 5 = Dormand-Prince, 4 = Cash-Karp, 1 = Gear (Init_ode's order).
  * mode 0: call the reference step() (bin/ode.cpp:459-494)
  * until lifetime >= t_end or max_steps steps; mode 1: the same loop written out
  * with the reference's Dormand_Prince_5 and error_succes so each attempt can be
@@ -141,7 +145,13 @@ long long ref_dp45_run(int n, double* pos, double* vel, const double* mass,
             } else {
                 for (;;) {
                     double ts = cl.lifetime, hs = od.h;
-                    double err = method == 4 ? RungaKutta4(cl, od) : Dormand_Prince_5(cl, od);
+                    double err = 0.0;
+                    if (method == 1) {
+                        GearMethod(cl, od);
+                        od.change_stepsize = false;  // as step() does for Gear
+                    } else {
+                        err = method == 4 ? RungaKutta4(cl, od) : Dormand_Prince_5(cl, od);
+                    }
                     bool acc = true;
                     if (od.change_stepsize) {
                         od.countstep++;

@@ -207,6 +207,13 @@ class Batch:
             check(st, "sg_batch_run")
         return [s.as_dict() for s in self._info], st
 
+    def variant(self) -> int:
+        """FP32c Coulomb launch shape this batch was planned with."""
+        self._live()
+        v = ctypes.c_int(0)
+        check(self._L.sg_batch_variant(self.ctx.handle, ctypes.byref(v)), "sg_batch_variant")
+        return v.value
+
     def info(self):
         self._live()
         check(self._L.sg_batch_info(self.ctx.handle, self._info), "sg_batch_info")

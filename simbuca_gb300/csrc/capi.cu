@@ -475,7 +475,13 @@ double active_interactions(Problem& P) {
 int enqueue_attempt(sg_ctx* ctx, Problem& P) {
     SgDpArgs a = dp_args(P);
     const double inter = ctx->timing ? active_interactions(P) : 0.0;
-    if (P.method == 4) {
+    if (P.method == 1) {
+        // Gear: predict, one force evaluation at the predicted state, correct
+        CK(sg_gear_stage(a, 0, P.n_rows, ctx->stream));
+        int st = launch_coulomb(ctx, P, true, inter, P.coulS);
+        if (st != SG_OK) return st;
+        CK(sg_gear_stage(a, 1, P.n_rows, ctx->stream));
+    } else if (P.method == 4) {
         // Cash-Karp: the step start is no stage of the previous step, so its Coulomb
         // inputs are rebuilt and all six stages take a Coulomb sum
         CK(sg_coords_from_state(a, P.qd, P.n_rows, ctx->stream));
@@ -669,6 +675,8 @@ int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel) 
                        ctx->stream));
     SgDpArgs a = dp_args(P);
     CK(sg_coords_from_state(a, P.qd, P.n_rows, ctx->stream));
+    // a new state restarts the Gear history
+    if (P.method == 1) CK(sg_gear_init(a, P.dperm, P.n_rows, ctx->stream));
     // the host vectors above are read by queued copies: finish before they go away
     CK(cudaStreamSynchronize(ctx->stream));
     return SG_OK;
@@ -863,7 +871,7 @@ int sg_batch_create(sg_ctx* ctx, int n_clouds, const int* counts, const sg_field
         if (!(op[c].rtol >= 0.0) || !(op[c].atol >= 0.0) || !(op[c].h0 > 0.0)) return SG_BAD_ARG;
         const int m = op[c].method == 0 ? 5 : op[c].method;
         const int m0 = op[0].method == 0 ? 5 : op[0].method;
-        if ((m != 5 && m != 4) || m != m0) return SG_BAD_ARG;
+        if ((m != 5 && m != 4 && m != 1) || m != m0) return SG_BAD_ARG;
         total += counts[c];
     }
     if (total > (1ll << 30)) return SG_BAD_ARG;
@@ -895,6 +903,15 @@ int sg_batch_create(sg_ctx* ctx, int n_clouds, const int* counts, const sg_field
         s.adaptive = op[c].adaptive;
         s.max_rejects = op[c].max_rejects;
         s.method = P.method;
+        {
+            // Init_ode's step powers (bin/ode.cpp:548-552); the reference is C++98, where
+            // pow(double, int) multiplies out: h^3 = h^2 h, h^4 = h^2 h^2, h^5 = h^3 h^2
+            const double h1 = op[c].h0, h2 = h1 * h1, h3 = h2 * h1;
+            s.hf[0] = h1 * h1 / 2.;
+            s.hf[1] = h3 / 6.;
+            s.hf[2] = h2 * h2 / 24.;
+            s.hf[3] = h3 * h2 / 120.;
+        }
         s.err = 0.0;
         s.status = SG_OK;
         s.done = (s.t >= s.t_end) ? 1 : 0;
@@ -1115,6 +1132,13 @@ int sg_fixup_count(sg_ctx* ctx, int64_t* count) {
 int sg_set_coulomb_variant(sg_ctx* ctx, int variant) {
     if (!ctx || variant < -1 || variant >= SG_C32_VARIANTS) return SG_BAD_ARG;
     ctx->c32_variant = variant;
+    return SG_OK;
+}
+
+int sg_batch_variant(sg_ctx* ctx, int* variant) {
+    if (!ctx || !variant) return SG_BAD_ARG;
+    if (ctx->batch.n_clouds == 0) return SG_NOT_READY;
+    *variant = ctx->batch.precision == SG_PREC_FP32C ? ctx->batch.variant : 0;
     return SG_OK;
 }
 

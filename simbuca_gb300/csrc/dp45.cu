@@ -303,6 +303,108 @@ __global__ void __launch_bounds__(SG_ROWS) ck_stage_kernel(DpArgs a) {
     }
 }
 
+
+// ---- Gear predictor-corrector, the reference's GearMethod (bin/ode.cpp:347-424) ----
+// Fifth-order Nordsieck form with one force evaluation per step and a fixed step.
+// Gear state in k, by column: acceleration of the last force call [0..2], b [3..5],
+// c [6..8], d [9..11].  The e terms of the reference are never read there; left out.
+#define SG_GEA0 (3.0 / 20.0)
+#define SG_GEA1 (251.0 / 360.0)
+#define SG_GEA3 (11.0 / 18.0)
+#define SG_GEA4 (1.0 / 6.0)
+#define SG_GEA5 (1.0 / 60.0)
+
+// InitAcceleraction (bin/ode.cpp:36-59): constant seeds for every ion of a cloud but the
+// last in the caller's order (left as allocated there, zero here); b = c = d = 0.
+__global__ void __launch_bounds__(SG_ROWS) gear_init_kernel(DpArgs a, const int* __restrict__ perm) {
+    const SgRowBlock rb = a.rows[blockIdx.x];
+    const SgCloud& cl = a.clouds[rb.cloud];
+    const int li = threadIdx.x;
+    if (li >= rb.n) return;
+    const int i = rb.i0 + li;
+    const size_t N = (size_t)a.n;
+    const int caller = perm ? perm[i] : i;
+    const bool last = caller == cl.off + cl.n - 1;
+    a.k[i] = last ? 0.0 : 1.6e9;
+    a.k[N + i] = last ? 0.0 : 1.1e9;
+    a.k[2 * N + i] = last ? 0.0 : -5e8;
+#pragma unroll
+    for (int c = 3; c < 12; c++) a.k[c * N + i] = 0.0;
+}
+
+template <int PHASE>
+__global__ void __launch_bounds__(SG_ROWS) gear_kernel(DpArgs a) {
+    const SgRowBlock rb = a.rows[blockIdx.x];
+    const SgCtrl& cs = a.ctrl[rb.cloud];
+    if (cs.done || cs.hold || cs.status != SG_OK) return;
+    const SgCloud& cl = a.clouds[rb.cloud];
+    const int li = threadIdx.x;
+    const bool active = li < rb.n;
+    const int i = rb.i0 + (active ? li : 0);
+    const int ig = cl.poff + (i - cl.off);
+    const size_t N = (size_t)a.n;
+    const double h = cs.h;
+    const double h2f = cs.hf[0], h3f = cs.hf[1], h4f = cs.hf[2], h5f = cs.hf[3];
+    float hu[3] = {0.f, 0.f, 0.f};
+    int bad = 0;
+    if (active) {
+        if (PHASE == 0) {
+            // predictor: Taylor series of the Nordsieck vector (bin/ode.cpp:367-375)
+            double p2[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const double ac = a.k[c * N + i], b = a.k[(3 + c) * N + i];
+                const double cc = a.k[(6 + c) * N + i], d = a.k[(9 + c) * N + i];
+                const double x = a.y[c * N + i], v = a.y[(3 + c) * N + i];
+                p2[c] = x + v * h + ac * h2f + b * h3f + cc * h4f + d * h5f;
+                a.ys[c * N + i] = p2[c];
+                a.ys[(3 + c) * N + i] = v + ac * h + b * h2f + cc * h3f + d * h4f;
+            }
+            write_coords(a, cl, ig, p2[0], p2[1], p2[2], hu);
+        } else {
+            // corrector (bin/ode.cpp:396-420) with the force at the predicted state
+            const bool frozen = (cl.fp.flags & SG_F_FROZEN_T) != 0;
+            const double ts = frozen ? cs.t : cs.t + h;
+            double st[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) st[c] = a.ys[c * N + i];
+            double f[3];
+            sg_field_accel(cl.fp, ts, a.qm[i], st[0], st[1], st[2], st[3], st[4], st[5], f[0],
+                           f[1], f[2]);
+            if (cl.fp.flags & SG_F_COULOMB) {
+                const double kqi = a.kq[i];
+#pragma unroll
+                for (int c = 0; c < 3; c++) f[c] += kqi * a.coulS[c * N + i];
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const double ac = a.k[c * N + i], b = a.k[(3 + c) * N + i];
+                const double cc = a.k[(6 + c) * N + i], d = a.k[(9 + c) * N + i];
+                const double sug = ac + b * h + cc * h2f + d * h3f;
+                const double bn = b + cc * h + d * h2f;
+                const double cn = cc + d * h;
+                const double ad = h2f * (f[c] - sug);
+                const double x = st[c] + SG_GEA0 * ad;
+                const double v = st[3 + c] + SG_GEA1 * ad / h;
+                a.ys[c * N + i] = x;
+                a.ys[(3 + c) * N + i] = v;
+                a.k[c * N + i] = f[c];
+                a.k[(3 + c) * N + i] = bn + SG_GEA3 * ad / h3f;
+                a.k[(6 + c) * N + i] = cn + SG_GEA4 * ad / h4f;
+                a.k[(9 + c) * N + i] = d + SG_GEA5 * ad / h5f;
+                bad |= !isfinite(x) || !isfinite(v);
+            }
+        }
+    }
+    if (PHASE == 0) {
+        if (a.fp32c && a.bbox) tile_bounds(a, cl, rb, active, hu[0], hu[1], hu[2]);
+    } else {
+        // no error estimate: the partial is 0, or NaN when the step left finite numbers
+        bad = __syncthreads_or(bad);
+        if (threadIdx.x == 0) a.err_part[blockIdx.x] = bad ? __longlong_as_double(0x7ff8000000000000LL) : 0.0;
+    }
+}
+
 // error_succes + step bookkeeping (bin/ode.cpp:426-494), one thread per cloud.
 // With *hold_on_accept set, a cloud that accepts holds (skips further attempts) until
 // the host clears the hold: used to take exactly one step per cloud.
@@ -323,14 +425,14 @@ __global__ void dp_control_kernel(const SgCloud* __restrict__ clouds, SgCtrl* __
     for (int b = 0; b < cl.nrb; b++) s += err_part[cl.rb0 + b];
     const double err = sqrt(s / (6 * cl.n));
     cs.err = err;
-    cs.force_evals += (cs.method == 4) ? 6 : 7;
-    cs.coulomb_evals += (cl.fp.flags & SG_F_COULOMB) ? 6 : 0;
+    cs.force_evals += (cs.method == 4) ? 6 : (cs.method == 1 ? 1 : 7);
+    cs.coulomb_evals += (cl.fp.flags & SG_F_COULOMB) ? (cs.method == 1 ? 1 : 6) : 0;
     int accepted = 1;
     if (!isfinite(err)) {
         cs.status = SG_NONFINITE;
         cs.done = 1;
         accepted = 0;
-    } else if (cs.adaptive) {
+    } else if (cs.adaptive && cs.method != 1) {  // step() turns control off for Gear
         const double alpha = 0.2, safe = 0.9, minscale = 0.2, maxscale = 10.0;
         if (err <= 1.0) {
             double scale;
@@ -560,6 +662,21 @@ cudaError_t sg_ck_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t s
         case 6: ck_stage_kernel<6><<<n_rows, SG_ROWS, 0, st>>>(a); break;
         default: return cudaErrorInvalidValue;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t sg_gear_stage(const SgDpArgs& a, int phase, int n_rows, cudaStream_t st) {
+    if (n_rows <= 0) return cudaSuccess;
+    if (phase == 0)
+        gear_kernel<0><<<n_rows, SG_ROWS, 0, st>>>(a);
+    else
+        gear_kernel<1><<<n_rows, SG_ROWS, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_gear_init(const SgDpArgs& a, const int* perm, int n_rows, cudaStream_t st) {
+    if (n_rows <= 0) return cudaSuccess;
+    gear_init_kernel<<<n_rows, SG_ROWS, 0, st>>>(a, perm);
     return cudaGetLastError();
 }
 

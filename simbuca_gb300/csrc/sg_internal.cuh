@@ -74,7 +74,8 @@ struct SgCloud {
 struct SgCtrl {
     double t, h, hnext, errold, err, t_end, rtol, atol, h_last;
     int32_t reject, adaptive, max_rejects, status, done, accepted, rejects_here, hold;
-    int32_t method, pad2;  // 5 Dormand-Prince, 4 Cash-Karp
+    int32_t method, pad2;  // 5 Dormand-Prince, 4 Cash-Karp, 1 Gear
+    double hf[4];          // Gear: h^2/2, h^3/6, h^4/24, h^5/120 of the initial step
     long long steps, rejects, force_evals, coulomb_evals;
 };
 
@@ -177,6 +178,9 @@ struct SgDpArgs {
 // ---- launchers implemented in the .cu files ------------------------------------
 cudaError_t sg_dp_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t st);
 cudaError_t sg_ck_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t st);
+// Gear: phase 0 predicts, phase 1 corrects; sg_gear_init seeds the Gear state in k
+cudaError_t sg_gear_stage(const SgDpArgs& a, int phase, int n_rows, cudaStream_t st);
+cudaError_t sg_gear_init(const SgDpArgs& a, const int* perm, int n_rows, cudaStream_t st);
 cudaError_t sg_dp_control(const SgCloud* clouds, SgCtrl* ctrl, const double* err_part,
                           const double* y, int n_clouds, const int* hold_on_accept,
                           cudaStream_t st);

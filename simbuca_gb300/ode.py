@@ -112,7 +112,7 @@ class IonCloud:
 
 
 class OdeVars:
-    """_ode_vars, bin/ode.h:58-133: Dormand-Prince settings and controller state."""
+    """_ode_vars, bin/ode.h:58-133: integrator settings and controller state."""
 
     def __init__(self, precision=abi.SG_PREC_FP64, device: int = 0):
         self.h = 1e-9            # httry default (bin/ode.cpp:509)
@@ -124,6 +124,7 @@ class OdeVars:
         self.EPS = float(np.finfo(np.float64).eps)
         self.change_stepsize = True
         self.DP5 = True
+        self.method = 5          # Init_ode order
         self.forcev = ForceVars()
         self.precision = precision
         self.device = device
@@ -133,9 +134,9 @@ class OdeVars:
         self._batch_key = None
 
     def Init_ode(self, ode_order: int, timestep: float, adaptive_stepsize: bool):
-        """bin/ode.cpp:539-587; only order 5 (Dormand-Prince) is on this path."""
-        if ode_order != 5:
-            raise ValueError("only the Dormand-Prince method (order 5) runs on libsimgb")
+        """bin/ode.cpp:539-587: order 5 Dormand-Prince, 4 Cash-Karp (the reference's
+        RungaKutta4), 1 Gear; the reference falls back to order 4 for any other."""
+        self.method = ode_order if ode_order in (1, 4, 5) else 4
         self.errold = 1.0e-4
         self.reject = False
         self.h = self.hnext = float(timestep)
@@ -162,12 +163,13 @@ def step(cloud: IonCloud, odev: OdeVars) -> None:
     """step(), bin/ode.cpp:459-494: one accepted step of the whole cloud on the device."""
     fp = odev.forcev.field_params()
     key = (cloud.nrparticles, odev.precision, bytes(fp), odev.rk_rtol, odev.rk_atol,
-           odev.change_stepsize)
+           odev.change_stepsize, odev.method)
     if odev._batch is None or odev._batch_key != key:
         op = OdeParams()
         op.rtol, op.atol, op.h0 = odev.rk_rtol, odev.rk_atol, odev.h
         op.t0, op.t_end = cloud.lifetime, float("inf")
         op.adaptive, op.max_rejects = int(odev.change_stepsize), 0
+        op.method = odev.method
         odev._batch = Batch(odev.context(), [cloud.nrparticles], [fp], [op], odev.precision)
         odev._batch.upload(cloud.pos, cloud.vel, cloud.mass, cloud.charge)
         odev._batch_key = key

@@ -110,7 +110,17 @@ def main():
                         mass=c.mass, charge=c.charge, pos=p, vel=v, ctrl=ctrl, hist=hist)
     out["ck45"] = (len(hist), int((hist[:, 3] == 0).sum()))
 
-    # 6. fixed step, 40 steps of 2 ns
+    # 6. Gear predictor-corrector (Init_ode order 1): fixed 2 ns steps through step()
+    c = cloud(150, 9)
+    p, v, ctrl, hist, nh = oracle.ref_dp45_run(
+        c.pos, c.vel, c.mass, c.charge, trap=1, tof=0, coulomb=1, coulomb_scale=1.0, trapp=TRAPP,
+        t0=0.0, t_end=1.0, h0=2e-9, adaptive=0, rtol=1e-9, atol=1e-15, max_steps=300, mode=0,
+        method=1)
+    np.savez_compressed(os.path.join(HERE, "gear_fixed.npz"), pos0=c.pos, vel0=c.vel,
+                        mass=c.mass, charge=c.charge, pos=p, vel=v, ctrl=ctrl)
+    out["gear"] = int(ctrl[5])
+
+    # 7. fixed step, 40 steps of 2 ns
     c = cloud(64, 7)
     p, v, ctrl, hist, nh = oracle.ref_dp45_run(
         c.pos, c.vel, c.mass, c.charge, trap=1, tof=0, coulomb=1, coulomb_scale=1.0, trapp=TRAPP,

@@ -126,6 +126,47 @@ def test_golden_cash_karp(ctx, prec):
     assert last["force_evals"] == 6 * len(hist)
 
 
+@pytest.mark.parametrize("prec", [SG_PREC_FP64, SG_PREC_FP32C])
+def test_golden_gear(ctx, prec):
+    """Gear predictor-corrector (bin/ode.cpp:347-424): 300 fixed steps of 2 ns against the
+    reference's own step() run, one force evaluation per step."""
+    g = np.load(os.path.join(GOLD, "gear_fixed.npz"))
+    b = one_cloud(ctx, g["pos0"], g["vel0"], g["mass"], g["charge"], paul_fp(TRAPP), 1e-9,
+                  1e-15, 2e-9, 1.0, prec, method=1)
+    info, _ = b.run(max_attempts=300)
+    s = info[0]
+    assert s["steps"] == 300 and s["rejects"] == 0 and s["status"] == 0
+    assert s["force_evals"] == 300 and s["h"] == 2e-9
+    p, v = b.download()
+    ep = np.abs(p - g["pos"]).max() / np.abs(g["pos"]).max()
+    ev = np.abs(v - g["vel"]).max() / np.abs(g["vel"]).max()
+    print(prec, ep, ev)
+    tol = 1e-11 if prec == SG_PREC_FP64 else 1e-7
+    assert ep <= tol and ev <= tol, (ep, ev)
+
+
+@pytest.mark.parametrize("prec", [SG_PREC_FP64, SG_PREC_FP32C])
+def test_gear_penning_vs_oracle(ctx, prec):
+    """Gear with the Penning trap, a quadrupole drive and friction: velocity-dependent
+    forces at the predicted state and stage time t + h."""
+    w = configs.penning_1k(n=300, seed=7)
+    c = w.clouds[0]
+    fp = configs.penning_field(quad=(0.5, configs.nu_c(configs.M_CS), 0.0, 0.0, 1.0), delta=1e3)
+    b = one_cloud(ctx, c.pos, c.vel, c.mass, c.charge, fp, 1e-9, 1e-15, 1e-9, 1.0, prec,
+                  method=1)
+    b.run(max_attempts=200)
+    p, v = b.download()
+    pr, vr, cr, _, _ = oracle.dp45_run(c.pos, c.vel, c.mass, c.charge, fp, rtol=1e-9,
+                                       atol=1e-15, h0=1e-9, t0=0.0, t_end=1.0, adaptive=False,
+                                       max_steps=200, method=1)
+    ep = np.abs(p - pr).max() / np.abs(pr).max()
+    ev = np.abs(v - vr).max() / np.abs(vr).max()
+    print(prec, ep, ev)
+    tol = 1e-11 if prec == SG_PREC_FP64 else 1e-7
+    assert ep <= tol and ev <= tol, (ep, ev)
+    assert b.info()[0]["t"] == pytest.approx(cr.t, rel=1e-14)
+
+
 def test_method_mix_rejected(ctx):
     fp = paul_fp(TRAPP)
     ops = [configs.ode(1e-9, 1e-15, 1e-9, 1e-7, method=m) for m in (5, 4)]

@@ -99,6 +99,19 @@ def test_ck45_adaptive_history():
     assert np.array_equal(p, g["pos"]) and np.array_equal(v, g["vel"])
 
 
+def test_gear_fixed_steps():
+    """GearMethod (bin/ode.cpp:347-424) through step(): 300 fixed steps, bit for bit."""
+    g = np.load(os.path.join(GOLD, "gear_fixed.npz"))
+    fp = paul_fp(np.array([50.0, 5.0, 0.001, 0.04, 0.04, 50e5, 100.0]))
+    fp.flags &= ~SG_F_TOF
+    p, v, c, hist, nh = oracle.dp45_run(g["pos0"], g["vel0"], g["mass"], g["charge"], fp,
+                                        rtol=1e-9, atol=1e-15, h0=2e-9, t0=0.0, t_end=1.0,
+                                        adaptive=False, max_steps=300, hist_cap=400, method=1)
+    assert nh == 300 and c.steps == int(g["ctrl"][5])
+    assert np.array_equal(p, g["pos"]) and np.array_equal(v, g["vel"])
+    assert c.t == g["ctrl"][0]
+
+
 def test_dp45_fixed_steps():
     g = np.load(os.path.join(GOLD, "dp45_fixed.npz"))
     fp = paul_fp(np.array([50.0, 5.0, 0.001, 0.04, 0.04, 50e5, 100.0]))
