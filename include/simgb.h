@@ -252,6 +252,18 @@ int sg_batch_read_log(sg_ctx* ctx, int cloud, float* feat, double* num, int cap,
 int sg_probe_peaks(sg_ctx* ctx, double* fp32_gflops, double* fp32x2_gflops,
                    double* fp64_gflops);
 
+/* ---- initial cloud ------------------------------------------------------------
+ * InitCloud (bin/initialization.cpp:117-206), host side: n ions uniform in the
+ * ellipsoid offset + semiaxis * (unit ball), drawn by rejection from the unit cube;
+ * speed v = sqrt(-2 E e / m ln(1 - sqrt(u))) around the energy E (eV) of the
+ * Maxwell-Boltzmann maximum, direction uniform on the sphere (theta = 2 pi u,
+ * phi = acos(2u - 1)).  With n_ev = 2, ev_max[1] sets the speed of the axial component.
+ * Random stream: MT19937 seeded with `seed`, doubles = 32-bit output * 2^-32, in the
+ * reference's draw order, so the same seed gives the reference's cloud.  mass in kg;
+ * pos (m) and vel (m/s) are written AoS [n][3]. */
+int sg_init_cloud(int n, const double* ev_max, int n_ev, uint32_t seed, const double* semiaxis,
+                  const double* offset, const double* mass, double* pos, double* vel);
+
 /* ---- drop-in slot of the reference's CUNBODY backend ------------------------
  * Same symbols and argument meaning as the closed library (bin/cunbody.h:11-33):
  *   ai[i] = sum_j mj[j] (xj[j]-xi[i]) / (|xj[j]-xi[i]|^2 + eps2)^{3/2}

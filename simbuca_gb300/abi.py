@@ -83,7 +83,7 @@ EXPORTED = [
     "sg_batch_set_state", "sg_batch_download", "sg_batch_attempts", "sg_dp45_step",
     "sg_batch_run", "sg_batch_info", "sg_batch_set_field", "sg_batch_set_t_end",
     "sg_set_kernel_timing", "sg_kernel_timing", "sg_fixup_count", "sg_set_coulomb_variant",
-    "sg_batch_variant",
+    "sg_batch_variant", "sg_init_cloud",
     "sg_set_use_graph",
     "sg_timer_start",
     "sg_timer_stop", "sg_batch_moments", "sg_probe_peaks",
@@ -130,6 +130,8 @@ def _declare(L):
     L.sg_fixup_count.argtypes = [_vp, ctypes.POINTER(ctypes.c_int64)]
     L.sg_set_coulomb_variant.argtypes = [_vp, ctypes.c_int]
     L.sg_batch_variant.argtypes = [_vp, ctypes.POINTER(ctypes.c_int)]
+    L.sg_init_cloud.argtypes = [ctypes.c_int, _dp, ctypes.c_int, ctypes.c_uint32, _dp, _dp, _dp,
+                                _dp, _dp]
     L.sg_timer_start.argtypes = [_vp]
     L.sg_timer_stop.argtypes = [_vp, _dp]
     L.sg_batch_moments.argtypes = [_vp, _dp]

@@ -264,3 +264,20 @@ class Batch:
         self._live()
         check(self._L.sg_batch_set_t_end(self.ctx.handle, int(cloud), float(t_end)),
               "sg_batch_set_t_end")
+
+
+def init_cloud(n: int, ev_max, seed: int, semiaxis, offset, mass):
+    """InitCloud (bin/initialization.cpp:117-206) through sg_init_cloud: n ions in the
+    ellipsoid offset + semiaxis * (unit ball), Maxwell-Boltzmann speeds around ev_max
+    (eV; one value, or radial and axial), MT19937 stream seeded with `seed`.  mass in kg
+    (scalar or per ion).  Returns (pos [n,3] m, vel [n,3] m/s)."""
+    L = abi.load()
+    ev = np.ascontiguousarray(np.atleast_1d(np.asarray(ev_max, np.float64)))
+    semi = np.ascontiguousarray(semiaxis, np.float64)
+    off = np.ascontiguousarray(offset, np.float64)
+    m = np.ascontiguousarray(np.broadcast_to(np.asarray(mass, np.float64), (n,)))
+    pos = np.empty((n, 3))
+    vel = np.empty((n, 3))
+    check(L.sg_init_cloud(int(n), dptr(ev), len(ev), int(seed) & 0xFFFFFFFF, dptr(semi),
+                          dptr(off), dptr(m), dptr(pos), dptr(vel)), "sg_init_cloud")
+    return pos, vel

@@ -9,7 +9,9 @@ synthetic clouds (numpy Philox), stored next to the outputs.
 """
 from __future__ import annotations
 
+import ctypes
 import os
+import subprocess
 import sys
 
 import numpy as np
@@ -22,6 +24,7 @@ import oracle  # noqa: E402
 from simbuca_gb300 import configs  # noqa: E402
 
 AMU = oracle.AMU
+REF_BIN = "/root/reference/bin"  # the reference checkout (read only)
 # Paul trap of the reference (_trap_param defaults, bin/trapparameters.cpp:2-10) with a
 # TOF kick: Vrf, Vdc, kappa, r0, z0, freq_rf, E_kick
 TRAPP = np.array([50.0, 5.0, 0.001, 0.04, 0.04, 50e5, 100.0])
@@ -35,6 +38,21 @@ def cloud(n, seed, sigma=0.5e-3, temp=300.0, mixed=False):
         c.charge = np.where(np.arange(n) % 3 == 0, 2, 1).astype(np.int32)
         c.mass = np.where(np.arange(n) % 2 == 0, 132.905, 86.909) * AMU
     return c
+
+
+def init_library():
+    """The reference's InitCloud harness (oracle/Makefile `make ref-init`).  Its
+    initialization.cpp reads ../libraries/ mass tables when loaded, so it is loaded
+    from the reference's bin/ directory."""
+    odir = os.path.join(ROOT, "oracle")
+    subprocess.run(["make", "-C", odir, "-s", "ref-init"], check=True)
+    cwd = os.getcwd()
+    os.chdir(REF_BIN)
+    try:
+        lib = ctypes.CDLL(os.path.join(odir, "_ref", "libsimbuca_ref_init.so"))
+    finally:
+        os.chdir(cwd)
+    return lib
 
 
 def main():
@@ -120,7 +138,29 @@ def main():
                         mass=c.mass, charge=c.charge, pos=p, vel=v, ctrl=ctrl)
     out["gear"] = int(ctrl[5])
 
-    # 7. fixed step, 40 steps of 2 ns
+    # 7. InitCloud (bin/initialization.cpp:117-206): the reference's generator itself,
+    #    one and two Maxwell-Boltzmann energies, mixed masses
+    init = {}
+    lib = init_library()
+    for tag, n, ev, seed, semi, off in (("a", 1000, [0.5], 7, [1e-3, 1e-3, 2e-3], [0, 0, 1e-4]),
+                                        ("b", 2500, [0.2, 0.05], 12345, [2e-3, 2e-3, 4e-3],
+                                         [1e-4, -2e-4, 0.0])):
+        mass = np.where(np.arange(n) % 2 == 0, 132.905, 86.909) * AMU
+        ev, semi, off = (np.array(x, np.float64) for x in (ev, semi, off))
+        pos, vel = np.zeros((n, 3)), np.zeros((n, 3))
+        ch = np.ones(n, np.int32)
+        dp = ctypes.POINTER(ctypes.c_double)
+        got = lib.ref_init_cloud(n, ev.ctypes.data_as(dp), len(ev), seed, semi.ctypes.data_as(dp),
+                                 off.ctypes.data_as(dp), mass.ctypes.data_as(dp),
+                                 ch.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                 pos.ctypes.data_as(dp), vel.ctypes.data_as(dp))
+        assert got == n
+        init.update({f"{tag}_n": n, f"{tag}_ev": ev, f"{tag}_seed": seed, f"{tag}_semi": semi,
+                     f"{tag}_off": off, f"{tag}_mass": mass, f"{tag}_pos": pos, f"{tag}_vel": vel})
+    np.savez_compressed(os.path.join(HERE, "init_cloud.npz"), **init)
+    out["init_cloud"] = 2
+
+    # 8. fixed step, 40 steps of 2 ns
     c = cloud(64, 7)
     p, v, ctrl, hist, nh = oracle.ref_dp45_run(
         c.pos, c.vel, c.mass, c.charge, trap=1, tof=0, coulomb=1, coulomb_scale=1.0, trapp=TRAPP,
