@@ -252,6 +252,42 @@ int sg_batch_read_log(sg_ctx* ctx, int cloud, float* feat, double* num, int cap,
 int sg_probe_peaks(sg_ctx* ctx, double* fp32_gflops, double* fp32x2_gflops,
                    double* fp64_gflops);
 
+/* ---- recorder: device-side observables ---------------------------------------
+ * The reference prints after a step once (t - t_start) > print_interval * prints so
+ * far (move_particles, bin/ion_fly.cpp:103-108): the state of every ion
+ * (PrintParticles) and per species the centroid, spread and energy (PrintCloud,
+ * bin/ioncloud.cpp:148-183).  The recorder applies the same rule on the device,
+ * inside the attempt sequence (no host round trip): a record is
+ *   [0] t (s),
+ *   [1 + 9 s .. 9 s + 9] for species s: x0 y0 z0 x1 y1 z1 (m), energy (eV), ions of s,
+ *                        ions of the cloud -- with the reference's arithmetic: centroid
+ *                        and spread divide by the cloud's ion count, the energy sums
+ *                        m (vx^2 + vy^2 + vz vy) / 2,
+ *   then x y z vx vy vz of every stride-th ion of the cloud (caller's order).
+ * Each cloud has a device ring of `capacity` records; the host drains the rings into
+ * host memory whenever a call synchronises (sg_batch_run, sg_dp45_step, sg_batch_info,
+ * ...), and a cloud whose ring is full waits until then.  The print clock starts at
+ * the time of this call (at t0 before an upload) and restarts on upload.
+ * print_interval 0 records only on sg_batch_record_now; capacity 0 turns it off.
+ * species: per ion (caller order) in [0, n_species), NULL = all 0; n_species <= 8. */
+int sg_batch_set_recorder(sg_ctx* ctx, double print_interval, int stride, int capacity,
+                          const int* species, int n_species);
+/* A record of every active cloud now (the reference's print after an operation). */
+int sg_batch_record_now(sg_ctx* ctx);
+/* Drained records held for `cloud`, doubles per record, ions kept per record. */
+int sg_batch_records(sg_ctx* ctx, int cloud, int64_t* n_records, int* record_len,
+                     int* n_kept);
+/* Moves up to max_records drained records of `cloud` (oldest first) into out
+ * [n][record_len]. */
+int sg_batch_read_records(sg_ctx* ctx, int cloud, int64_t max_records, double* out,
+                          int64_t* n_read);
+/* The reference's text output of the drained records of `cloud`, appended to
+ * <prefix>_pAll.txt (ID name t(ms) x y z (mm) vx vy vz (m/s) E(eV) per kept ion) and
+ * <prefix>_cloud<s>.txt (s name N t(ms) x0 y0 z0 x1 y1 z1 (mm) E(eV)), with the
+ * reference's header for new files; names[s] names species s.  Consumes the records. */
+int sg_batch_write_text(sg_ctx* ctx, int cloud, const char* prefix, const char* const* names,
+                        int n_names);
+
 /* ---- initial cloud ------------------------------------------------------------
  * InitCloud (bin/initialization.cpp:117-206), host side: n ions uniform in the
  * ellipsoid offset + semiaxis * (unit ball), drawn by rejection from the unit cube;

@@ -87,6 +87,7 @@ def lib():
         L.orc_dp45_replay.argtypes = [ctypes.c_int, _dp, _dp, _dp, _ip, ctypes.c_void_p, _dp,
                                       _dp, ctypes.c_int]
         L.orc_rk_replay.argtypes = [ctypes.c_int] + L.orc_dp45_replay.argtypes
+        L.orc_cloud_stats.argtypes = [ctypes.c_int, _dp, _dp, _dp, _ip, ctypes.c_int, _dp]
         _orc = L
     return _orc
 
@@ -203,6 +204,10 @@ def ref_lib():
                                    ctypes.c_longlong, ctypes.c_int, _dp, ctypes.c_longlong,
                                    _dp, ctypes.c_int]
         L.ref_dp45_run.restype = ctypes.c_longlong
+        L.ref_print.argtypes = [ctypes.c_int, _dp, _dp, _dp, _ip, _ip,
+                                ctypes.POINTER(ctypes.c_char_p), ctypes.c_int, ctypes.c_double,
+                                ctypes.c_char_p, ctypes.c_longlong]
+        L.ref_print.restype = ctypes.c_longlong
         _ref = L
     return _ref
 
@@ -235,3 +240,39 @@ def ref_dp45_run(pos, vel, mass, charge, *, trap, tof, coulomb, coulomb_scale, t
                                 float(atol), int(max_steps), int(mode), _d(hist), int(hist_cap),
                                 _d(ctrl), int(method))
     return pos, vel, ctrl, hist[:min(max(nh, 0), hist_cap)], nh
+
+
+def cloud_stats(pos, vel, mass, species, n_species):
+    """PrintCloud statistics per species: [n_species, 9] (x0 y0 z0 x1 y1 z1 m, energy eV,
+    ions of the species, ions of the cloud)."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    vel = np.ascontiguousarray(vel, np.float64)
+    mass = np.ascontiguousarray(mass, np.float64)
+    species = np.ascontiguousarray(species, np.int32)
+    out = np.zeros((n_species, 9))
+    lib().orc_cloud_stats(len(mass), _d(pos), _d(vel), _d(mass), _i(species), int(n_species),
+                          _d(out))
+    return out
+
+
+def ref_print(pos, vel, mass, charge, species, names, t):
+    """The reference's PrintParticles + PrintCloud text for a state: {file suffix: text}."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    vel = np.ascontiguousarray(vel, np.float64)
+    mass = np.ascontiguousarray(mass, np.float64)
+    charge = np.ascontiguousarray(charge, np.int32)
+    species = np.ascontiguousarray(species, np.int32)
+    arr = (ctypes.c_char_p * len(names))(*[x.encode() for x in names])
+    cap = 200 * len(mass) + 4096
+    buf = ctypes.create_string_buffer(cap)
+    ln = ref_lib().ref_print(len(mass), _d(pos), _d(vel), _d(mass), _i(charge), _i(species), arr,
+                             len(names), float(t), buf, cap)
+    text = buf.raw[:ln].decode()
+    out, cur = {}, None
+    for line in text.splitlines(keepends=True):
+        if line.startswith("@@"):
+            cur = line[2:].strip()
+            out[cur] = ""
+        elif cur is not None:
+            out[cur] += line
+    return out

@@ -737,3 +737,46 @@ void orc_moments(int n, const double* pos, const double* vel, const double* mass
     out[10] = ez * (2.0 / (3.0 * ORC_KB));
     out[11] = n;
 }
+
+/* PrintCloud statistics (bin/ioncloud.cpp:148-183) per species s (ions with
+ * species[i] == s): out[9 s + 0..8] = centroid x0, y0, z0 (m), spread x1, y1, z1 (m),
+ * energy (eV), ions of the species, ions of the cloud.  The reference's arithmetic is
+ * kept as it is: the centroid and the spread divide by the number of ions of the whole
+ * cloud, and the energy sums m (vx^2 + vy^2 + vz vy) / 2. */
+void orc_cloud_stats(int n, const double* pos, const double* vel, const double* mass,
+                     const int* species, int n_species, double* out) {
+    const double j_to_ev = 6.24150e18; /* bin/globals.h:9 */
+    for (int s = 0; s < n_species; s++) {
+        double x0 = 0, y0 = 0, z0 = 0, x1 = 0, y1 = 0, z1 = 0, energy = 0.0;
+        int count = 0;
+        for (int i = 0; i < n; i++)
+            if (species[i] == s) {
+                x0 += pos[3 * i];
+                y0 += pos[3 * i + 1];
+                z0 += pos[3 * i + 2];
+                energy += 0.5 * j_to_ev * mass[i] *
+                          (vel[3 * i] * vel[3 * i] + vel[3 * i + 1] * vel[3 * i + 1] +
+                           vel[3 * i + 2] * vel[3 * i + 1]);
+                count++;
+            }
+        x0 /= n;
+        y0 /= n;
+        z0 /= n;
+        for (int i = 0; i < n; i++)
+            if (species[i] == s) {
+                x1 += (pos[3 * i] - x0) * (pos[3 * i] - x0);
+                y1 += (pos[3 * i + 1] - y0) * (pos[3 * i + 1] - y0);
+                z1 += (pos[3 * i + 2] - z0) * (pos[3 * i + 2] - z0);
+            }
+        double* o = out + 9 * s;
+        o[0] = x0;
+        o[1] = y0;
+        o[2] = z0;
+        o[3] = sqrt(x1 / n);
+        o[4] = sqrt(y1 / n);
+        o[5] = sqrt(z1 / n);
+        o[6] = energy;
+        o[7] = count;
+        o[8] = n;
+    }
+}

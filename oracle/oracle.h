@@ -123,6 +123,12 @@ int orc_rk_replay(int method, int n, double* pos, double* vel, const double* mas
                   const int* charge, const sg_field_params* fp, const double* ts,
                   const double* hs, int nsteps);
 
+/* PrintCloud statistics (bin/ioncloud.cpp:148-183) per species: out[n_species][9] =
+ * x0, y0, z0, x1, y1, z1 (m), energy (eV), ions of the species, ions of the cloud,
+ * with the reference's arithmetic (divisions by the cloud's ion count, vz vy term). */
+void orc_cloud_stats(int n, const double* pos, const double* vel, const double* mass,
+                     const int* species, int n_species, double* out);
+
 /* Moments of one cloud: out[12] as sg_batch_moments. */
 void orc_moments(int n, const double* pos, const double* vel, const double* mass,
                  double* out);

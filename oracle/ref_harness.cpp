@@ -194,4 +194,62 @@ long long ref_dp45_run(int n, double* pos, double* vel, const double* mass,
     return ret;
 }
 
+/* PrintParticles + PrintCloud (bin/ioncloud.cpp:85-183) of the given state at lifetime t,
+ * ions named names[species[i]].  The text of <prefix>_pAll.txt followed by each
+ * <prefix>_cloud<k>.txt is copied into out (capacity cap bytes, NUL-terminated),
+ * files separated by a line "@@<file name suffix>".  Returns the length written. */
+long long ref_print(int n, const double* pos, const double* vel, const double* mass,
+                    const int* charge, const int* species, const char* const* names,
+                    int n_names, double t, char* out, long long cap) {
+    RefRun* r = new RefRun;
+    const double trapp[7] = {0, 0, 0, 1, 1, 0, 0};
+    setup(*r, 0, pos, vel, mass, charge, 0, 0, 0, 1.0, trapp, t, 1e-9, 1, 1e-7, 1e-7);
+    for (int i = 0; i < n; i++) {
+        Ion ion;
+        ion.mass = (long double)mass[i];
+        ion.charge = charge[i];
+        ion.SetName(names[species[i]]);
+        Particle p(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], vel[3 * i], vel[3 * i + 1],
+                   vel[3 * i + 2]);
+        r->cloud.AddParticle(p, ion);
+    }
+    r->cloud.InitializePoolVectors();
+    r->cloud.CopyParticlesToVectors();
+    r->cloud.lifetime = t;
+    r->cloud.PrintParticles();
+    r->cloud.PrintCloud();
+    r->cloud.globalstream->flush();
+    for (size_t k = 0; k < r->cloud.cloud_stream.size(); k++) r->cloud.cloud_stream[k]->flush();
+    long long len = 0;
+    std::string files[64];
+    int nf = 0;
+    files[nf++] = "_pAll.txt";
+    for (size_t k = 0; k < r->cloud.cloud_stream.size() && nf < 64; k++) {
+        char b[32];
+        snprintf(b, sizeof b, "_cloud%d.txt", (int)k);
+        files[nf++] = b;
+    }
+    for (int f = 0; f < nf; f++) {
+        std::string name = r->prefix + files[f];
+        std::string head = "@@" + files[f] + "\n";
+        if (len + (long long)head.size() < cap) {
+            memcpy(out + len, head.data(), head.size());
+            len += head.size();
+        }
+        FILE* fp = fopen(name.c_str(), "r");
+        if (!fp) continue;
+        char buf[4096];
+        size_t got;
+        while ((got = fread(buf, 1, sizeof buf, fp)) > 0)
+            for (size_t i = 0; i < got && len + 1 < cap; i++) out[len++] = buf[i];
+        fclose(fp);
+        if (f > 0) unlink(name.c_str());
+    }
+    if (cap > 0) out[len < cap ? len : cap - 1] = 0;
+    teardown(*r);
+    delete r;
+    (void)n_names;
+    return len;
+}
+
 }  // extern "C"

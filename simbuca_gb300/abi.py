@@ -83,7 +83,8 @@ EXPORTED = [
     "sg_batch_set_state", "sg_batch_download", "sg_batch_attempts", "sg_dp45_step",
     "sg_batch_run", "sg_batch_info", "sg_batch_set_field", "sg_batch_set_t_end",
     "sg_set_kernel_timing", "sg_kernel_timing", "sg_fixup_count", "sg_set_coulomb_variant",
-    "sg_batch_variant", "sg_init_cloud",
+    "sg_batch_variant", "sg_init_cloud", "sg_batch_set_recorder", "sg_batch_record_now",
+    "sg_batch_records", "sg_batch_read_records", "sg_batch_write_text",
     "sg_set_use_graph",
     "sg_timer_start",
     "sg_timer_stop", "sg_batch_moments", "sg_probe_peaks",
@@ -130,6 +131,15 @@ def _declare(L):
     L.sg_fixup_count.argtypes = [_vp, ctypes.POINTER(ctypes.c_int64)]
     L.sg_set_coulomb_variant.argtypes = [_vp, ctypes.c_int]
     L.sg_batch_variant.argtypes = [_vp, ctypes.POINTER(ctypes.c_int)]
+    L.sg_batch_set_recorder.argtypes = [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, _ip,
+                                        ctypes.c_int]
+    L.sg_batch_record_now.argtypes = [_vp]
+    L.sg_batch_records.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
+                                   ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.sg_batch_read_records.argtypes = [_vp, ctypes.c_int, ctypes.c_int64, _dp,
+                                        ctypes.POINTER(ctypes.c_int64)]
+    L.sg_batch_write_text.argtypes = [_vp, ctypes.c_int, ctypes.c_char_p,
+                                      ctypes.POINTER(ctypes.c_char_p), ctypes.c_int]
     L.sg_init_cloud.argtypes = [ctypes.c_int, _dp, ctypes.c_int, ctypes.c_uint32, _dp, _dp, _dp,
                                 _dp, _dp]
     L.sg_timer_start.argtypes = [_vp]

@@ -214,6 +214,47 @@ class Batch:
         check(self._L.sg_batch_variant(self.ctx.handle, ctypes.byref(v)), "sg_batch_variant")
         return v.value
 
+    def set_recorder(self, print_interval: float, stride: int = 1, capacity: int = 64,
+                     species=None, n_species: int = 1):
+        """Device-side observables every print_interval of simulated time (the
+        reference's print rule); species per ion in the caller's order."""
+        self._live()
+        sp = None
+        if species is not None:
+            self._species = np.ascontiguousarray(species, np.int32)
+            sp = iptr(self._species)
+        check(self._L.sg_batch_set_recorder(self.ctx.handle, float(print_interval), int(stride),
+                                            int(capacity), sp, int(n_species)),
+              "sg_batch_set_recorder")
+        self._n_species = int(n_species)
+
+    def record_now(self):
+        self._live()
+        check(self._L.sg_batch_record_now(self.ctx.handle), "sg_batch_record_now")
+
+    def records(self, cloud: int = 0):
+        """Drained records of a cloud: dict(t [R], stats [R, species, 9], ions [R, kept, 6])."""
+        self._live()
+        n, ln, kept = ctypes.c_int64(0), ctypes.c_int(0), ctypes.c_int(0)
+        check(self._L.sg_batch_records(self.ctx.handle, int(cloud), ctypes.byref(n),
+                                       ctypes.byref(ln), ctypes.byref(kept)), "sg_batch_records")
+        out = np.empty((n.value, max(ln.value, 1)))
+        got = ctypes.c_int64(0)
+        check(self._L.sg_batch_read_records(self.ctx.handle, int(cloud), n.value, dptr(out),
+                                            ctypes.byref(got)), "sg_batch_read_records")
+        out = out[:got.value]
+        S = getattr(self, "_n_species", 1)
+        return {"t": out[:, 0].copy(),
+                "stats": out[:, 1:1 + 9 * S].reshape(len(out), S, 9),
+                "ions": out[:, 1 + 9 * S:].reshape(len(out), kept.value, 6)}
+
+    def write_text(self, cloud: int, prefix: str, names):
+        """The reference's _pAll.txt / _cloud<s>.txt lines of the drained records."""
+        self._live()
+        arr = (ctypes.c_char_p * len(names))(*[x.encode() for x in names])
+        check(self._L.sg_batch_write_text(self.ctx.handle, int(cloud), prefix.encode(), arr,
+                                          len(names)), "sg_batch_write_text")
+
     def info(self):
         self._live()
         check(self._L.sg_batch_info(self.ctx.handle, self._info), "sg_batch_info")

@@ -5,7 +5,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <ctime>
 #include <mutex>
+#include <string>
 #include <utility>
 #include <vector>
 
@@ -55,6 +57,16 @@ struct Problem {
     int log_cap = 0;
     int use_mlp = 0;
     double safety = 0.9;
+    // recorder (device-side observables): rings of records per cloud, drained into
+    // host memory whenever the host synchronises
+    double* ring = nullptr;
+    int* spec0 = nullptr;  // species per ion, caller order
+    int* spec = nullptr;   // species per ion, device order
+    int n_species = 1, rec_stride = 1, rec_cap = 0;
+    double print_interval = 0.0;
+    std::vector<std::vector<double>> rec_host;
+    std::vector<int> hspec0;
+    std::vector<double> hmass0;
 };
 
 struct TimedLaunch {
@@ -129,6 +141,9 @@ void free_problem(Problem& P) {
     cudaFree(P.pst);
     cudaFree(P.wbf);
     cudaFree(P.dperm);
+    cudaFree(P.ring);
+    cudaFree(P.spec0);
+    cudaFree(P.spec);
     cudaFree(P.bbox);
     cudaFree(P.kq0);
     cudaFree(P.qm0);
@@ -348,6 +363,10 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(cudaMalloc(&P.wbf, SG_MLP_NP * 2));
     CK(cudaMemset(P.wbf, 0, SG_MLP_NP * 2));
     CK(dalloc(&P.dperm, N));
+    CK(dalloc(&P.spec0, N));
+    CK(dalloc(&P.spec, N));
+    CK(cudaMemset(P.spec0, 0, N * sizeof(int)));
+    CK(cudaMemset(P.spec, 0, N * sizeof(int)));
     CK(dalloc(&P.bbox, (size_t)std::max(P.ntiles, 1) * 8));
     CK(dalloc(&P.kq0, N));
     CK(dalloc(&P.qm0, N));
@@ -391,6 +410,52 @@ SgDpArgs dp_args(Problem& P) {
     a.npad = P.npad;
     a.fp32c = P.precision == SG_PREC_FP32C ? 1 : 0;
     return a;
+}
+
+SgRecArgs rec_args(Problem& P) {
+    SgRecArgs r;
+    r.rows = P.drows;
+    r.clouds = P.dc;
+    r.ctrl = P.dctrl;
+    r.y = P.y;
+    r.mass = P.mass;
+    r.spec = P.spec;
+    r.perm = P.dperm;
+    r.ring = P.ring;
+    r.n = P.n;
+    r.n_species = P.n_species;
+    r.stride = P.rec_stride;
+    return r;
+}
+
+// Moves the records written since the last drain into host memory and lets clouds held
+// by a full ring go on.  The stream must be idle and hctrl current (after sync_ctrl).
+int drain_records(sg_ctx* ctx, Problem& P) {
+    if (P.rec_cap <= 0) return SG_OK;
+    bool changed = false;
+    for (int c = 0; c < P.n_clouds; c++) {
+        SgCtrl& s = P.hctrl[c];
+        const SgCloud& cl = P.hc[c];
+        const long long k = s.rec_count - s.rec_drained;
+        if (k <= 0 && !(s.hold & 2)) continue;
+        std::vector<double>& dst = P.rec_host[c];
+        for (long long r = s.rec_drained; r < s.rec_count; r++) {
+            const size_t at = dst.size();
+            dst.resize(at + cl.rec_len);
+            const double* src = P.ring + cl.rec_off + (r % P.rec_cap) * (long long)cl.rec_len;
+            CK(cudaMemcpyAsync(dst.data() + at, src, sizeof(double) * cl.rec_len,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        s.rec_drained = s.rec_count;
+        s.hold &= ~2;
+        changed = true;
+    }
+    if (changed) {
+        CK(cudaMemcpyAsync(P.dctrl, P.hctrl, sizeof(SgCtrl) * P.n_clouds, cudaMemcpyHostToDevice,
+                           ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return SG_OK;
 }
 
 cudaEvent_t take_event(sg_ctx* ctx) {
@@ -500,6 +565,7 @@ int enqueue_attempt(sg_ctx* ctx, Problem& P) {
     }
     CK(sg_dp_control(P.dc, P.dctrl, P.err_part, P.y, P.n_clouds, P.flags + 1, ctx->stream));
     CK(sg_dp_commit(a, P.n_rows, ctx->stream));
+    if (P.rec_cap > 0) CK(sg_record(rec_args(P), P.n_rows, P.n_clouds, ctx->stream));
     if (P.log_cap > 0 || P.use_mlp) {
         CK(sg_moments(a, P.mass, P.mom, P.n_rows, ctx->stream));
         CK(sg_proposer_launch(P.dc, P.dctrl, P.mom, P.pst, P.wbf, P.log_feat, P.log_num,
@@ -600,7 +666,7 @@ int sync_ctrl(sg_ctx* ctx, Problem& P) {
     CK(cudaStreamSynchronize(ctx->stream));
     flush_timing(ctx);
     if (errword != 0) return errword;
-    return SG_OK;
+    return drain_records(ctx, P);
 }
 
 void fill_info(const Problem& P, sg_step_info* info) {
@@ -663,6 +729,7 @@ int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel) 
     CK(sg_gather(P.qm0, P.dperm, P.qm, P.n, ctx->stream));
     CK(sg_gather(P.qd0, P.dperm, P.qd, P.n, ctx->stream));
     CK(sg_gather(P.mass0, P.dperm, P.mass, P.n, ctx->stream));
+    CK(sg_gather_int(P.spec0, P.dperm, P.spec, P.n, ctx->stream));
     for (int c = 0; c < P.n_clouds; c++) {
         set_frame(P.hc[c], pos, P.hc[c].off);
         double v2 = 0.0;
@@ -922,6 +989,9 @@ int sg_batch_create(sg_ctx* ctx, int n_clouds, const int* counts, const sg_field
         return st;
     }
     memcpy(P.hctrl, P.hctrl0.data(), sizeof(SgCtrl) * n_clouds);
+    P.rec_host.assign(n_clouds, std::vector<double>());
+    P.hspec0.assign(P.n, 0);
+    P.hmass0.assign(P.n, 0.0);
     return SG_OK;
 }
 
@@ -940,6 +1010,8 @@ int sg_batch_upload(sg_ctx* ctx, const double* pos, const double* vel, const dou
     CK(cudaMemcpyAsync(P.qm0, qm.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(P.qd0, qd.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(P.mass0, mass, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    P.hmass0.assign(mass, mass + N);
+    for (auto& r : P.rec_host) r.clear();  // records of the previous state
     memcpy(P.hctrl, P.hctrl0.data(), sizeof(SgCtrl) * P.n_clouds);
     CK(cudaMemcpyAsync(P.dctrl, P.hctrl0.data(), sizeof(SgCtrl) * P.n_clouds,
                        cudaMemcpyHostToDevice, ctx->stream));
@@ -1051,6 +1123,189 @@ int sg_batch_run(sg_ctx* ctx, int64_t max_attempts, sg_step_info* info) {
     }
     fill_info(P, info);
     return st;
+}
+
+
+// ---- recorder: device-side observables and the reference's text output ------------
+int sg_batch_set_recorder(sg_ctx* ctx, double print_interval, int stride, int capacity,
+                          const int* species, int n_species) {
+    if (!ctx || stride < 1 || capacity < 0 || n_species < 1 || n_species > SG_MAX_SPECIES ||
+        !(print_interval >= 0.0))
+        return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    if (species)
+        for (int i = 0; i < P.n; i++)
+            if (species[i] < 0 || species[i] >= n_species) return SG_BAD_ARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    drop_graph(ctx);  // the attempt sequence gains or loses the record kernels
+    cudaFree(P.ring);
+    P.ring = nullptr;
+    P.rec_cap = capacity;
+    P.rec_stride = stride;
+    P.n_species = n_species;
+    P.print_interval = print_interval;
+    if (species)
+        P.hspec0.assign(species, species + P.n);
+    else
+        P.hspec0.assign(P.n, 0);
+    long long off = 0;
+    for (int c = 0; c < P.n_clouds; c++) {
+        SgCloud& cl = P.hc[c];
+        cl.nsel = (cl.n + stride - 1) / stride;
+        cl.rec_len = 1 + SG_STAT_LEN * n_species + 6 * cl.nsel;
+        cl.rec_off = off;
+        off += (long long)capacity * cl.rec_len;
+    }
+    if (capacity > 0) CK(dalloc(&P.ring, (size_t)off));
+    CK(cudaMemcpyAsync(P.spec0, P.hspec0.data(), sizeof(int) * P.n, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(sg_gather_int(P.spec0, P.dperm, P.spec, P.n, ctx->stream));
+    CK(cudaMemcpyAsync(P.dc, P.hc.data(), sizeof(SgCloud) * P.n_clouds, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    P.rec_host.assign(P.n_clouds, std::vector<double>());
+    // the print clock starts now: at the initial time before an upload, else at t
+    CK(cudaMemcpyAsync(P.hctrl, P.dctrl, sizeof(SgCtrl) * P.n_clouds, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int c = 0; c < P.n_clouds; c++) {
+        for (SgCtrl* s : {&P.hctrl0[c], &P.hctrl[c]}) {
+            s->print_interval = print_interval;
+            s->t_print0 = s->t;
+            s->n_print = 0;
+            s->rec_count = 0;
+            s->rec_drained = 0;
+            s->rec_cap = capacity;
+            s->print_due = 0;
+            s->hold &= ~2;
+        }
+        P.hctrl0[c].t_print0 = P.hctrl0[c].t;
+    }
+    if (!P.uploaded) memcpy(P.hctrl, P.hctrl0.data(), sizeof(SgCtrl) * P.n_clouds);
+    CK(cudaMemcpyAsync(P.dctrl, P.hctrl, sizeof(SgCtrl) * P.n_clouds, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
+int sg_batch_record_now(sg_ctx* ctx) {
+    if (!ctx) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (!P.uploaded) return SG_NOT_READY;
+    if (P.rec_cap <= 0) return SG_BAD_ARG;
+    CK(cudaSetDevice(ctx->device));
+    int st = sync_ctrl(ctx, P);  // drains: the rings have room
+    if (st != SG_OK) return st;
+    CK(sg_record_now(P.dctrl, P.n_clouds, ctx->stream));
+    CK(sg_record(rec_args(P), P.n_rows, P.n_clouds, ctx->stream));
+    return sync_ctrl(ctx, P);
+}
+
+int sg_batch_records(sg_ctx* ctx, int cloud, int64_t* n_records, int* record_len,
+                     int* n_kept) {
+    if (!ctx) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    if (cloud < 0 || cloud >= P.n_clouds) return SG_BAD_ARG;
+    const SgCloud& cl = P.hc[cloud];
+    const int len = P.rec_cap > 0 ? cl.rec_len : 0;
+    if (n_records) *n_records = len ? (int64_t)(P.rec_host[cloud].size() / len) : 0;
+    if (record_len) *record_len = len;
+    if (n_kept) *n_kept = P.rec_cap > 0 ? cl.nsel : 0;
+    return SG_OK;
+}
+
+int sg_batch_read_records(sg_ctx* ctx, int cloud, int64_t max_records, double* out,
+                          int64_t* n_read) {
+    if (!ctx || max_records < 0 || (max_records > 0 && !out)) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    if (cloud < 0 || cloud >= P.n_clouds || P.rec_cap <= 0) return SG_BAD_ARG;
+    const size_t len = (size_t)P.hc[cloud].rec_len;
+    std::vector<double>& src = P.rec_host[cloud];
+    const int64_t k = std::min<int64_t>(max_records, (int64_t)(src.size() / len));
+    if (k > 0) {
+        memcpy(out, src.data(), sizeof(double) * len * (size_t)k);
+        src.erase(src.begin(), src.begin() + (ptrdiff_t)(len * (size_t)k));
+    }
+    if (n_read) *n_read = k;
+    return SG_OK;
+}
+
+namespace {
+// File header of the reference's output files (bin/ioncloud.cpp:227-235, 246-253).
+void write_header(FILE* f, const char* columns) {
+    time_t now = time(nullptr);
+    fprintf(f, "#Simulation started: %s", ctime(&now));
+    fputs("#------------------------------------------------------------------------------#\n", f);
+    fputs("#                          JILA EDM Paul Trap Simulation                       #\n", f);
+    fputs("#      Dormand-Prince Runga-Kutta with Proportional Integrating controller     #\n", f);
+    fputs("#------------------------------------------------------------------------------#\n", f);
+    fputs(columns, f);
+    fputs("#*******************************************************************************\n", f);
+}
+
+FILE* open_append(const std::string& name, const char* columns) {
+    FILE* f = fopen(name.c_str(), "a");
+    if (f && ftell(f) == 0) write_header(f, columns);
+    return f;
+}
+}  // namespace
+
+// PrintParticles / PrintCloud lines (bin/ioncloud.cpp:85-183) for the drained records of
+// one cloud, appended to <prefix>_pAll.txt and <prefix>_cloud<s>.txt; the records are
+// consumed.  Scientific notation with 6 digits, as the reference's streams are set up.
+int sg_batch_write_text(sg_ctx* ctx, int cloud, const char* prefix, const char* const* names,
+                        int n_names) {
+    if (!ctx || !prefix || !names) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    if (cloud < 0 || cloud >= P.n_clouds || P.rec_cap <= 0 || n_names < P.n_species)
+        return SG_BAD_ARG;
+    const SgCloud& cl = P.hc[cloud];
+    const size_t len = (size_t)cl.rec_len;
+    std::vector<double>& recs = P.rec_host[cloud];
+    const size_t nrec = recs.size() / len;
+    const double j_to_ev = 6.24150e18;  // bin/globals.h:9
+    FILE* fa = open_append(std::string(prefix) + "_pAll.txt",
+                           "#index \t mass \t t (ms) \t x y z (mm) vx vy vz (m/s) \t Energy(eV)\n");
+    if (!fa) return SG_BAD_ARG;
+    std::vector<FILE*> fc(P.n_species, nullptr);
+    for (int s = 0; s < P.n_species; s++) {
+        fc[s] = open_append(std::string(prefix) + "_cloud" + std::to_string(s) + ".txt",
+                            "#index \t type \t #particules \t t (ms) \t x0 y0 z0 (mm) sx sy sz (m/s) \t Energy(eV)\n");
+        if (!fc[s]) {
+            fclose(fa);
+            for (FILE* f : fc)
+                if (f) fclose(f);
+            return SG_BAD_ARG;
+        }
+    }
+    for (size_t r = 0; r < nrec; r++) {
+        const double* rec = recs.data() + r * len;
+        const double t = rec[0];
+        const double* ions = rec + 1 + SG_STAT_LEN * P.n_species;
+        for (int j = 0; j < cl.nsel; j++) {
+            const int loc = j * P.rec_stride;
+            const int gi = cl.off + loc;
+            const double* y = ions + 6 * j;
+            const double e =
+                P.hmass0[gi] * (y[3] * y[3] + y[4] * y[4] + y[5] * y[5]) * 0.5 * j_to_ev;
+            fprintf(fa, "%d %s %e %e %e %e %e %e %e %e\n", loc, names[P.hspec0[gi]], t * 1000.0,
+                    y[0] * 1000.0, y[1] * 1000.0, y[2] * 1000.0, y[3], y[4], y[5], e);
+        }
+        for (int s = 0; s < P.n_species; s++) {
+            const double* o = rec + 1 + SG_STAT_LEN * s;
+            fprintf(fc[s], "%d %s %d %e %e %e %e %e %e %e %e\n", s, names[s], (int)o[8], t * 1e3,
+                    1000.0 * o[0], 1000.0 * o[1], 1000.0 * o[2], 1000.0 * o[3], 1000.0 * o[4],
+                    1000.0 * o[5], o[6]);
+        }
+    }
+    fclose(fa);
+    for (FILE* f : fc) fclose(f);
+    recs.clear();
+    return SG_OK;
 }
 
 int sg_batch_info(sg_ctx* ctx, sg_step_info* info) {

@@ -417,8 +417,10 @@ __global__ void dp_control_kernel(const SgCloud* __restrict__ clouds, SgCtrl* __
     const SgCloud cl = clouds[c];
     if (cs.done || cs.hold || cs.status != SG_OK) {
         ctrl[c].accepted = 0;
+        ctrl[c].print_due = 0;
         return;
     }
+    cs.print_due = 0;
     double s = 0.0;
     // Cash-Karp: the reference adds to the previous norm, odev.err is never reset there
     if (cs.method == 4) s = cs.err;
@@ -471,7 +473,20 @@ __global__ void dp_control_kernel(const SgCloud* __restrict__ clouds, SgCtrl* __
         cs.steps++;
         cs.rejects_here = 0;
         if (cs.t >= cs.t_end) cs.done = 1;
-        if (*hold_on_accept) cs.hold = 1;
+        if (*hold_on_accept) cs.hold |= 1;
+        // the reference prints after a step once (t - start) > interval * prints so far
+        // (bin/ion_fly.cpp:103-108); the record goes to the next ring slot, and a full
+        // ring holds the cloud until the host has drained it
+        if (cs.rec_cap > 0 && cs.print_interval > 0.0 &&
+            (cs.t - cs.t_print0) > cs.print_interval * (double)cs.n_print) {
+            cs.n_print++;
+            if (cs.rec_count - cs.rec_drained < cs.rec_cap) {
+                cs.print_due = 1;
+                cs.rec_slot = (int)(cs.rec_count % cs.rec_cap);
+                cs.rec_count++;
+            }
+            if (cs.rec_count - cs.rec_drained >= cs.rec_cap) cs.hold |= 2;
+        }
     }
     cs.accepted = accepted;
     ctrl[c] = cs;
@@ -479,7 +494,7 @@ __global__ void dp_control_kernel(const SgCloud* __restrict__ clouds, SgCtrl* __
 
 __global__ void clear_hold_kernel(SgCtrl* ctrl, int n_clouds) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < n_clouds) ctrl[c].hold = 0;
+    if (c < n_clouds) ctrl[c].hold &= ~1;
 }
 
 // Commit an accepted attempt: pos <- pos2, vel <- vel2 (bin/ode.cpp:488-489) and the

@@ -68,15 +68,25 @@ struct SgCloud {
     float wc;            // FP32c close-pair threshold on 1/r^3 (frame units)
     float pad2;
     sg_field_params fp;
+    long long rec_off;   // recorder: first double of this cloud's record ring
+    int32_t nsel;        // recorder: ions kept per record (every stride-th in caller order)
+    int32_t rec_len;     // recorder: doubles per record
 };
 
 // Per-cloud Dormand-Prince controller (the scalar part of _ode_vars, bin/ode.h:58-97).
 struct SgCtrl {
     double t, h, hnext, errold, err, t_end, rtol, atol, h_last;
+    // hold: bit 0 = one step per call taken, bit 1 = record ring full; either stops the
+    // cloud's kernels until the host clears it
     int32_t reject, adaptive, max_rejects, status, done, accepted, rejects_here, hold;
     int32_t method, pad2;  // 5 Dormand-Prince, 4 Cash-Karp, 1 Gear
     double hf[4];          // Gear: h^2/2, h^3/6, h^4/24, h^5/120 of the initial step
     long long steps, rejects, force_evals, coulomb_evals;
+    // recorder: the reference's print rule (bin/ion_fly.cpp:103-108), record due now
+    // when (t - t_print0) > print_interval * n_print after an accepted step
+    double print_interval, t_print0;
+    long long n_print, rec_count, rec_drained;
+    int32_t print_due, rec_slot, rec_cap, pad3;
 };
 
 // ---- learned step-size proposer (proposer.cu) -------------------------------------
@@ -174,6 +184,27 @@ struct SgDpArgs {
     int npad;             // padded ions
     int fp32c;            // write the FP32 frame coordinates
 };
+
+// ---- device-side observables (observe.cu) -------------------------------------------
+// A record of a cloud: [0] t, then per species s < n_species the PrintCloud statistics
+// (bin/ioncloud.cpp:148-183) x0 y0 z0 x1 y1 z1 (m) energy (eV) n_s n, then the state
+// x y z vx vy vz of every stride-th ion in the caller's order.
+#define SG_MAX_SPECIES 8
+#define SG_STAT_LEN 9
+struct SgRecArgs {
+    const SgRowBlock* rows;
+    const SgCloud* clouds;
+    const SgCtrl* ctrl;
+    const double* y;     // [6][N]
+    const double* mass;  // [N] kg, device order
+    const int* spec;     // [N] species, device order
+    const int* perm;     // device position -> caller's ion index
+    double* ring;
+    int n, n_species, stride;
+};
+cudaError_t sg_record(const SgRecArgs& r, int n_rows, int n_clouds, cudaStream_t st);
+cudaError_t sg_record_now(SgCtrl* ctrl, int n_clouds, cudaStream_t st);
+cudaError_t sg_gather_int(const int* src, const int* perm, int* dst, int n, cudaStream_t st);
 
 // ---- launchers implemented in the .cu files ------------------------------------
 cudaError_t sg_dp_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t st);

@@ -160,7 +160,24 @@ def main():
     np.savez_compressed(os.path.join(HERE, "init_cloud.npz"), **init)
     out["init_cloud"] = 2
 
-    # 8. fixed step, 40 steps of 2 ns
+    # 8. the reference's text output (PrintParticles + PrintCloud) of a two-species state
+    rng = configs.rng_for(31)
+    n = 300
+    species = (rng.random(n) < 0.3).astype(np.int32)  # 0 = Cs133, 1 = Rb87
+    mass = np.where(species == 0, 132.905, 86.909) * AMU
+    pos = rng.normal(0.0, 6e-4, (n, 3)) + np.array([1e-5, -2e-5, 3e-5])
+    vel = rng.normal(0.0, 120.0, (n, 3))
+    names = ["Cs133", "Rb87"]
+    text = oracle.ref_print(pos, vel, mass, np.ones(n, np.int32), species, names, 3.7e-6)
+    data = {k: [ln for ln in v.splitlines() if ln and not ln.startswith("#")]
+            for k, v in text.items()}
+    np.savez_compressed(os.path.join(HERE, "print_state.npz"), pos=pos, vel=vel, mass=mass,
+                        species=species, names=np.array(names), t=3.7e-6,
+                        pall=np.array(data["_pAll.txt"]), cloud0=np.array(data["_cloud0.txt"]),
+                        cloud1=np.array(data["_cloud1.txt"]))
+    out["print_state"] = len(data["_pAll.txt"])
+
+    # 9. fixed step, 40 steps of 2 ns
     c = cloud(64, 7)
     p, v, ctrl, hist, nh = oracle.ref_dp45_run(
         c.pos, c.vel, c.mass, c.charge, trap=1, tof=0, coulomb=1, coulomb_scale=1.0, trapp=TRAPP,

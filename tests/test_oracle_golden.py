@@ -166,3 +166,20 @@ def test_live_reference_random():
                            coulomb_scale=1.5, trapp=trapp)
     f = oracle.force(pos, vel, mass, charge, 3.3e-7, paul_fp(trapp, True, True, 1.5))
     assert np.array_equal(f, ref)
+
+
+def _num(lines):
+    return np.array([[float(x) for x in ln.split()[2:]] for ln in lines])
+
+
+def test_cloud_stats_match_reference_text():
+    """PrintCloud statistics (bin/ioncloud.cpp:148-183) of the oracle against the
+    reference's own output lines (6 significant digits)."""
+    g = np.load(os.path.join(GOLD, "print_state.npz"))
+    st = oracle.cloud_stats(g["pos"], g["vel"], g["mass"], g["species"], 2)
+    for s in range(2):
+        ln = str(g[f"cloud{s}"][0]).split()
+        assert int(ln[0]) == s and ln[1] == str(g["names"][s]) and int(ln[2]) == len(g["mass"])
+        ref = np.array([float(x) for x in ln[3:]])
+        mine = np.concatenate([[float(g["t"]) * 1e3], st[s, :6] * 1e3, st[s, 6:7]])
+        np.testing.assert_allclose(mine, ref, rtol=1.5e-6)
