@@ -288,6 +288,50 @@ int sg_batch_read_records(sg_ctx* ctx, int cloud, int64_t max_records, double* o
 int sg_batch_write_text(sg_ctx* ctx, int cloud, const char* prefix, const char* const* names,
                         int n_names);
 
+/* ---- operations: the reference's operation sequence, run on the device --------
+ * operations::launch (bin/operation.cpp:33-77, 111-124) runs its operations one after
+ * the other, each through move_particles (bin/ion_fly.cpp:17-116): steps are taken
+ * while t < t_start + duration, the trap ramp sets Vrf/Vdc before every step
+ * (bin/ion_fly.cpp:95-99).  Here the whole sequence advances inside the control kernel,
+ * on the device, between two attempts, with no host round trip:
+ *   NORMAL        trap terms on (the cloud's Paul and Penning terms), TOF off
+ *   TOF           trap off, TOF kick E_kick on
+ *   TRAP_RAMP     trap on, Vrf/Vdc = old (1 - r) + new r before each step,
+ *                 r = (t - t_start) / duration, old = the values when it starts
+ *   FREE          trap and TOF off (the reference's fall-through "free flight")
+ *   DISSOCIATION  no time passes; ions of species `reactant` become species `product`
+ *                 with print mass `product_mass` (kg) where the reference's MT19937
+ *                 stream, seeded 0, draws below `fraction`, one draw per reactant ion
+ *                 in order (bin/operation.cpp:59-70).  As in the reference the
+ *                 dynamics keep the ions' masses: only records and text change.
+ * print_time > 0 sets the recorder's print interval from that operation on;
+ * timestep > 0 sets h = hnext = print_time, which is what the reference does with its
+ * ode_timestep (bin/operation.cpp:36-39).  print_after records the state when the
+ * operation ends (odev.print_after_operation).  The batch's t_end is replaced by the
+ * end of the last operation.  Set after sg_batch_create (before or after an upload: an
+ * upload restarts the sequence). */
+enum {
+    SG_OP_NORMAL = 0,
+    SG_OP_TOF = 1,
+    SG_OP_TRAP_RAMP = 2,
+    SG_OP_FREE = 3,
+    SG_OP_DISSOCIATION = 4
+};
+typedef struct sg_operation {
+    int32_t kind;
+    int32_t print_after;
+    double duration;      /* s */
+    double print_time;    /* s, 0 = unchanged */
+    double timestep;      /* nonzero: h = hnext = print_time */
+    double new_vrf, new_vdc;  /* TRAP_RAMP targets (V) */
+    double e_kick;        /* TOF (V/m) */
+    int32_t reactant, product;  /* DISSOCIATION species */
+    double fraction, product_mass;
+} sg_operation;
+int sg_batch_set_operations(sg_ctx* ctx, const sg_operation* ops, int n_ops);
+/* Index of each cloud's current operation (n_ops once the sequence has ended). */
+int sg_batch_operation_index(sg_ctx* ctx, int* index);
+
 /* ---- initial cloud ------------------------------------------------------------
  * InitCloud (bin/initialization.cpp:117-206), host side: n ions uniform in the
  * ellipsoid offset + semiaxis * (unit ball), drawn by rejection from the unit cube;

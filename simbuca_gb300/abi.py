@@ -71,6 +71,19 @@ class StepInfo(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
 
 
+SG_OP_NORMAL, SG_OP_TOF, SG_OP_TRAP_RAMP, SG_OP_FREE, SG_OP_DISSOCIATION = 0, 1, 2, 3, 4
+
+
+class Operation(ctypes.Structure):
+    """sg_operation (include/simgb.h)."""
+    _fields_ = [("kind", ctypes.c_int32), ("print_after", ctypes.c_int32),
+                ("duration", ctypes.c_double), ("print_time", ctypes.c_double),
+                ("timestep", ctypes.c_double), ("new_vrf", ctypes.c_double),
+                ("new_vdc", ctypes.c_double), ("e_kick", ctypes.c_double),
+                ("reactant", ctypes.c_int32), ("product", ctypes.c_int32),
+                ("fraction", ctypes.c_double), ("product_mass", ctypes.c_double)]
+
+
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
 _vp = ctypes.c_void_p
@@ -85,6 +98,7 @@ EXPORTED = [
     "sg_set_kernel_timing", "sg_kernel_timing", "sg_fixup_count", "sg_set_coulomb_variant",
     "sg_batch_variant", "sg_init_cloud", "sg_batch_set_recorder", "sg_batch_record_now",
     "sg_batch_records", "sg_batch_read_records", "sg_batch_write_text",
+    "sg_batch_set_operations", "sg_batch_operation_index",
     "sg_set_use_graph",
     "sg_timer_start",
     "sg_timer_stop", "sg_batch_moments", "sg_probe_peaks",
@@ -140,6 +154,8 @@ def _declare(L):
                                         ctypes.POINTER(ctypes.c_int64)]
     L.sg_batch_write_text.argtypes = [_vp, ctypes.c_int, ctypes.c_char_p,
                                       ctypes.POINTER(ctypes.c_char_p), ctypes.c_int]
+    L.sg_batch_set_operations.argtypes = [_vp, ctypes.POINTER(Operation), ctypes.c_int]
+    L.sg_batch_operation_index.argtypes = [_vp, ctypes.POINTER(ctypes.c_int)]
     L.sg_init_cloud.argtypes = [ctypes.c_int, _dp, ctypes.c_int, ctypes.c_uint32, _dp, _dp, _dp,
                                 _dp, _dp]
     L.sg_timer_start.argtypes = [_vp]

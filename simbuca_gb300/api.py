@@ -233,7 +233,8 @@ class Batch:
         check(self._L.sg_batch_record_now(self.ctx.handle), "sg_batch_record_now")
 
     def records(self, cloud: int = 0):
-        """Drained records of a cloud: dict(t [R], stats [R, species, 9], ions [R, kept, 6])."""
+        """Drained records of a cloud: dict(t [R], stats [R, species, 9],
+        ions [R, kept, 8] = x y z vx vy vz, energy (eV), species)."""
         self._live()
         n, ln, kept = ctypes.c_int64(0), ctypes.c_int(0), ctypes.c_int(0)
         check(self._L.sg_batch_records(self.ctx.handle, int(cloud), ctypes.byref(n),
@@ -246,7 +247,7 @@ class Batch:
         S = getattr(self, "_n_species", 1)
         return {"t": out[:, 0].copy(),
                 "stats": out[:, 1:1 + 9 * S].reshape(len(out), S, 9),
-                "ions": out[:, 1 + 9 * S:].reshape(len(out), kept.value, 6)}
+                "ions": out[:, 1 + 9 * S:].reshape(len(out), kept.value, 8)}
 
     def write_text(self, cloud: int, prefix: str, names):
         """The reference's _pAll.txt / _cloud<s>.txt lines of the drained records."""
@@ -254,6 +255,26 @@ class Batch:
         arr = (ctypes.c_char_p * len(names))(*[x.encode() for x in names])
         check(self._L.sg_batch_write_text(self.ctx.handle, int(cloud), prefix.encode(), arr,
                                           len(names)), "sg_batch_write_text")
+
+    def set_operations(self, ops):
+        """The operation sequence (list of abi.Operation or dicts of its fields), run on
+        the device; replaces the batch's end time."""
+        self._live()
+        arr = (abi.Operation * max(len(ops), 1))()
+        for k, o in enumerate(ops):
+            if isinstance(o, dict):
+                for key, v in o.items():
+                    setattr(arr[k], key, v)
+            else:
+                arr[k] = o
+        check(self._L.sg_batch_set_operations(self.ctx.handle, arr, len(ops)),
+              "sg_batch_set_operations")
+
+    def operation_index(self):
+        self._live()
+        out = (ctypes.c_int * self.n_clouds)()
+        check(self._L.sg_batch_operation_index(self.ctx.handle, out), "sg_batch_operation_index")
+        return list(out)
 
     def info(self):
         self._live()

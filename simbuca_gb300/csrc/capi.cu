@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "sg_internal.cuh"
+#include "sg_mt19937.h"
 
 namespace {
 
@@ -67,6 +68,14 @@ struct Problem {
     std::vector<std::vector<double>> rec_host;
     std::vector<int> hspec0;
     std::vector<double> hmass0;
+    double *pmass = nullptr, *pmass0 = nullptr;  // print masses (dissociation), both orders
+    // operation sequence
+    std::vector<sg_field_params> fp0;  // field parameters as created / set by the caller
+    std::vector<SgOp> hops;
+    SgOp* dops = nullptr;
+    int* dis_spec = nullptr;     // [dissociations][N] caller order
+    double* dis_mass = nullptr;
+    int n_dis = 0;
 };
 
 struct TimedLaunch {
@@ -144,6 +153,11 @@ void free_problem(Problem& P) {
     cudaFree(P.ring);
     cudaFree(P.spec0);
     cudaFree(P.spec);
+    cudaFree(P.pmass);
+    cudaFree(P.pmass0);
+    cudaFree(P.dops);
+    cudaFree(P.dis_spec);
+    cudaFree(P.dis_mass);
     cudaFree(P.bbox);
     cudaFree(P.kq0);
     cudaFree(P.qm0);
@@ -367,6 +381,10 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(dalloc(&P.spec, N));
     CK(cudaMemset(P.spec0, 0, N * sizeof(int)));
     CK(cudaMemset(P.spec, 0, N * sizeof(int)));
+    CK(dalloc(&P.pmass, N));
+    CK(dalloc(&P.pmass0, N));
+    CK(cudaMemset(P.pmass, 0, N * sizeof(double)));
+    CK(cudaMemset(P.pmass0, 0, N * sizeof(double)));
     CK(dalloc(&P.bbox, (size_t)std::max(P.ntiles, 1) * 8));
     CK(dalloc(&P.kq0, N));
     CK(dalloc(&P.qm0, N));
@@ -412,14 +430,67 @@ SgDpArgs dp_args(Problem& P) {
     return a;
 }
 
+// Host copy of the per-cloud records, field parameters included, from the device.
+cudaError_t pull_clouds(sg_ctx* ctx, Problem& P) {
+    cudaError_t e = cudaMemcpyAsync(P.hc.data(), P.dc, sizeof(SgCloud) * P.n_clouds,
+                                    cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(ctx->stream);
+}
+
+// Species and print masses after each dissociation of the sequence, caller order: per
+// cloud the reference's loop over its ions (bin/operation.cpp:59-70) with MTRand seeded
+// 0 at each dissociation, one draw per ion of the reactant species.
+int dissociation_tables(sg_ctx* ctx, Problem& P) {
+    int n_dis = 0;
+    for (const SgOp& op : P.hops)
+        if (op.kind == SG_OP_DISSOCIATION) n_dis++;
+    cudaFree(P.dis_spec);
+    cudaFree(P.dis_mass);
+    P.dis_spec = nullptr;
+    P.dis_mass = nullptr;
+    P.n_dis = n_dis;
+    if (n_dis == 0) return SG_OK;
+    const size_t N = (size_t)P.n;
+    std::vector<int> spec(P.hspec0);
+    std::vector<double> mass(P.hmass0);
+    std::vector<int> ts(N * n_dis);
+    std::vector<double> tm(N * n_dis);
+    int d = 0;
+    for (const SgOp& op : P.hops) {
+        if (op.kind != SG_OP_DISSOCIATION) continue;
+        for (int c = 0; c < P.n_clouds; c++) {
+            SgMt19937 rng(0u);
+            for (int i = P.hc[c].off; i < P.hc[c].off + P.hc[c].n; i++)
+                if (spec[i] == op.reactant && rng.uniform() < op.fraction) {
+                    spec[i] = op.product;
+                    mass[i] = op.product_mass;
+                }
+        }
+        std::copy(spec.begin(), spec.end(), ts.begin() + d * N);
+        std::copy(mass.begin(), mass.end(), tm.begin() + d * N);
+        d++;
+    }
+    CK(dalloc(&P.dis_spec, N * n_dis));
+    CK(dalloc(&P.dis_mass, N * n_dis));
+    CK(cudaMemcpyAsync(P.dis_spec, ts.data(), sizeof(int) * ts.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(P.dis_mass, tm.data(), sizeof(double) * tm.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
 SgRecArgs rec_args(Problem& P) {
     SgRecArgs r;
     r.rows = P.drows;
     r.clouds = P.dc;
     r.ctrl = P.dctrl;
     r.y = P.y;
-    r.mass = P.mass;
+    r.mass = P.pmass;
     r.spec = P.spec;
+    r.dis_spec = P.dis_spec;
+    r.dis_mass = P.dis_mass;
     r.perm = P.dperm;
     r.ring = P.ring;
     r.n = P.n;
@@ -563,9 +634,12 @@ int enqueue_attempt(sg_ctx* ctx, Problem& P) {
             CK(sg_dp_stage(a, s, P.n_rows, ctx->stream));
         }
     }
-    CK(sg_dp_control(P.dc, P.dctrl, P.err_part, P.y, P.n_clouds, P.flags + 1, ctx->stream));
+    CK(sg_dp_control(P.dc, P.dctrl, P.err_part, P.y, P.n_clouds, P.flags + 1, P.dops,
+                     ctx->stream));
     CK(sg_dp_commit(a, P.n_rows, ctx->stream));
     if (P.rec_cap > 0) CK(sg_record(rec_args(P), P.n_rows, P.n_clouds, ctx->stream));
+    if (P.n_dis > 0)
+        CK(sg_dissociate(rec_args(P), P.pmass, P.spec0, P.pmass0, P.n_rows, ctx->stream));
     if (P.log_cap > 0 || P.use_mlp) {
         CK(sg_moments(a, P.mass, P.mom, P.n_rows, ctx->stream));
         CK(sg_proposer_launch(P.dc, P.dctrl, P.mom, P.pst, P.wbf, P.log_feat, P.log_num,
@@ -730,6 +804,7 @@ int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel) 
     CK(sg_gather(P.qd0, P.dperm, P.qd, P.n, ctx->stream));
     CK(sg_gather(P.mass0, P.dperm, P.mass, P.n, ctx->stream));
     CK(sg_gather_int(P.spec0, P.dperm, P.spec, P.n, ctx->stream));
+    CK(sg_gather(P.pmass0, P.dperm, P.pmass, P.n, ctx->stream));
     for (int c = 0; c < P.n_clouds; c++) {
         set_frame(P.hc[c], pos, P.hc[c].off);
         double v2 = 0.0;
@@ -955,6 +1030,7 @@ int sg_batch_create(sg_ctx* ctx, int n_clouds, const int* counts, const sg_field
     P.method = op[0].method == 0 ? 5 : op[0].method;
     P.hc.assign(n_clouds, SgCloud());
     for (int c = 0; c < n_clouds; c++) P.hc[c].fp = fp[c];
+    P.fp0.assign(fp, fp + n_clouds);
     plan(P, ctx->n_sm);
     P.hctrl0.assign(n_clouds, SgCtrl());
     for (int c = 0; c < n_clouds; c++) {
@@ -1011,13 +1087,28 @@ int sg_batch_upload(sg_ctx* ctx, const double* pos, const double* vel, const dou
     CK(cudaMemcpyAsync(P.qd0, qd.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(P.mass0, mass, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     P.hmass0.assign(mass, mass + N);
+    CK(cudaMemcpyAsync(P.pmass0, mass, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(P.spec0, P.hspec0.data(), N * sizeof(int), cudaMemcpyHostToDevice,
+                       ctx->stream));
     for (auto& r : P.rec_host) r.clear();  // records of the previous state
     memcpy(P.hctrl, P.hctrl0.data(), sizeof(SgCtrl) * P.n_clouds);
-    CK(cudaMemcpyAsync(P.dctrl, P.hctrl0.data(), sizeof(SgCtrl) * P.n_clouds,
-                       cudaMemcpyHostToDevice, ctx->stream));
+    // the operation sequence restarts from the caller's field parameters
+    for (int c = 0; c < P.n_clouds; c++) {
+        P.hc[c].fp = P.fp0[c];
+        if (!P.hops.empty()) sg_start_ops(P.hctrl[c], P.hc[c].fp, P.hops.data(), 0);
+    }
+    {
+        int st0 = dissociation_tables(ctx, P);
+        if (st0 != SG_OK) return st0;
+    }
+    CK(cudaMemcpyAsync(P.dctrl, P.hctrl, sizeof(SgCtrl) * P.n_clouds, cudaMemcpyHostToDevice,
+                       ctx->stream));
     CK(cudaMemsetAsync(P.flags, 0, 4 * sizeof(int), ctx->stream));
     int st = upload_state(ctx, P, pos, vel);
     if (st != SG_OK) return st;
+    // a dissociation at the very start of the sequence
+    if (P.n_dis > 0)
+        CK(sg_dissociate(rec_args(P), P.pmass, P.spec0, P.pmass0, P.n_rows, ctx->stream));
     // stage-1 Coulomb sum of the initial state
     st = launch_coulomb(ctx, P, true, active_interactions(P), P.coul1);
     if (st != SG_OK) return st;
@@ -1036,6 +1127,8 @@ int sg_batch_set_state(sg_ctx* ctx, const double* pos, const double* vel) {
     Problem& P = ctx->batch;
     if (!P.uploaded) return SG_NOT_READY;
     CK(cudaSetDevice(ctx->device));
+    // field parameters as the device has them now (a ramp may have moved them)
+    CK(pull_clouds(ctx, P));
     int st = upload_state(ctx, P, pos, vel);
     if (st != SG_OK) return st;
     st = launch_coulomb(ctx, P, true, active_interactions(P), P.coul1);
@@ -1154,11 +1247,17 @@ int sg_batch_set_recorder(sg_ctx* ctx, double print_interval, int stride, int ca
     for (int c = 0; c < P.n_clouds; c++) {
         SgCloud& cl = P.hc[c];
         cl.nsel = (cl.n + stride - 1) / stride;
-        cl.rec_len = 1 + SG_STAT_LEN * n_species + 6 * cl.nsel;
+        cl.rec_len = 1 + SG_STAT_LEN * n_species + SG_ION_LEN * cl.nsel;
         cl.rec_off = off;
         off += (long long)capacity * cl.rec_len;
     }
     if (capacity > 0) CK(dalloc(&P.ring, (size_t)off));
+    {
+        // keep the device's field parameters (a ramp may have moved them)
+        std::vector<SgCloud> cur(P.n_clouds);
+        CK(cudaMemcpy(cur.data(), P.dc, sizeof(SgCloud) * P.n_clouds, cudaMemcpyDeviceToHost));
+        for (int c = 0; c < P.n_clouds; c++) P.hc[c].fp = cur[c].fp;
+    }
     CK(cudaMemcpyAsync(P.spec0, P.hspec0.data(), sizeof(int) * P.n, cudaMemcpyHostToDevice,
                        ctx->stream));
     CK(sg_gather_int(P.spec0, P.dperm, P.spec, P.n, ctx->stream));
@@ -1267,7 +1366,6 @@ int sg_batch_write_text(sg_ctx* ctx, int cloud, const char* prefix, const char* 
     const size_t len = (size_t)cl.rec_len;
     std::vector<double>& recs = P.rec_host[cloud];
     const size_t nrec = recs.size() / len;
-    const double j_to_ev = 6.24150e18;  // bin/globals.h:9
     FILE* fa = open_append(std::string(prefix) + "_pAll.txt",
                            "#index \t mass \t t (ms) \t x y z (mm) vx vy vz (m/s) \t Energy(eV)\n");
     if (!fa) return SG_BAD_ARG;
@@ -1288,12 +1386,10 @@ int sg_batch_write_text(sg_ctx* ctx, int cloud, const char* prefix, const char* 
         const double* ions = rec + 1 + SG_STAT_LEN * P.n_species;
         for (int j = 0; j < cl.nsel; j++) {
             const int loc = j * P.rec_stride;
-            const int gi = cl.off + loc;
-            const double* y = ions + 6 * j;
-            const double e =
-                P.hmass0[gi] * (y[3] * y[3] + y[4] * y[4] + y[5] * y[5]) * 0.5 * j_to_ev;
-            fprintf(fa, "%d %s %e %e %e %e %e %e %e %e\n", loc, names[P.hspec0[gi]], t * 1000.0,
-                    y[0] * 1000.0, y[1] * 1000.0, y[2] * 1000.0, y[3], y[4], y[5], e);
+            const double* y = ions + SG_ION_LEN * j;
+            const int sp = (int)y[7];
+            fprintf(fa, "%d %s %e %e %e %e %e %e %e %e\n", loc, names[sp], t * 1000.0,
+                    y[0] * 1000.0, y[1] * 1000.0, y[2] * 1000.0, y[3], y[4], y[5], y[6]);
         }
         for (int s = 0; s < P.n_species; s++) {
             const double* o = rec + 1 + SG_STAT_LEN * s;
@@ -1305,6 +1401,98 @@ int sg_batch_write_text(sg_ctx* ctx, int cloud, const char* prefix, const char* 
     fclose(fa);
     for (FILE* f : fc) fclose(f);
     recs.clear();
+    return SG_OK;
+}
+
+
+// ---- operation sequence -----------------------------------------------------------
+int sg_batch_set_operations(sg_ctx* ctx, const sg_operation* ops, int n_ops) {
+    if (!ctx || n_ops < 0 || n_ops > 64 || (n_ops > 0 && !ops)) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    std::vector<SgOp> h(n_ops);
+    int d = 0;
+    for (int k = 0; k < n_ops; k++) {
+        const sg_operation& o = ops[k];
+        if (o.kind < SG_OP_NORMAL || o.kind > SG_OP_DISSOCIATION) return SG_BAD_ARG;
+        if (!(o.duration >= 0.0) || !(o.print_time >= 0.0)) return SG_BAD_ARG;
+        // ode_timestep sets the step to print_time: it must be a step
+        if (o.timestep != 0.0 && !(o.print_time > 0.0)) return SG_BAD_ARG;
+        if (o.kind == SG_OP_DISSOCIATION &&
+            (o.reactant < 0 || o.reactant >= SG_MAX_SPECIES || o.product < 0 ||
+             o.product >= SG_MAX_SPECIES || !(o.product_mass > 0.0)))
+            return SG_BAD_ARG;
+        SgOp& q = h[k];
+        memset(&q, 0, sizeof q);
+        q.kind = o.kind;
+        q.print_after = o.print_after != 0;
+        q.duration = o.kind == SG_OP_DISSOCIATION ? 0.0 : o.duration;
+        q.print_time = o.print_time;
+        q.timestep = o.timestep;
+        q.new_vrf = o.new_vrf;
+        q.new_vdc = o.new_vdc;
+        q.e_kick = o.e_kick;
+        q.reactant = o.reactant;
+        q.product = o.product;
+        q.fraction = o.fraction;
+        q.product_mass = o.product_mass;
+        q.dis_index = o.kind == SG_OP_DISSOCIATION ? d++ : -1;
+    }
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    drop_graph(ctx);
+    cudaFree(P.dops);
+    P.dops = nullptr;
+    P.hops = h;
+    if (n_ops > 0) {
+        CK(dalloc(&P.dops, (size_t)n_ops));
+        CK(cudaMemcpy(P.dops, h.data(), sizeof(SgOp) * n_ops, cudaMemcpyHostToDevice));
+    }
+    for (int c = 0; c < P.n_clouds; c++) {
+        const int bits = P.fp0[c].flags & (SG_F_PAUL | SG_F_PENNING);
+        P.hctrl0[c].n_ops = n_ops;
+        P.hctrl0[c].trap_bits = bits;
+        P.hctrl0[c].op_index = 0;
+        P.hctrl0[c].dis_due = 0;
+    }
+    if (!P.uploaded) return dissociation_tables(ctx, P);
+    // start the sequence now, from the caller's field parameters, at each cloud's time
+    int st = sync_ctrl(ctx, P);
+    if (st != SG_OK) return st;
+    for (int c = 0; c < P.n_clouds; c++) {
+        SgCtrl& cs = P.hctrl[c];
+        cs.n_ops = n_ops;
+        cs.trap_bits = P.hctrl0[c].trap_bits;
+        cs.dis_due = 0;
+        P.hc[c].fp = P.fp0[c];
+        if (n_ops > 0 && cs.status == SG_OK) {
+            cs.done = 0;
+            sg_start_ops(cs, P.hc[c].fp, P.hops.data(), 0);
+        }
+    }
+    st = dissociation_tables(ctx, P);
+    if (st != SG_OK) return st;
+    {
+        std::vector<SgCloud> cur(P.n_clouds);
+        CK(cudaMemcpy(cur.data(), P.dc, sizeof(SgCloud) * P.n_clouds, cudaMemcpyDeviceToHost));
+        for (int c = 0; c < P.n_clouds; c++) cur[c].fp = P.hc[c].fp;
+        CK(cudaMemcpy(P.dc, cur.data(), sizeof(SgCloud) * P.n_clouds, cudaMemcpyHostToDevice));
+    }
+    CK(cudaMemcpy(P.dctrl, P.hctrl, sizeof(SgCtrl) * P.n_clouds, cudaMemcpyHostToDevice));
+    if (P.n_dis > 0)
+        CK(sg_dissociate(rec_args(P), P.pmass, P.spec0, P.pmass0, P.n_rows, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
+int sg_batch_operation_index(sg_ctx* ctx, int* index) {
+    if (!ctx || !index) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    int st = sync_ctrl(ctx, P);
+    if (st != SG_OK) return st;
+    for (int c = 0; c < P.n_clouds; c++) index[c] = P.hctrl[c].op_index;
     return SG_OK;
 }
 
@@ -1325,6 +1513,7 @@ int sg_batch_set_field(sg_ctx* ctx, int cloud, const sg_field_params* fp) {
     if ((fp->flags & SG_F_COULOMB) != (P.hc[cloud].fp.flags & SG_F_COULOMB)) return SG_BAD_ARG;
     CK(cudaSetDevice(ctx->device));
     P.hc[cloud].fp = *fp;
+    P.fp0[cloud] = *fp;
     CK(cudaMemcpyAsync(&P.dc[cloud].fp, fp, sizeof(sg_field_params), cudaMemcpyHostToDevice,
                        ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));

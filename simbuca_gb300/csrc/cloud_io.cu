@@ -14,39 +14,9 @@
 #include <cstring>
 
 #include "../../include/simgb.h"
+#include "sg_mt19937.h"
 
 namespace {
-
-class Mt19937 {
-public:
-    explicit Mt19937(uint32_t s) {
-        st_[0] = s;
-        for (int i = 1; i < N; i++) st_[i] = 1812433253u * (st_[i - 1] ^ (st_[i - 1] >> 30)) + (uint32_t)i;
-        pos_ = N;
-    }
-    uint32_t next() {
-        if (pos_ == N) twist();
-        uint32_t y = st_[pos_++];
-        y ^= y >> 11;
-        y ^= (y << 7) & 0x9d2c5680u;
-        y ^= (y << 15) & 0xefc60000u;
-        return y ^ (y >> 18);
-    }
-    double uniform() { return (double)next() * (1.0 / 4294967296.0); }
-
-private:
-    static constexpr int N = 624, M = 397;
-    static uint32_t mix(uint32_t u, uint32_t v) {
-        const uint32_t y = (u & 0x80000000u) | (v & 0x7fffffffu);
-        return (y >> 1) ^ ((v & 1u) ? 0x9908b0dfu : 0u);
-    }
-    void twist() {
-        for (int i = 0; i < N; i++) st_[i] = st_[(i + M) % N] ^ mix(st_[i], st_[(i + 1) % N]);
-        pos_ = 0;
-    }
-    uint32_t st_[N];
-    int pos_;
-};
 
 // bin/globals.h:4,11 (pi, eV_to_Joule)
 constexpr double kPi = 3.14159265358979323;
@@ -60,7 +30,7 @@ extern "C" int sg_init_cloud(int n, const double* ev_max, int n_ev, uint32_t see
     if (n < 0 || (n > 0 && (!ev_max || !semiaxis || !offset || !mass || !pos || !vel)))
         return SG_BAD_ARG;
     if (n_ev != 1 && n_ev != 2) return SG_BAD_ARG;
-    Mt19937 rng(seed);
+    SgMt19937 rng(seed);
     for (int i = 0; i < n; i++) {
         double u[3];
         for (;;) {

@@ -408,9 +408,10 @@ __global__ void __launch_bounds__(SG_ROWS) gear_kernel(DpArgs a) {
 // error_succes + step bookkeeping (bin/ode.cpp:426-494), one thread per cloud.
 // With *hold_on_accept set, a cloud that accepts holds (skips further attempts) until
 // the host clears the hold: used to take exactly one step per cloud.
-__global__ void dp_control_kernel(const SgCloud* __restrict__ clouds, SgCtrl* __restrict__ ctrl,
+__global__ void dp_control_kernel(SgCloud* __restrict__ clouds, SgCtrl* __restrict__ ctrl,
                                   const double* __restrict__ err_part, const double* __restrict__ y,
-                                  int n_clouds, const int* __restrict__ hold_on_accept) {
+                                  int n_clouds, const int* __restrict__ hold_on_accept,
+                                  const SgOp* __restrict__ ops) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n_clouds) return;
     SgCtrl cs = ctrl[c];
@@ -472,14 +473,31 @@ __global__ void dp_control_kernel(const SgCloud* __restrict__ clouds, SgCtrl* __
         cs.h = cs.hnext;
         cs.steps++;
         cs.rejects_here = 0;
-        if (cs.t >= cs.t_end) cs.done = 1;
+        int print_now = 0;
+        if (cs.n_ops > 0) {
+            cs.dis_due = 0;
+            if (cs.t >= cs.t_end) {
+                // the operation has ended: print after it, start the next one
+                print_now = ops[cs.op_index].print_after;
+                print_now |= sg_start_ops(cs, clouds[c].fp, ops, cs.op_index + 1);
+            } else if (ops[cs.op_index].kind == SG_OP_TRAP_RAMP) {
+                // Vrf/Vdc for the next step (bin/ion_fly.cpp:95-99)
+                const SgOp& op = ops[cs.op_index];
+                const double ramp = (cs.t - cs.t_op_start) / (cs.t_end - cs.t_op_start);
+                clouds[c].fp.Vrf = cs.old_vrf * (1 - ramp) + op.new_vrf * ramp;
+                clouds[c].fp.Vdc = cs.old_vdc * (1 - ramp) + op.new_vdc * ramp;
+            }
+        } else if (cs.t >= cs.t_end) {
+            cs.done = 1;
+        }
         if (*hold_on_accept) cs.hold |= 1;
         // the reference prints after a step once (t - start) > interval * prints so far
         // (bin/ion_fly.cpp:103-108); the record goes to the next ring slot, and a full
         // ring holds the cloud until the host has drained it
-        if (cs.rec_cap > 0 && cs.print_interval > 0.0 &&
-            (cs.t - cs.t_print0) > cs.print_interval * (double)cs.n_print) {
-            cs.n_print++;
+        const bool rule = cs.print_interval > 0.0 &&
+                          (cs.t - cs.t_print0) > cs.print_interval * (double)cs.n_print;
+        if (cs.rec_cap > 0 && (rule || print_now)) {
+            if (rule) cs.n_print++;
             if (cs.rec_count - cs.rec_drained < cs.rec_cap) {
                 cs.print_due = 1;
                 cs.rec_slot = (int)(cs.rec_count % cs.rec_cap);
@@ -695,11 +713,11 @@ cudaError_t sg_gear_init(const SgDpArgs& a, const int* perm, int n_rows, cudaStr
     return cudaGetLastError();
 }
 
-cudaError_t sg_dp_control(const SgCloud* clouds, SgCtrl* ctrl, const double* err_part,
+cudaError_t sg_dp_control(SgCloud* clouds, SgCtrl* ctrl, const double* err_part,
                           const double* y, int n_clouds, const int* hold_on_accept,
-                          cudaStream_t st) {
+                          const SgOp* ops, cudaStream_t st) {
     dp_control_kernel<<<(n_clouds + 127) / 128, 128, 0, st>>>(clouds, ctrl, err_part, y, n_clouds,
-                                                              hold_on_accept);
+                                                              hold_on_accept, ops);
     return cudaGetLastError();
 }
 

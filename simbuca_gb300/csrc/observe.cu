@@ -27,10 +27,30 @@ __global__ void __launch_bounds__(SG_ROWS) record_ions_kernel(SgRecArgs r) {
     const int i = rb.i0 + li;
     const int loc = r.perm[i] - cl.off;
     if (loc % r.stride) return;
-    double* out = record_of(r, cl, cs) + 1 + SG_STAT_LEN * r.n_species + 6 * (loc / r.stride);
+    double* out = record_of(r, cl, cs) + 1 + SG_STAT_LEN * r.n_species + SG_ION_LEN * (loc / r.stride);
     const size_t N = (size_t)r.n;
 #pragma unroll
     for (int c = 0; c < 6; c++) out[c] = r.y[c * N + i];
+    // PrintParticle's energy (bin/ioncloud.cpp:86)
+    out[6] = r.mass[i] * (out[3] * out[3] + out[4] * out[4] + out[5] * out[5]) * 0.5 * kJouleToEv;
+    out[7] = (double)r.spec[i];
+}
+
+// Species and print masses after a dissociation (tables in the caller's order).
+__global__ void __launch_bounds__(SG_ROWS) dissociate_kernel(SgRecArgs r, double* __restrict__ mass,
+                                                             int* __restrict__ spec0,
+                                                             double* __restrict__ mass0) {
+    const SgRowBlock rb = r.rows[blockIdx.x];
+    const SgCtrl& cs = r.ctrl[rb.cloud];
+    if (!cs.dis_due) return;
+    const int li = threadIdx.x;
+    if (li >= rb.n) return;
+    const int i = rb.i0 + li;
+    const size_t at = (size_t)(cs.dis_due - 1) * r.n + r.perm[i];
+    r.spec[i] = r.dis_spec[at];
+    mass[i] = r.dis_mass[at];
+    spec0[r.perm[i]] = r.dis_spec[at];  // caller's order, for later state uploads
+    mass0[r.perm[i]] = r.dis_mass[at];
 }
 
 // Block-wide sum of K values per thread into red (thread 0 reads the totals).
@@ -161,6 +181,12 @@ cudaError_t sg_gather_int(const int* src, const int* perm, int* dst, int n, cuda
 cudaError_t sg_record(const SgRecArgs& r, int n_rows, int n_clouds, cudaStream_t st) {
     if (n_rows > 0) record_ions_kernel<<<n_rows, SG_ROWS, 0, st>>>(r);
     if (n_clouds > 0) record_stats_kernel<<<n_clouds, 256, 0, st>>>(r);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_dissociate(const SgRecArgs& r, double* mass, int* spec0, double* mass0, int n_rows,
+                          cudaStream_t st) {
+    if (n_rows > 0) dissociate_kernel<<<n_rows, SG_ROWS, 0, st>>>(r, mass, spec0, mass0);
     return cudaGetLastError();
 }
 

@@ -87,7 +87,55 @@ struct SgCtrl {
     double print_interval, t_print0;
     long long n_print, rec_count, rec_drained;
     int32_t print_due, rec_slot, rec_cap, pad3;
+    // operation sequence (sg_batch_set_operations): current operation, its start, the
+    // ramp's starting Vrf/Vdc, the cloud's trap terms, dissociation to apply (index+1)
+    int32_t op_index, n_ops, trap_bits, dis_due;
+    double t_op_start, old_vrf, old_vdc;
 };
+
+// One operation of the sequence (sg_operation plus the row of its dissociation table).
+struct SgOp {
+    int32_t kind, print_after;
+    double duration, print_time, timestep, new_vrf, new_vdc, e_kick;
+    int32_t dis_index, reactant, product, pad;
+    double fraction, product_mass;
+};
+
+// Starts operation `from` of the sequence at the cloud's current time: the settings of
+// operation::launch (bin/operation.cpp:33-77) and move_particles' end time; operations
+// that take no time end at once (a dissociation applies its table).  Past the last
+// operation the cloud is done.  Returns 1 if an ended operation asked for a print.
+__host__ __device__ inline int sg_start_ops(SgCtrl& cs, sg_field_params& fp, const SgOp* ops,
+                                            int from) {
+    int print = 0;
+    for (int k = from; k < cs.n_ops; k++) {
+        const SgOp& op = ops[k];
+        cs.op_index = k;
+        if (op.kind == SG_OP_DISSOCIATION) {
+            cs.dis_due = op.dis_index + 1;
+            continue;
+        }
+        if (op.print_time > 0.0) cs.print_interval = op.print_time;
+        if (op.timestep != 0.0) cs.h = cs.hnext = op.print_time;
+        const bool trap = op.kind == SG_OP_NORMAL || op.kind == SG_OP_TRAP_RAMP;
+        fp.flags = trap ? (fp.flags | cs.trap_bits) : (fp.flags & ~cs.trap_bits);
+        if (op.kind == SG_OP_TOF) {
+            fp.flags |= SG_F_TOF;
+            fp.E_kick = op.e_kick;
+        } else {
+            fp.flags &= ~SG_F_TOF;
+        }
+        cs.old_vrf = fp.Vrf;
+        cs.old_vdc = fp.Vdc;
+        cs.t_op_start = cs.t;
+        cs.t_end = cs.t + op.duration;
+        if (cs.t < cs.t_end) return print;
+        print |= op.print_after;
+    }
+    cs.op_index = cs.n_ops;
+    cs.done = 1;
+    return print;
+}
 
 // ---- learned step-size proposer (proposer.cu) -------------------------------------
 #define SG_MLP_IN 16
@@ -188,21 +236,27 @@ struct SgDpArgs {
 // ---- device-side observables (observe.cu) -------------------------------------------
 // A record of a cloud: [0] t, then per species s < n_species the PrintCloud statistics
 // (bin/ioncloud.cpp:148-183) x0 y0 z0 x1 y1 z1 (m) energy (eV) n_s n, then the state
-// x y z vx vy vz of every stride-th ion in the caller's order.
+// x y z vx vy vz, energy (eV) and species of every stride-th ion in the caller's order.
 #define SG_MAX_SPECIES 8
 #define SG_STAT_LEN 9
+#define SG_ION_LEN 8
 struct SgRecArgs {
     const SgRowBlock* rows;
     const SgCloud* clouds;
     const SgCtrl* ctrl;
     const double* y;     // [6][N]
-    const double* mass;  // [N] kg, device order
-    const int* spec;     // [N] species, device order
+    const double* mass;  // [N] print mass (kg), device order
+    int* spec;           // [N] species, device order
+    const int* dis_spec;     // dissociation tables [tables][N] in the caller's order
+    const double* dis_mass;
     const int* perm;     // device position -> caller's ion index
     double* ring;
     int n, n_species, stride;
 };
 cudaError_t sg_record(const SgRecArgs& r, int n_rows, int n_clouds, cudaStream_t st);
+// species and print masses of a dissociation that the control kernel applied
+cudaError_t sg_dissociate(const SgRecArgs& r, double* mass, int* spec0, double* mass0, int n_rows,
+                          cudaStream_t st);
 cudaError_t sg_record_now(SgCtrl* ctrl, int n_clouds, cudaStream_t st);
 cudaError_t sg_gather_int(const int* src, const int* perm, int* dst, int n, cudaStream_t st);
 
@@ -212,9 +266,9 @@ cudaError_t sg_ck_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t s
 // Gear: phase 0 predicts, phase 1 corrects; sg_gear_init seeds the Gear state in k
 cudaError_t sg_gear_stage(const SgDpArgs& a, int phase, int n_rows, cudaStream_t st);
 cudaError_t sg_gear_init(const SgDpArgs& a, const int* perm, int n_rows, cudaStream_t st);
-cudaError_t sg_dp_control(const SgCloud* clouds, SgCtrl* ctrl, const double* err_part,
+cudaError_t sg_dp_control(SgCloud* clouds, SgCtrl* ctrl, const double* err_part,
                           const double* y, int n_clouds, const int* hold_on_accept,
-                          cudaStream_t st);
+                          const SgOp* ops, cudaStream_t st);
 cudaError_t sg_clear_hold(SgCtrl* ctrl, int n_clouds, cudaStream_t st);
 int sg_probe_iters(int which);
 cudaError_t sg_dp_commit(const SgDpArgs& a, int n_rows, cudaStream_t st);

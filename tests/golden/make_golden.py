@@ -55,7 +55,35 @@ def init_library():
     return lib
 
 
+OPS = dict(kinds=[0, 2, 1, 3, 0], durations=[4e-8, 6e-8, 2e-8, 2e-8, 3e-8],
+           new_vrf=[0, 80.0, 0, 0, 0], new_vdc=[0, 2.0, 0, 0, 0], e_kick=[0, 0, 50.0, 0, 0])
+
+
+def ops_scenario(path):
+    """One operation sequence through the reference's operations::launch, in a process
+    of its own (the reference keeps the run's state in globals)."""
+    lib = init_library()
+    c = cloud(64, 41)
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    arrs = {k: np.ascontiguousarray(v, np.float64) for k, v in OPS.items() if k != "kinds"}
+    kinds = np.ascontiguousarray(OPS["kinds"], np.int32)
+    pos, vel, t = np.zeros((64, 3)), np.zeros((64, 3)), np.zeros(3)
+    lib.ref_ops_run(64, c.pos.ctypes.data_as(dp), c.vel.ctypes.data_as(dp),
+                    c.mass.ctypes.data_as(dp), c.charge.ctypes.data_as(ip),
+                    TRAPP.ctypes.data_as(dp), 1, ctypes.c_double(2e-9), 5, len(kinds),
+                    kinds.ctypes.data_as(ip), arrs["durations"].ctypes.data_as(dp),
+                    arrs["new_vrf"].ctypes.data_as(dp), arrs["new_vdc"].ctypes.data_as(dp),
+                    arrs["e_kick"].ctypes.data_as(dp), pos.ctypes.data_as(dp),
+                    vel.ctypes.data_as(dp), t.ctypes.data_as(dp))
+    np.savez_compressed(path, pos0=c.pos, vel0=c.vel, mass=c.mass, charge=c.charge, pos=pos,
+                        vel=vel, t=t, h0=2e-9, **{k: np.asarray(v) for k, v in OPS.items()})
+
+
 def main():
+    if len(sys.argv) > 2 and sys.argv[1] == "--ops":
+        ops_scenario(sys.argv[2])
+        return
     oracle.build(ref=True)
     assert oracle.ref_available(), "reference harness did not build"
     out = {}
@@ -177,7 +205,13 @@ def main():
                         cloud1=np.array(data["_cloud1.txt"]))
     out["print_state"] = len(data["_pAll.txt"])
 
-    # 9. fixed step, 40 steps of 2 ns
+    # 9. an operation sequence (normal, trap ramp, TOF, free flight, normal) with fixed
+    #    2 ns Dormand-Prince steps through the reference's operations::launch
+    subprocess.run([sys.executable, os.path.abspath(__file__), "--ops",
+                    os.path.join(HERE, "ops_sequence.npz")], check=True)
+    out["ops_sequence"] = float(np.load(os.path.join(HERE, "ops_sequence.npz"))["t"][0])
+
+    # 10. fixed step, 40 steps of 2 ns
     c = cloud(64, 7)
     p, v, ctrl, hist, nh = oracle.ref_dp45_run(
         c.pos, c.vel, c.mass, c.charge, trap=1, tof=0, coulomb=1, coulomb_scale=1.0, trapp=TRAPP,

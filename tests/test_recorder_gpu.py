@@ -45,7 +45,11 @@ def test_record_now_vs_oracle(ctx, n, prec):
     assert r["t"].tolist() == [2.5e-7]
     ref = oracle.cloud_stats(pos, vel, mass, species, 2)
     np.testing.assert_allclose(r["stats"][0], ref, rtol=1e-12, atol=1e-20)
-    assert np.array_equal(r["ions"][0], np.hstack([pos, vel])[::3])
+    ions = r["ions"][0]
+    assert np.array_equal(ions[:, :6], np.hstack([pos, vel])[::3])
+    assert np.array_equal(ions[:, 7], species[::3])
+    e = mass * (vel ** 2).sum(1) * 0.5 * 6.24150e18  # PrintParticle's energy
+    np.testing.assert_allclose(ions[:, 6], e[::3], rtol=1e-13)
     assert b.records(0)["t"].size == 0  # consumed
 
 
@@ -81,7 +85,7 @@ def test_print_rule_and_states(ctx):
         cx.close()
     assert rec["t"].tolist() == exp_t
     for got, exp in zip(rec["ions"], exp_y):
-        assert np.array_equal(got, exp)
+        assert np.array_equal(got[:, :6], exp)
 
 
 def test_ring_full_holds_then_resumes(ctx):
