@@ -190,3 +190,78 @@ def step(cloud: IonCloud, odev: OdeVars) -> None:
 def GetTimeStep(odev: OdeVars) -> float:
     """bin/ode.cpp:496-498."""
     return odev.h
+
+
+@dataclasses.dataclass
+class Operation:
+    """operation, bin/operation.h:17-33: one step of the run's sequence."""
+    name: str = "normal"       # normal | tof | trap_ramp | dissociation | anything else
+    time: float = 1e-9         # duration (s)
+    print_time: float = 0.0
+    timestep: float = 0.0
+    dissociation_fraction: float = 1.0
+    dissociation_reactant: int = 0   # species index (the reference uses ion names)
+    dissociation_product: int = 0
+    product_mass: float = 0.0        # kg
+
+
+class Operations:
+    """operations, bin/operation.h:35-44: add(), total_time(), launch().  launch runs
+    the whole sequence on the device (sg_batch_set_operations): the trap switches, the
+    trap ramp to trap_param.newVrf/newVdc and the TOF kick trap_param.E_kick are the
+    reference's, taken from odev.forcev as its INI parser leaves them."""
+
+    _KINDS = {"normal": abi.SG_OP_NORMAL, "tof": abi.SG_OP_TOF,
+              "trap_ramp": abi.SG_OP_TRAP_RAMP, "dissociation": abi.SG_OP_DISSOCIATION}
+
+    def __init__(self):
+        self.ops: list[Operation] = []
+
+    def add(self, op: Operation) -> None:
+        self.ops.append(op)
+
+    def total_time(self) -> float:
+        return float(sum(op.time for op in self.ops))
+
+    def launch(self, cloud: IonCloud, odev: OdeVars, print_after_operation: bool = False,
+               recorder=None):
+        """Runs every operation; cloud.pos/vel/lifetime are updated.  recorder, if given,
+        is (print_interval, stride, capacity) for the device recorder; the batch is
+        returned so that its records can be read."""
+        if not self.ops:
+            raise RuntimeError("No operation loaded")
+        fv = odev.forcev
+        trap0 = fv.trap
+        fv.trap = True  # the trap terms the operations switch
+        fp = fv.field_params()
+        fv.trap = trap0
+        tp = fv.trap_param
+        seq = []
+        for o in self.ops:
+            kind = self._KINDS.get(o.name, abi.SG_OP_FREE)
+            q = abi.Operation()
+            q.kind, q.print_after = kind, int(print_after_operation)
+            q.duration, q.print_time, q.timestep = o.time, o.print_time, o.timestep
+            q.new_vrf, q.new_vdc, q.e_kick = tp.newVrf, tp.newVdc, tp.E_kick
+            q.reactant, q.product = o.dissociation_reactant, o.dissociation_product
+            q.fraction, q.product_mass = o.dissociation_fraction, o.product_mass
+            seq.append(q)
+        op = OdeParams()
+        op.rtol, op.atol, op.h0 = odev.rk_rtol, odev.rk_atol, odev.h
+        op.t0, op.t_end = cloud.lifetime, float("inf")
+        op.adaptive, op.max_rejects, op.method = int(odev.change_stepsize), 0, odev.method
+        b = Batch(odev.context(), [cloud.nrparticles], [fp], [op], odev.precision)
+        b.upload(cloud.pos, cloud.vel, cloud.mass, cloud.charge)
+        if recorder is not None:
+            b.set_recorder(*recorder)
+        b.set_operations(seq)
+        info, st = b.run(raise_on_error=False)
+        if st == abi.SG_H_UNDERFLOW:
+            raise RuntimeError("stepsize underflow created")
+        abi.check(st, "operations")
+        cloud.pos, cloud.vel = b.download()
+        cloud.pos2, cloud.vel2 = cloud.pos.copy(), cloud.vel.copy()
+        cloud.lifetime = info[0]["t"]
+        odev.h = odev.hnext = info[0]["h"]
+        odev._batch = None  # the next step() starts from the new state
+        return b

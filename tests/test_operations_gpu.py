@@ -109,3 +109,26 @@ def test_dissociation(ctx):
     e = np.where(exp == 2, pm, mass) * (v ** 2).sum(1) * 0.5 * 6.24150e18
     np.testing.assert_allclose(r["ions"][1][:, 6], e, rtol=1e-13)
     assert r["stats"][1][2][7] == (exp == 2).sum()
+
+
+def test_reference_mirror_operations():
+    """The same sequence through the reference-shaped Python mirror (operation /
+    operations with trap_param.newVrf/newVdc/E_kick as the INI parser leaves them)."""
+    from simbuca_gb300 import ode
+    g = np.load(os.path.join(GOLD, "ops_sequence.npz"))
+    cloud = ode.IonCloud(g["pos0"], g["vel0"], g["mass"], g["charge"])
+    odev = ode.OdeVars(precision=SG_PREC_FP64)
+    odev.Init_ode(5, float(g["h0"]), False)
+    fv = odev.forcev
+    fv.coulomb_interaction, fv.coulomb_scale = True, 1.0
+    tp = fv.trap_param
+    tp.Vrf, tp.Vdc, tp.kappa, tp.r0, tp.z0, tp.freq_rf, tp.E_kick = [float(x) for x in TRAPP]
+    tp.newVrf, tp.newVdc, tp.E_kick = 80.0, 2.0, 50.0
+    ops = ode.Operations()
+    for name, d in zip(["normal", "trap_ramp", "tof", "nop", "normal"], g["durations"]):
+        ops.add(ode.Operation(name=name, time=float(d)))
+    assert ops.total_time() == pytest.approx(1.7e-7)
+    ops.launch(cloud, odev)
+    assert cloud.lifetime == g["t"][0]
+    ep = np.abs(cloud.pos - g["pos"]).max() / np.abs(g["pos"]).max()
+    assert ep <= 1e-11, ep
