@@ -199,6 +199,7 @@ def run_ours(args, dist: Dist):
     s_before = info0()
 
     # ---- device-resident timed region -------------------------------------
+    ctx.fixup_count()  # reset the FP32c conditioning fix-up counter
     ctx.set_kernel_timing(True)
     clocks = ClockSampler(dist.local)
     dist.barrier()
@@ -217,6 +218,7 @@ def run_ours(args, dist: Dist):
     s_after = info0()
     kt = ctx.kernel_timing()
     ctx.set_kernel_timing(False)
+    fixups = ctx.fixup_count()
     total_ms = sum(step_ms)
     sim_us = sum(a["t"] - b["t"] for a, b in zip(s_after, s_before)) * 1e6
     attempts = sum((a["steps"] + a["rejects"]) - (b["steps"] + b["rejects"])
@@ -295,6 +297,7 @@ def run_ours(args, dist: Dist):
                 max(1, sum(a["steps"] - b["steps"] for a, b in zip(e_after, e_before)))},
         "mean_h": sim_us * 1e-6 / max(1, sum(a["steps"] - b["steps"] for a, b in zip(s_after, s_before))),
         "gpu_launches": int(attempts * 21),
+        "fixup_ions_per_coulomb_call": fixups / max(1, kt["coulomb_launches"]),
         "attempts": int(attempts),
         "interactions_per_s": kt["interactions"] / (kt["coulomb_ms"] * 1e-3) if kt["coulomb_ms"] else None,
         "roofline": {"bound": "fp32" if prec == abi.SG_PREC_FP32C else "fp64",

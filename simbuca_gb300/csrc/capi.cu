@@ -223,7 +223,7 @@ void plan(Problem& P, int n_sm) {
     P.npad = poff;
     P.ntiles = tiles;
     P.n_rows = (int)P.hrows.size();
-    P.sorted = P.precision == SG_PREC_FP32C && P.variant == SG_C32_SORTED;
+    P.sorted = P.precision == SG_PREC_FP32C && sg_variant_sorted(P.variant);
 
     const bool f32 = P.precision == SG_PREC_FP32C;
     const int ib = f32 ? sg_coulomb_fp32c_ib(P.variant) : SG_C64_IB;
@@ -246,7 +246,7 @@ void plan(Problem& P, int n_sm) {
     if (items > 0 && items < target) {
         const int f = (int)std::ceil(target / (double)items);
         for (int c = 0; c < C; c++)
-            if (S[c] > 0) S[c] = std::min(S[c] * f, std::max(1, P.hc[c].npad / 256));
+            if (S[c] > 0) S[c] = std::min(S[c] * f, std::max(1, P.hc[c].npad / 128));
     }
     P.max_slots = 0;
     for (int c = 0; c < C; c++) {

@@ -496,8 +496,8 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
     }
 }
 
-template <int NT, int IPT>
-__global__ void __launch_bounds__(NT, 4) coulomb_fp32c_sorted_kernel(const float* __restrict__ c32,
+template <int NT, int IPT, int MINB, int STAGES>
+__global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const float* __restrict__ c32,
                                                             const double* __restrict__ c64,
                                                             const SgWorkItem* __restrict__ items,
                                                             const SgCloud* __restrict__ clouds,
@@ -506,8 +506,8 @@ __global__ void __launch_bounds__(NT, 4) coulomb_fp32c_sorted_kernel(const float
                                                             int npad_total, int* errword,
                                                             const float* __restrict__ bbox) {
     constexpr int T = SG_TILE;
-    __shared__ __align__(128) float tile[SG_STAGES][7][T];
-    __shared__ __align__(8) uint64_t full[SG_STAGES];
+    __shared__ __align__(128) float tile[STAGES][7][T];
+    __shared__ __align__(8) uint64_t full[STAGES];
     __shared__ double corr[3][NT * IPT];
 
     const SgWorkItem it = items[blockIdx.x];
@@ -553,13 +553,13 @@ __global__ void __launch_bounds__(NT, 4) coulomb_fp32c_sorted_kernel(const float
     const int ntiles = (it.nj + T - 1) / T;
     bool ok = true;
     if (tid == 0) {
-        for (int s = 0; s < SG_STAGES; s++) mbar_init(&full[s], 1);
+        for (int s = 0; s < STAGES; s++) mbar_init(&full[s], 1);
         fence_mbar_init();
     }
     __syncthreads();
     // prologue: fill the ring
     if (tid == 0) {
-        for (int s = 0; s < SG_STAGES && s < ntiles; s++) {
+        for (int s = 0; s < STAGES && s < ntiles; s++) {
             const int j0 = it.j0 + s * T;
             const int len = min(T, it.j0 + it.nj - j0);
             const uint32_t bytes = (uint32_t)len * 4u;
@@ -583,8 +583,8 @@ __global__ void __launch_bounds__(NT, 4) coulomb_fp32c_sorted_kernel(const float
     // still estimate sum_j |f_ij|^2 when the whole cloud is one or two tiles.
     const int flush_len = (cl.npad <= 2048) ? 16 : SG_TILE;
     for (int t = 0; t < ntiles; t++) {
-        const int s = t % SG_STAGES;
-        const uint32_t parity = (uint32_t)((t / SG_STAGES) & 1);
+        const int s = t % STAGES;
+        const uint32_t parity = (uint32_t)((t / STAGES) & 1);
         const int j0 = it.j0 + t * T;
         const int len = min(T, it.j0 + it.nj - j0);
         const bool arrived = mbar_wait(&full[s], parity);
@@ -593,8 +593,8 @@ __global__ void __launch_bounds__(NT, 4) coulomb_fp32c_sorted_kernel(const float
             if (tid == 0) {
                 atomicExch(errword, SG_TIMEOUT);
                 // drain the copies still in flight (tiles t .. t+STAGES-1), bounded
-                for (int u = t; u < ntiles && u < t + SG_STAGES; u++)
-                    (void)mbar_wait(&full[u % SG_STAGES], (uint32_t)((u / SG_STAGES) & 1));
+                for (int u = t; u < ntiles && u < t + STAGES; u++)
+                    (void)mbar_wait(&full[u % STAGES], (uint32_t)((u / STAGES) & 1));
             }
             __syncthreads();
             break;
@@ -680,9 +680,9 @@ __global__ void __launch_bounds__(NT, 4) coulomb_fp32c_sorted_kernel(const float
             }
         }
         __syncthreads();  // every thread is done with ring slot s
-        if (tid == 0 && t + SG_STAGES < ntiles) {
+        if (tid == 0 && t + STAGES < ntiles) {
             fence_proxy_async();
-            const int jn = it.j0 + (t + SG_STAGES) * T;
+            const int jn = it.j0 + (t + STAGES) * T;
             const int ln = min(T, it.j0 + it.nj - jn);
             const uint32_t bytes = (uint32_t)ln * 4u;
             mbar_arrive_tx(&full[s], 7u * bytes);
@@ -902,7 +902,7 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
 // Launch shapes of the FP32c kernel (threads per block, ions per thread); the work
 // planner sizes i-blocks as threads x ions.  Variant 0 is the default.
 static const int kC32Shapes[SG_C32_VARIANTS][2] = {{128, 4}, {128, 2}, {256, 2}, {64, 4},
-                                                   {128, 4}};
+                                                   {128, 4}, {64, 2}, {32, 4}, {32, 4}};
 
 int sg_coulomb_fp32c_ib(int variant) {
     if (variant < 0 || variant >= SG_C32_VARIANTS) variant = 0;
@@ -924,8 +924,21 @@ cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s) {
             coulomb_fp32c_kernel<64, 4><<<a.n_items, 64, 0, s>>>(
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
             break;
+        case 5:
+            coulomb_fp32c_kernel<64, 2><<<a.n_items, 64, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
+            break;
+        case 6:
+            coulomb_fp32c_kernel<32, 4><<<a.n_items, 32, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
+            break;
         case SG_C32_SORTED:
-            coulomb_fp32c_sorted_kernel<128, 4><<<a.n_items, 128, 0, s>>>(
+            coulomb_fp32c_sorted_kernel<128, 4, 4, SG_STAGES><<<a.n_items, 128, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            break;
+        case SG_C32_SORTED_LEAF:
+            // one k-d leaf per block: warps never wait for a slower (near) neighbour
+            coulomb_fp32c_sorted_kernel<32, 4, 16, 3><<<a.n_items, 32, 0, s>>>(
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         default:
@@ -949,7 +962,7 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
     if (fp32c)
         coulomb_reduce_kernel<true><<<n_rows, SG_ROWS, 0, s>>>(
             rows, a.clouds, a.ctrl, a.part, a.c32, a.c64, a.npad_total, out, n_total, counters,
-            a.variant == SG_C32_SORTED ? a.bbox : nullptr);
+            sg_variant_sorted(a.variant) ? a.bbox : nullptr);
     else
         coulomb_reduce_kernel<false><<<n_rows, SG_ROWS, 0, s>>>(
             rows, a.clouds, a.ctrl, a.part, a.c32, a.c64, a.npad_total, out, n_total, counters,

@@ -121,3 +121,21 @@ def test_sorted_variant(ctx, n):
         ctx.set_coulomb_variant(-1)
     e = rel_err_per_ion(a, ref)
     assert e.max() <= 1e-6, summary(e)
+
+
+@pytest.mark.parametrize("variant", list(range(8)))
+@pytest.mark.parametrize("n", [33, 1000, 3000])
+def test_every_launch_shape(ctx, variant, n):
+    """Every FP32c launch shape (sg_set_coulomb_variant) on small and mid-size clouds."""
+    rng = np.random.default_rng(7 * n + variant)
+    pos = rng.normal(0, 5e-4, (n, 3))
+    q = np.ones(n)
+    kq = kq_of(np.full(n, 132.905 * oracle.AMU), q)
+    ref = oracle.coulomb_kq(pos, q, kq)
+    ctx.set_coulomb_variant(variant)
+    try:
+        a = ctx.coulomb_accel(pos, q, kq, SG_PREC_FP32C)
+    finally:
+        ctx.set_coulomb_variant(-1)
+    e = rel_err_per_ion(a, ref)
+    assert e.max() <= 1e-6, (variant, n, summary(e))
