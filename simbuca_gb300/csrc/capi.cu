@@ -781,14 +781,14 @@ void ion_constants(const Problem& P, const double* mass, const int* charge,
     }
 }
 
-// Uploads positions/velocities (AoS host) into y and rebuilds the Coulomb inputs.
 // Uploads positions/velocities (AoS host, caller's order) into y -- in k-d tree order for
 // the sorted kernel -- brings the per-ion constants into the same order and rebuilds the
 // Coulomb inputs.  The constants in the caller's order (kq0, qm0, qd0, mass0) must be on
 // the device already.
-int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel) {
+int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel,
+                 bool resort = true) {
     const size_t N = (size_t)P.n;
-    if (P.sorted) {
+    if (P.sorted && resort) {
         for (int c = 0; c < P.n_clouds; c++)
             kd_order(pos, P.hc[c].off, P.hc[c].n, P.perm.data() + P.hc[c].off);
         CK(cudaMemcpyAsync(P.dperm, P.perm.data(), sizeof(int) * N, cudaMemcpyHostToDevice,
@@ -1129,7 +1129,9 @@ int sg_batch_set_state(sg_ctx* ctx, const double* pos, const double* vel) {
     CK(cudaSetDevice(ctx->device));
     // field parameters as the device has them now (a ramp may have moved them)
     CK(pull_clouds(ctx, P));
-    int st = upload_state(ctx, P, pos, vel);
+    // a continuing run keeps its ion order: the tile bounds are recomputed from the new
+    // positions at every stage, so an older k-d order costs some far pairs, never accuracy
+    int st = upload_state(ctx, P, pos, vel, false);
     if (st != SG_OK) return st;
     st = launch_coulomb(ctx, P, true, active_interactions(P), P.coul1);
     if (st != SG_OK) return st;

@@ -643,8 +643,11 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
                 kahan_add(ks[k][0], kc[k][0], tx_);
                 kahan_add(ks[k][1], kc[k][1], ty_);
                 kahan_add(ks[k][2], kc[k][2], tz_);
-                // sum of squared partial sums: estimates sum_j |f_ij|^2 (conditioning test)
-                s2[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2[k])));
+                // sum of squared partial sums of the near tiles, where the pairs that the
+                // reduction's FP64 fix-up re-evaluates live; far tiles hold no such pair, and
+                // in k-d order their coherent tile sums would flag ions for nothing
+                if (!far)
+                    s2[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2[k])));
             }
         }
         // close pairs of this tile, one flagged ion at a time by the whole warp

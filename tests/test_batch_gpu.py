@@ -132,3 +132,35 @@ def test_sorted_order_round_trip(ctx):
         ctx.set_coulomb_variant(-1)
     ep, ev = replay_error(c, fp, np.array(ts), np.array(hs), p, v)
     assert ep <= 1e-9 and ev <= 1e-9, (ep, ev)
+
+
+@pytest.mark.parametrize("variant", [4, 7])
+def test_sorted_set_state_keeps_order(ctx, variant):
+    """set_state on a k-d ordered batch keeps the ion order (only the tile bounds move):
+    the caller's order comes back and the next steps still match the oracle."""
+    w = configs.penning_1k(n=4000, seed=22)
+    c = w.clouds[0]
+    fp = configs.penning_field(delta=1e3)
+    ctx.set_coulomb_variant(variant)
+    try:
+        b = Batch(ctx, [4000], [fp], [configs.ode(1e-9, 1e-15, 1e-9, 1.0)], SG_PREC_FP32C)
+        b.upload(c.pos, c.vel, c.mass, c.charge)
+        rng = np.random.default_rng(5)
+        p1 = c.pos + rng.normal(0, 2e-5, c.pos.shape)  # every ion moved
+        v1 = c.vel * 0.9
+        b.set_state(p1, v1)
+        p, v = b.download()
+        assert np.array_equal(p, p1) and np.array_equal(v, v1)
+        t0 = b.info()[0]["t"]
+        ts, hs = [], []
+        for _ in range(4):
+            i0 = b.info()[0]
+            info, _ = b.step()
+            ts.append(i0["t"])
+            hs.append(info[0]["h_last"])
+        p, v = b.download()
+    finally:
+        ctx.set_coulomb_variant(-1)
+    from simbuca_gb300.configs import Cloud
+    ep, ev = replay_error(Cloud(p1, v1, c.mass, c.charge), fp, np.array(ts), np.array(hs), p, v)
+    assert ep <= 1e-9 and ev <= 1e-9, (ep, ev)
