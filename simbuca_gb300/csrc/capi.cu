@@ -172,15 +172,18 @@ void free_problem(Problem& P) {
 inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
 // Launch shape for a set of clouds when the context has no explicit choice: the
-// cloud carrying the most pair work decides.  Measured on GB300 (simbuca_gb300/tune.py):
-// 128 threads x 2 ions is fastest up to a few thousand ions per cloud (more blocks,
-// less padding of small i-ranges); from ~16k ions on the ions are put in k-d tree order
-// and far tile pairs take the high parts only.
+// cloud carrying the most pair work decides.  Measured on GB300 (simbuca_gb300/tune.py,
+// Coulomb kernel time per call): 128 x 2 for a few hundred ions; 64 x 2 from ~1k to
+// ~16k ions (0.032 ms at 1,024, 0.18 ms at 16,384); from tens of thousands of ions the
+// k-d ordered form with one leaf per block, whose far tile pairs take the high parts
+// only (1.93 ms vs 2.51 ms for the best plain shape at 65,536; 27.7 vs 40.5 ms at
+// 262,144).
 int auto_variant(const std::vector<int>& counts, int requested) {
     if (requested >= 0) return requested;
     int big = 0;
     for (int n : counts) big = std::max(big, n);
-    return big <= 8192 ? 1 : SG_C32_SORTED;
+    if (big <= 512) return 1;
+    return big < 40000 ? 5 : SG_C32_SORTED_LEAF;
 }
 
 // Partition clouds into row blocks and Coulomb work items.  Items are sized so that

@@ -147,6 +147,15 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 }
 
 
+__device__ __forceinline__ double rsqrt_fp64(double r2) {
+    // FP32 SFU seed, then y = y0 (1 + e/2 + 3 e^2/8), e = 1 - r2 y0^2 (binomial series of
+    // (1-e)^(-1/2)); the truncation error is ~(5/16) e^3 with |e| < 2^-22.
+    const double y0 = (double)rsqrt_approx(__double2float_rn(r2));
+    const double e = fma(-r2 * y0, y0, 1.0);
+    const double p = fma(e, 0.375, 0.5);
+    return fma(y0 * e, p, y0);
+}
+
 // Close pairs of one flagged ion against one shared-memory tile, evaluated by the
 // whole warp (lanes stride over the tile): pairs whose FP32 1/r^3 exceeded wc get their
 // exact FP64 term, minus the capped FP32 term the main loop already summed (a product
@@ -170,7 +179,7 @@ __device__ __forceinline__ void close_pairs_warp(const float (*tl)[SG_TILE], int
             const double ry = yi - c64[npad_total + jg];
             const double rz = zi - c64[2 * (size_t)npad_total + jg];
             const double r2d = rx * rx + ry * ry + rz * rz;
-            const double inv = 1.0 / sqrt(r2d);
+            const double inv = rsqrt_fp64(r2d);
             const double wq = c64[3 * (size_t)npad_total + jg] * inv * inv * inv;
             cx += wq * rx + invL2 * ((double)wf * (double)p.dx);
             cy += wq * ry + invL2 * ((double)wf * (double)p.dy);
@@ -579,9 +588,10 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         for (int q = 0; q < 6; q++) wbox[q] = bbox[8 * (size_t)wt + q];
     }
     const float dfar2 = cl.dfar * cl.dfar;
-    // Small clouds fold partial sums every 16 j-ions so that the squared partial sums
-    // still estimate sum_j |f_ij|^2 when the whole cloud is one or two tiles.
-    const int flush_len = (cl.npad <= 2048) ? 16 : SG_TILE;
+    // Partial sums are folded into the compensated accumulators every 32 j-ions (16 for
+    // small clouds): in k-d order the terms of a tile point the same way, and a 128-term
+    // FP32 running sum would carry 4x the rounding error of the summands.
+    const int flush_len = (cl.npad <= 2048) ? 16 : 32;
     for (int t = 0; t < ntiles; t++) {
         const int s = t % STAGES;
         const uint32_t parity = (uint32_t)((t / STAGES) & 1);
@@ -712,14 +722,6 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
 // ---------------------------------------------------------------------------
 // FP64 kernel (plain form).  c64 = 4 double arrays (x, y, z, q) in SI units.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double rsqrt_fp64(double r2) {
-    // FP32 SFU seed, then y = y0 (1 + e/2 + 3 e^2/8), e = 1 - r2 y0^2 (binomial series of
-    // (1-e)^(-1/2)); the truncation error is ~(5/16) e^3 with |e| < 2^-22.
-    const double y0 = (double)rsqrt_approx(__double2float_rn(r2));
-    const double e = fma(-r2 * y0, y0, 1.0);
-    const double p = fma(e, 0.375, 0.5);
-    return fma(y0 * e, p, y0);
-}
 
 template <int NT, int IPT>
 __global__ void __launch_bounds__(NT) coulomb_fp64_kernel(const double* __restrict__ c64,
@@ -808,6 +810,7 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     __shared__ int list[SG_ROWS];
     __shared__ int nl;
     __shared__ double cx[SG_ROWS], cy[SG_ROWS], cz[SG_ROWS], pm[SG_ROWS];
+    __shared__ double wsum[SG_ROWS / 32][3];
     const SgRowBlock rb = rows[blockIdx.x];
     if (ctrl != nullptr &&
         (ctrl[rb.cloud].done || ctrl[rb.cloud].hold || ctrl[rb.cloud].status != SG_OK))
@@ -840,16 +843,18 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
         const int warp = li >> 5, lane = li & 31;
         const double invL2 = cl.invL * cl.invL;
         const float wc = cl.wc;
-        for (int k = warp; k < nl; k += SG_ROWS / 32) {
+        // flagged ions one at a time, the whole block striding over the cloud's j-ions
+        for (int k = 0; k < nl; k++) {
             const int lk = list[k];
             const int igk = cl.poff + (rb.i0 + lk - cl.off);
-            const float thr3 = (float)pow(0.1 * pm[lk], 1.5);
+            const double tq = 0.1 * pm[lk];
+            const float thr3 = (float)(tq * sqrt(tq));  // (|P|/10)^(3/2): |f_ij| > |P|/10
             const float xih = c32[igk], yih = c32[NP + igk], zih = c32[2 * NP + igk];
             const float xil = c32[4 * NP + igk], yil = c32[5 * NP + igk], zil = c32[6 * NP + igk];
             const double xi = c64[igk], yi = c64[NP + igk], zi = c64[2 * NP + igk];
             double ax = 0.0, ay = 0.0, az = 0.0;
             const float* ibox = bbox ? bbox + 8 * (size_t)(cl.tile0 + (igk - cl.poff) / 128) : nullptr;
-            for (int j = lane; j < cl.npad; j += 32) {
+            for (int j = li; j < cl.npad; j += SG_ROWS) {
                 const int jg = cl.poff + j;
                 PairF p = pair_f32(c32[jg], c32[NP + jg], c32[2 * NP + jg], c32[4 * NP + jg],
                                    c32[5 * NP + jg], c32[6 * NP + jg], xih, yih, zih, xil, yil,
@@ -869,7 +874,7 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
                 if (p.y3 > thr3 && p.y3 <= wc && jg != igk) {
                     const float wf = __fmul_rn(c32[3 * NP + jg], p.y3);
                     const double rx = xi - c64[jg], ry = yi - c64[NP + jg], rz = zi - c64[2 * NP + jg];
-                    const double inv = 1.0 / sqrt(rx * rx + ry * ry + rz * rz);
+                    const double inv = rsqrt_fp64(rx * rx + ry * ry + rz * rz);
                     const double wq = c64[3 * NP + jg] * inv * inv * inv;
                     ax += wq * rx + invL2 * ((double)wf * (double)p.dx);
                     ay += wq * ry + invL2 * ((double)wf * (double)p.dy);
@@ -882,10 +887,23 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
                 az += __shfl_down_sync(0xffffffffu, az, o);
             }
             if (lane == 0) {
-                cx[lk] = ax;
-                cy[lk] = ay;
-                cz[lk] = az;
+                wsum[warp][0] = ax;
+                wsum[warp][1] = ay;
+                wsum[warp][2] = az;
             }
+            __syncthreads();
+            if (li == 0) {
+                double sx = 0.0, sy = 0.0, sz = 0.0;
+                for (int w = 0; w < SG_ROWS / 32; w++) {
+                    sx += wsum[w][0];
+                    sy += wsum[w][1];
+                    sz += wsum[w][2];
+                }
+                cx[lk] = sx;
+                cy[lk] = sy;
+                cz[lk] = sz;
+            }
+            __syncthreads();
         }
         __syncthreads();
         if (li == 0 && nl > 0 && counters != nullptr) atomicAdd(counters, nl);

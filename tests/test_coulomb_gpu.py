@@ -103,8 +103,9 @@ def test_bad_arguments(ctx):
     assert L.sg_coulomb_accel(ctx.handle, 0, -1, None, None, None, None) == abi.SG_BAD_ARG
 
 
+@pytest.mark.parametrize("variant", [4, 7])
 @pytest.mark.parametrize("n", [100, 1000, 5000, 20000])
-def test_sorted_variant(ctx, n):
+def test_sorted_variant(ctx, n, variant):
     """Ions in k-d tree order, far tile pairs from the high parts only: same accuracy,
     results returned in the caller's order."""
     rng = np.random.default_rng(100 + n)
@@ -114,7 +115,7 @@ def test_sorted_variant(ctx, n):
     kq = kq_of(np.full(n, 132.905 * oracle.AMU), q)
     rows = np.unique(rng.choice(n, min(n, 600), replace=False))
     ref = np.stack([oracle.coulomb_kq_rows(pos, q, kq, int(i), int(i) + 1)[0] for i in rows])
-    ctx.set_coulomb_variant(4)
+    ctx.set_coulomb_variant(variant)
     try:
         a = ctx.coulomb_accel(pos, q, kq, SG_PREC_FP32C)[rows]
     finally:
