@@ -800,6 +800,9 @@ __global__ void __launch_bounds__(NT) coulomb_fp64_kernel(const double* __restri
 // ---------------------------------------------------------------------------
 constexpr double kKappa2 = 2.25;
 
+// tiles listed for the fix-up scan of one ion in k-d order
+constexpr int kNearCap = 1024;
+
 template <bool F32>
 __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     const SgRowBlock* __restrict__ rows, const SgCloud* __restrict__ clouds,
@@ -811,6 +814,8 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     __shared__ int nl;
     __shared__ double cx[SG_ROWS], cy[SG_ROWS], cz[SG_ROWS], pm[SG_ROWS];
     __shared__ double wsum[SG_ROWS / 32][3];
+    __shared__ int wcnt[SG_ROWS / 32];
+    __shared__ int near_tiles[kNearCap];
     const SgRowBlock rb = rows[blockIdx.x];
     if (ctrl != nullptr &&
         (ctrl[rb.cloud].done || ctrl[rb.cloud].hold || ctrl[rb.cloud].status != SG_OK))
@@ -854,12 +859,43 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
             const double xi = c64[igk], yi = c64[NP + igk], zi = c64[2 * NP + igk];
             double ax = 0.0, ay = 0.0, az = 0.0;
             const float* ibox = bbox ? bbox + 8 * (size_t)(cl.tile0 + (igk - cl.poff) / 128) : nullptr;
-            for (int j = li; j < cl.npad; j += SG_ROWS) {
+            // k-d ordered clouds: scan only the tiles near the ion's own tile, listed in
+            // order by a block-wide ballot (far tiles were summed from the high parts and
+            // are left as they are); the whole cloud if the list would overflow
+            int n_near = 0;
+            if (ibox != nullptr) {
+                const int nt = (cl.npad + 127) / 128, itile = (igk - cl.poff) / 128;
+                const float dfar2 = cl.dfar * cl.dfar;
+                for (int t0 = 0; t0 < nt; t0 += SG_ROWS) {
+                    const int t = t0 + li;
+                    const bool nr = t < nt && (t == itile ||
+                                               box_dist2(ibox, bbox + 8 * (size_t)(cl.tile0 + t)) <= dfar2);
+                    const unsigned m = __ballot_sync(0xffffffffu, nr);
+                    if (lane == 0) wcnt[warp] = __popc(m);
+                    __syncthreads();
+                    int off = n_near, tot = 0;
+                    for (int w = 0; w < SG_ROWS / 32; w++) {
+                        if (w < warp) off += wcnt[w];
+                        tot += wcnt[w];
+                    }
+                    if (nr) {
+                        const int at = off + __popc(m & ((1u << lane) - 1u));
+                        if (at < kNearCap) near_tiles[at] = t;
+                    }
+                    __syncthreads();
+                    n_near += tot;
+                }
+            }
+            const bool listed = ibox != nullptr && n_near <= kNearCap;
+            const int n_scan = listed ? n_near * 128 : cl.npad;
+            for (int qj = li; qj < n_scan; qj += SG_ROWS) {
+                const int j = listed ? near_tiles[qj >> 7] * 128 + (qj & 127) : qj;
+                if (j >= cl.npad) continue;
                 const int jg = cl.poff + j;
                 PairF p = pair_f32(c32[jg], c32[NP + jg], c32[2 * NP + jg], c32[4 * NP + jg],
                                    c32[5 * NP + jg], c32[6 * NP + jg], xih, yih, zih, xil, yil,
                                    zil);
-                if (ibox != nullptr) {
+                if (ibox != nullptr && !listed) {
                     // the sorted kernel summed this pair from the high parts if its tiles are far
                     const float* jbox = bbox + 8 * (size_t)(cl.tile0 + j / 128);
                     const bool same = (igk - cl.poff) / 128 == j / 128;
@@ -923,7 +959,8 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
 // Launch shapes of the FP32c kernel (threads per block, ions per thread); the work
 // planner sizes i-blocks as threads x ions.  Variant 0 is the default.
 static const int kC32Shapes[SG_C32_VARIANTS][2] = {{128, 4}, {128, 2}, {256, 2}, {64, 4},
-                                                   {128, 4}, {64, 2}, {32, 4}, {32, 4}};
+                                                   {128, 4}, {64, 2}, {32, 4}, {32, 4},
+                                                   {64, 2}, {128, 1}};
 
 int sg_coulomb_fp32c_ib(int variant) {
     if (variant < 0 || variant >= SG_C32_VARIANTS) variant = 0;
@@ -960,6 +997,15 @@ cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s) {
         case SG_C32_SORTED_LEAF:
             // one k-d leaf per block: warps never wait for a slower (near) neighbour
             coulomb_fp32c_sorted_kernel<32, 4, 16, 3><<<a.n_items, 32, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            break;
+        case 8:
+            // one leaf per block split over two warps (same far/near decisions)
+            coulomb_fp32c_sorted_kernel<64, 2, 12, 3><<<a.n_items, 64, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            break;
+        case 9:
+            coulomb_fp32c_sorted_kernel<128, 1, 8, 3><<<a.n_items, 128, 0, s>>>(
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         default:
