@@ -505,6 +505,30 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
     }
 }
 
+// Adds packed partial sums (two interleaved FP32 sums per ion and component) into the
+// compensated accumulators; with `near`, also their squares into the conditioning
+// estimate (near tiles hold the pairs the reduction's FP64 fix-up re-evaluates; in k-d
+// order the coherent sums of far tiles would flag ions for nothing).
+template <int IPT>
+__device__ __forceinline__ void fold_partials(const f2* ax, const f2* ay, const f2* az,
+                                              float (*ks)[3], float (*kc)[3], float* s2,
+                                              bool near) {
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        float a, b;
+        upk(ax[k], a, b);
+        const float tx_ = __fadd_rn(a, b);
+        upk(ay[k], a, b);
+        const float ty_ = __fadd_rn(a, b);
+        upk(az[k], a, b);
+        const float tz_ = __fadd_rn(a, b);
+        kahan_add(ks[k][0], kc[k][0], tx_);
+        kahan_add(ks[k][1], kc[k][1], ty_);
+        kahan_add(ks[k][2], kc[k][2], tz_);
+        if (near) s2[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2[k])));
+    }
+}
+
 template <int NT, int IPT, int MINB, int STAGES>
 __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const float* __restrict__ c32,
                                                             const double* __restrict__ c64,
@@ -588,9 +612,9 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         for (int q = 0; q < 6; q++) wbox[q] = bbox[8 * (size_t)wt + q];
     }
     const float dfar2 = cl.dfar * cl.dfar;
-    // Partial sums are folded into the compensated accumulators every 32 j-ions (16 for
-    // small clouds): in k-d order the terms of a tile point the same way, and a 128-term
-    // FP32 running sum would carry 4x the rounding error of the summands.
+    // FP32 running sums restart every 32 j-ions (16 for small clouds): in k-d order the
+    // terms of a tile point the same way, and a 128-term running sum would carry several
+    // times the rounding error of the summands.
     const int flush_len = (cl.npad <= 2048) ? 16 : 32;
     for (int t = 0; t < ntiles; t++) {
         const int s = t % STAGES;
@@ -627,6 +651,14 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         const int jt = cl.tile0 + (j0 - cl.poff) / 128;
         for (int q = 0; q < 6; q++) jbox[q] = bbox[8 * (size_t)jt + q];
         const bool far = !diag && box_dist2(wbox, jbox) > dfar2;  // uniform per warp
+        // Two-level sums with few ions per thread: FP32 partials of flush_len j-ions are
+        // added into a tile partial (packed), the tile partial into the compensated
+        // accumulators.  With 4 ions per thread the extra registers would spill, so each
+        // partial goes to the compensated accumulators directly.
+        constexpr bool kTwoLevel = IPT <= 2;
+        f2 tax[IPT], tay[IPT], taz[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) tax[k] = tay[k] = taz[k] = 0ull;
         for (int jb = 0; jb < len; jb += flush_len) {
             const int je = min(len, jb + flush_len);
             f2 ax[IPT], ay[IPT], az[IPT];
@@ -640,26 +672,18 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
             else
                 tile_pairs<IPT, true>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh, zh,
                                       xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
-            // fold the partial sums into the compensated accumulators
+            if (kTwoLevel) {
 #pragma unroll
-            for (int k = 0; k < IPT; k++) {
-                float a, b;
-                upk(ax[k], a, b);
-                const float tx_ = __fadd_rn(a, b);
-                upk(ay[k], a, b);
-                const float ty_ = __fadd_rn(a, b);
-                upk(az[k], a, b);
-                const float tz_ = __fadd_rn(a, b);
-                kahan_add(ks[k][0], kc[k][0], tx_);
-                kahan_add(ks[k][1], kc[k][1], ty_);
-                kahan_add(ks[k][2], kc[k][2], tz_);
-                // sum of squared partial sums of the near tiles, where the pairs that the
-                // reduction's FP64 fix-up re-evaluates live; far tiles hold no such pair, and
-                // in k-d order their coherent tile sums would flag ions for nothing
-                if (!far)
-                    s2[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2[k])));
+                for (int k = 0; k < IPT; k++) {
+                    tax[k] = add2(tax[k], ax[k]);
+                    tay[k] = add2(tay[k], ay[k]);
+                    taz[k] = add2(taz[k], az[k]);
+                }
+            } else {
+                fold_partials<IPT>(ax, ay, az, ks, kc, s2, !far);
             }
         }
+        if (kTwoLevel) fold_partials<IPT>(tax, tay, taz, ks, kc, s2, !far);
         // close pairs of this tile, one flagged ion at a time by the whole warp
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
