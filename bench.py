@@ -162,6 +162,13 @@ def l2_flush():
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
+def coulomb_kernel_name(prec, variant):
+    from simbuca_gb300 import abi
+    if prec != abi.SG_PREC_FP32C:
+        return "coulomb_fp64_kernel"
+    return "coulomb_fp32c_sorted_kernel" if variant in (4, 7, 8, 9) else "coulomb_fp32c_kernel"
+
+
 def run_ours(args, dist: Dist):
     import torch
     from simbuca_gb300 import abi, configs
@@ -264,9 +271,11 @@ def run_ours(args, dist: Dist):
     if os.path.exists(tpath):
         try:
             tj = json.load(open(tpath))
-            key = f"{args.workload}:{args.precision}"
-            if key in tj:
-                traffic = tj[key]["dram_bytes_per_launch"]
+            for key in (f"{args.workload}:{args.precision}:{batch.variant()}",
+                        f"{args.workload}:{args.precision}"):
+                if key in tj:
+                    traffic = tj[key]["dram_bytes_per_launch"]
+                    break
         except (ValueError, KeyError):
             traffic = None
 
@@ -303,7 +312,7 @@ def run_ours(args, dist: Dist):
         "roofline": {"bound": "fp32" if prec == abi.SG_PREC_FP32C else "fp64",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
-                     "kernel": "coulomb_fp32c_kernel" if prec == abi.SG_PREC_FP32C else "coulomb_fp64_kernel",
+                     "kernel": coulomb_kernel_name(prec, batch.variant()),
                      "flops_per_interaction": FLOPS_PER_INTERACTION,
                      "peak_source": "measured in-run by FMA issue probes (sg_probe_peaks)",
                      "coulomb_share_of_step": kt["coulomb_ms"] / total_ms if total_ms else None},
