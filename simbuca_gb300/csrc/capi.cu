@@ -176,15 +176,15 @@ inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 // Coulomb kernel time per call): 128 x 2 for a few hundred ions; 64 x 2 from ~1k to
 // ~16k ions (0.032 ms at 1,024, 0.18 ms at 16,384); above that the k-d ordered forms
 // with one 128-ion leaf per block, whose far tile pairs take the high parts only: the
-// leaf over four warps up to ~100k ions (0.53 vs 0.67 ms at 32,768; 1.91 vs 2.54 ms at
-// 65,536), one warp per leaf beyond (28.8 vs 41.7 ms at 262,144).
+// leaf over four warps up to ~100k ions (0.53 vs 0.67 ms at 32,768; 1.86 vs 2.54 ms at
+// 65,536), over two warps beyond (28.1 vs 41.7 ms at 262,144).
 int auto_variant(const std::vector<int>& counts, int requested) {
     if (requested >= 0) return requested;
     int big = 0;
     for (int n : counts) big = std::max(big, n);
     if (big <= 512) return 1;
     if (big < 24000) return 5;
-    return big < 131072 ? 9 : SG_C32_SORTED_LEAF;
+    return big < 131072 ? 9 : 8;
 }
 
 // Partition clouds into row blocks and Coulomb work items.  Items are sized so that

@@ -678,12 +678,23 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
                     tax[k] = add2(tax[k], ax[k]);
                     tay[k] = add2(tay[k], ay[k]);
                     taz[k] = add2(taz[k], az[k]);
+                    if (!far) {
+                        // conditioning estimate from the partial sums of near tiles
+                        float a, b;
+                        upk(ax[k], a, b);
+                        const float px = __fadd_rn(a, b);
+                        upk(ay[k], a, b);
+                        const float py = __fadd_rn(a, b);
+                        upk(az[k], a, b);
+                        const float pz = __fadd_rn(a, b);
+                        s2[k] = fmaf(px, px, fmaf(py, py, fmaf(pz, pz, s2[k])));
+                    }
                 }
             } else {
                 fold_partials<IPT>(ax, ay, az, ks, kc, s2, !far);
             }
         }
-        if (kTwoLevel) fold_partials<IPT>(tax, tay, taz, ks, kc, s2, !far);
+        if (kTwoLevel) fold_partials<IPT>(tax, tay, taz, ks, kc, s2, false);
         // close pairs of this tile, one flagged ion at a time by the whole warp
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
