@@ -200,6 +200,16 @@ void plan(Problem& P, int n_sm) {
     P.cloud_inter.assign(C, 0.0);
     int off = 0, poff = 0, tiles = 0;
     P.any_coulomb = false;
+    P.sorted = P.precision == SG_PREC_FP32C && sg_variant_sorted(P.variant);
+    // Row blocks of SG_ROWS ions, or fewer for small batches: the stage, control and
+    // reduction kernels are FP64 work, which GB300 runs at a small fraction of its FP32
+    // rate per SM, so a 1,000-ion cloud is spread over 32 SMs rather than 4.  The k-d
+    // ordered shapes keep full blocks (each covers two 128-ion tiles for the tile bounds).
+    long long total_ions = 0;
+    for (int c = 0; c < C; c++) total_ions += P.counts[c];
+    int rows = SG_ROWS;
+    if (!P.sorted)
+        while (rows > 32 && total_ions / rows < 2LL * n_sm) rows /= 2;
     for (int c = 0; c < C; c++) {
         SgCloud& cl = P.hc[c];
         memset(&cl, 0, sizeof cl);
@@ -211,11 +221,11 @@ void plan(Problem& P, int n_sm) {
         cl.tile0 = tiles;
         tiles += (cl.npad + 127) / 128;
         cl.rb0 = (int)P.hrows.size();
-        for (int i = 0; i < cl.n; i += SG_ROWS) {
+        for (int i = 0; i < cl.n; i += rows) {
             SgRowBlock rb;
             rb.cloud = c;
             rb.i0 = off + i;
-            rb.n = std::min(SG_ROWS, cl.n - i);
+            rb.n = std::min(rows, cl.n - i);
             rb.pad = 0;
             P.hrows.push_back(rb);
         }
@@ -227,7 +237,6 @@ void plan(Problem& P, int n_sm) {
     P.npad = poff;
     P.ntiles = tiles;
     P.n_rows = (int)P.hrows.size();
-    P.sorted = P.precision == SG_PREC_FP32C && sg_variant_sorted(P.variant);
 
     const bool f32 = P.precision == SG_PREC_FP32C;
     const int ib = f32 ? sg_coulomb_fp32c_ib(P.variant) : SG_C64_IB;

@@ -651,14 +651,9 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         const int jt = cl.tile0 + (j0 - cl.poff) / 128;
         for (int q = 0; q < 6; q++) jbox[q] = bbox[8 * (size_t)jt + q];
         const bool far = !diag && box_dist2(wbox, jbox) > dfar2;  // uniform per warp
-        // Two-level sums with few ions per thread: FP32 partials of flush_len j-ions are
-        // added into a tile partial (packed), the tile partial into the compensated
-        // accumulators.  With 4 ions per thread the extra registers would spill, so each
-        // partial goes to the compensated accumulators directly.
-        constexpr bool kTwoLevel = IPT <= 2;
-        f2 tax[IPT], tay[IPT], taz[IPT];
-#pragma unroll
-        for (int k = 0; k < IPT; k++) tax[k] = tay[k] = taz[k] = 0ull;
+        // Each 32-ion FP32 partial goes straight into the compensated accumulators.  (Adding
+        // the partials of a tile first, in FP32, saved 3 % of the kernel time but raised the
+        // worst ion's error on the 65,536-ion cloud from 5.7e-7 to 8.8e-7.)
         for (int jb = 0; jb < len; jb += flush_len) {
             const int je = min(len, jb + flush_len);
             f2 ax[IPT], ay[IPT], az[IPT];
@@ -672,29 +667,8 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
             else
                 tile_pairs<IPT, true>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh, zh,
                                       xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
-            if (kTwoLevel) {
-#pragma unroll
-                for (int k = 0; k < IPT; k++) {
-                    tax[k] = add2(tax[k], ax[k]);
-                    tay[k] = add2(tay[k], ay[k]);
-                    taz[k] = add2(taz[k], az[k]);
-                    if (!far) {
-                        // conditioning estimate from the partial sums of near tiles
-                        float a, b;
-                        upk(ax[k], a, b);
-                        const float px = __fadd_rn(a, b);
-                        upk(ay[k], a, b);
-                        const float py = __fadd_rn(a, b);
-                        upk(az[k], a, b);
-                        const float pz = __fadd_rn(a, b);
-                        s2[k] = fmaf(px, px, fmaf(py, py, fmaf(pz, pz, s2[k])));
-                    }
-                }
-            } else {
-                fold_partials<IPT>(ax, ay, az, ks, kc, s2, !far);
-            }
+            fold_partials<IPT>(ax, ay, az, ks, kc, s2, !far);
         }
-        if (kTwoLevel) fold_partials<IPT>(tax, tay, taz, ks, kc, s2, false);
         // close pairs of this tile, one flagged ion at a time by the whole warp
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
@@ -995,7 +969,7 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
 // planner sizes i-blocks as threads x ions.  Variant 0 is the default.
 static const int kC32Shapes[SG_C32_VARIANTS][2] = {{128, 4}, {128, 2}, {256, 2}, {64, 4},
                                                    {128, 4}, {64, 2}, {32, 4}, {32, 4},
-                                                   {64, 2}, {128, 1}};
+                                                   {64, 2}, {128, 1}, {32, 2}, {32, 1}};
 
 int sg_coulomb_fp32c_ib(int variant) {
     if (variant < 0 || variant >= SG_C32_VARIANTS) variant = 0;
@@ -1042,6 +1016,14 @@ cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s) {
         case 9:
             coulomb_fp32c_sorted_kernel<128, 1, 8, 3><<<a.n_items, 128, 0, s>>>(
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            break;
+        case 10:
+            coulomb_fp32c_kernel<32, 2><<<a.n_items, 32, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
+            break;
+        case 11:
+            coulomb_fp32c_kernel<32, 1><<<a.n_items, 32, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
             break;
         default:
             coulomb_fp32c_kernel<128, 4><<<a.n_items, 128, 0, s>>>(

@@ -124,7 +124,7 @@ def test_sorted_variant(ctx, n, variant):
     assert e.max() <= 1e-6, summary(e)
 
 
-@pytest.mark.parametrize("variant", list(range(10)))
+@pytest.mark.parametrize("variant", list(range(12)))
 @pytest.mark.parametrize("n", [33, 1000, 3000])
 def test_every_launch_shape(ctx, variant, n):
     """Every FP32c launch shape (sg_set_coulomb_variant) on small and mid-size clouds."""
