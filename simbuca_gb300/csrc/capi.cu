@@ -173,16 +173,18 @@ inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
 // Launch shape for a set of clouds when the context has no explicit choice: the
 // cloud carrying the most pair work decides.  Measured on GB300 (simbuca_gb300/tune.py,
-// Coulomb kernel time per call): 128 x 2 for a few hundred ions; 64 x 2 from ~1k to
-// ~16k ions (0.032 ms at 1,024, 0.18 ms at 16,384); above that the k-d ordered forms
-// with one 128-ion leaf per block, whose far tile pairs take the high parts only: the
-// leaf over four warps up to ~100k ions (0.53 vs 0.67 ms at 32,768; 1.86 vs 2.54 ms at
-// 65,536), over two warps beyond (28.1 vs 41.7 ms at 262,144).
+// Coulomb kernel time per call): one-warp blocks of 32 x 1 ions up to a few thousand ions
+// per cloud (0.022 ms at 1,024 against 0.032 for 64 x 2), 32 x 2 around 8k, 64 x 2 to
+// ~16k; above that the k-d ordered forms with one 128-ion leaf per block, whose far tile
+// pairs take the high parts only: the leaf over four warps up to ~100k ions (0.53 vs
+// 0.67 ms at 32,768; 1.86 vs 2.54 ms at 65,536), over two warps beyond (28.1 vs 41.7 ms
+// at 262,144).
 int auto_variant(const std::vector<int>& counts, int requested) {
     if (requested >= 0) return requested;
     int big = 0;
     for (int n : counts) big = std::max(big, n);
-    if (big <= 512) return 1;
+    if (big <= 6000) return 11;
+    if (big <= 12000) return 10;
     if (big < 24000) return 5;
     return big < 131072 ? 9 : 8;
 }
