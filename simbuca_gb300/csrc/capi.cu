@@ -174,8 +174,8 @@ inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 // Launch shape for a set of clouds when the context has no explicit choice: the
 // cloud carrying the most pair work decides.  Measured on GB300 (simbuca_gb300/tune.py,
 // Coulomb kernel time per call): one-warp blocks of 32 x 1 ions up to a few thousand ions
-// per cloud (0.022 ms at 1,024 against 0.032 for 64 x 2), 32 x 2 around 8k, 64 x 2 to
-// ~16k; above that the k-d ordered forms with one 128-ion leaf per block, whose far tile
+// per cloud (0.022 ms at 1,024 against 0.032 for 64 x 2), 64 x 2 to ~16k (also the
+// better shape for the 512-cloud scan of up to 8,192 ions each); above that the k-d ordered forms with one 128-ion leaf per block, whose far tile
 // pairs take the high parts only: the leaf over four warps up to ~100k ions (0.53 vs
 // 0.67 ms at 32,768; 1.86 vs 2.54 ms at 65,536), over two warps beyond (28.1 vs 41.7 ms
 // at 262,144).
@@ -184,7 +184,6 @@ int auto_variant(const std::vector<int>& counts, int requested) {
     int big = 0;
     for (int n : counts) big = std::max(big, n);
     if (big <= 6000) return 11;
-    if (big <= 12000) return 10;
     if (big < 24000) return 5;
     return big < 131072 ? 9 : 8;
 }
@@ -261,7 +260,12 @@ void plan(Problem& P, int n_sm) {
     if (items > 0 && items < target) {
         const int f = (int)std::ceil(target / (double)items);
         for (int c = 0; c < C; c++)
-            if (S[c] > 0) S[c] = std::min(S[c] * f, std::max(1, P.hc[c].npad / 128));
+            if (S[c] > 0) {
+                // more j-chunks than 8 only for large clouds: each chunk is one partial sum
+                // per ion for the reduction to add up
+                const int cap_s = P.hc[c].npad <= 8192 ? 8 : (1 << 30);
+                S[c] = std::min({S[c] * f, std::max(1, P.hc[c].npad / 128), cap_s});
+            }
     }
     P.max_slots = 0;
     for (int c = 0; c < C; c++) {
