@@ -260,12 +260,7 @@ void plan(Problem& P, int n_sm) {
     if (items > 0 && items < target) {
         const int f = (int)std::ceil(target / (double)items);
         for (int c = 0; c < C; c++)
-            if (S[c] > 0) {
-                // more j-chunks than 8 only for large clouds: each chunk is one partial sum
-                // per ion for the reduction to add up
-                const int cap_s = P.hc[c].npad <= 8192 ? 8 : (1 << 30);
-                S[c] = std::min({S[c] * f, std::max(1, P.hc[c].npad / 128), cap_s});
-            }
+            if (S[c] > 0) S[c] = std::min(S[c] * f, std::max(1, P.hc[c].npad / 128));
     }
     P.max_slots = 0;
     for (int c = 0; c < C; c++) {
