@@ -164,3 +164,33 @@ def test_sorted_set_state_keeps_order(ctx, variant):
     from simbuca_gb300.configs import Cloud
     ep, ev = replay_error(Cloud(p1, v1, c.mass, c.charge), fp, np.array(ts), np.array(hs), p, v)
     assert ep <= 1e-9 and ev <= 1e-9, (ep, ev)
+
+
+@pytest.mark.parametrize("prec", [SG_PREC_FP64, SG_PREC_FP32C])
+def test_ragged_edges(ctx, prec):
+    """One-, two- and three-ion clouds, a cloud without the Coulomb term and a larger
+    cloud in one batch, each with its own end time: every cloud matches the oracle
+    replaying its accepted steps."""
+    rng = configs.rng_for(88)
+    counts = [1, 2, 3, 700, 40]
+    clouds = [configs.gaussian_cloud(rng, n, 0.4e-3, 300.0, np.full(n, 132.905)) for n in counts]
+    fields = [configs.penning_field(delta=1e3) for _ in counts]
+    fields[4] = configs.penning_field(coulomb=False, delta=1e3)
+    odes = [configs.ode(1e-9, 1e-15, 1e-9, t) for t in (2e-7, 3e-7, 1e-7, 2.5e-7, 4e-7)]
+    allp = np.concatenate([c.pos for c in clouds])
+    allv = np.concatenate([c.vel for c in clouds])
+    allm = np.concatenate([c.mass for c in clouds])
+    allq = np.concatenate([c.charge for c in clouds])
+    b = Batch(ctx, counts, fields, odes, prec)
+    b.upload(allp, allv, allm, allq)
+    ts, hs, info = run_recording(b)
+    p, v = b.download()
+    off = 0
+    tol = 1e-12 if prec == SG_PREC_FP64 else 1e-9
+    for k, c in enumerate(clouds):
+        n = counts[k]
+        assert info[k]["done"] == 1 and info[k]["status"] == 0
+        assert info[k]["t"] >= odes[k].t_end
+        ep, ev = replay_error(c, fields[k], ts[k], hs[k], p[off:off + n], v[off:off + n])
+        assert ep <= tol and ev <= tol, (k, ep, ev)
+        off += n
