@@ -616,19 +616,7 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
     // terms of a tile point the same way, and a 128-term running sum would carry several
     // times the rounding error of the summands.
     const int flush_len = (cl.npad <= 2048) ? 16 : 32;
-    // bounding box of the next j-tile, loaded one tile ahead so that its latency is hidden
-    float nbox[6];
-    {
-        const int jt0 = cl.tile0 + (it.j0 - cl.poff) / 128;
-        for (int q = 0; q < 6; q++) nbox[q] = __ldg(bbox + 8 * (size_t)jt0 + q);
-    }
     for (int t = 0; t < ntiles; t++) {
-        float jbox[6];
-        for (int q = 0; q < 6; q++) jbox[q] = nbox[q];
-        if (t + 1 < ntiles) {
-            const int jtn = cl.tile0 + (it.j0 + (t + 1) * T - cl.poff) / 128;
-            for (int q = 0; q < 6; q++) nbox[q] = __ldg(bbox + 8 * (size_t)jtn + q);
-        }
         const int s = t % STAGES;
         const uint32_t parity = (uint32_t)((t / STAGES) & 1);
         const int j0 = it.j0 + t * T;
@@ -659,6 +647,9 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         // The tile holding this block's own ions takes the variant that keeps the self
         // pair (dx = 0, contributes nothing) out of the close-pair flag.
         const bool diag = (j0 < it.i0 + it.ni) && (j0 + len > it.i0);
+        float jbox[6];
+        const int jt = cl.tile0 + (j0 - cl.poff) / 128;
+        for (int q = 0; q < 6; q++) jbox[q] = bbox[8 * (size_t)jt + q];
         const bool far = !diag && box_dist2(wbox, jbox) > dfar2;  // uniform per warp
         // Each 32-ion FP32 partial goes straight into the compensated accumulators.  (Adding
         // the partials of a tile first, in FP32, saved 3 % of the kernel time but raised the
