@@ -282,7 +282,8 @@ __device__ __forceinline__ void tile_pairs_far(const float* tx, const float* ty,
                                                const float* tq, int jb, int je, const f2* xh,
                                                const f2* yh, const f2* zh, f2 tiny2, f2* ax,
                                                f2* ay, f2* az) {
-#pragma unroll 2
+    constexpr int kFarUnroll = IPT == 1 ? 4 : 2;  // one ion per thread: more j pairs in flight
+#pragma unroll kFarUnroll
     for (int jj = jb; jj < je; jj += 2) {
         const f2 Xj = *reinterpret_cast<const f2*>(tx + jj);
         const f2 Yj = *reinterpret_cast<const f2*>(ty + jj);
