@@ -166,7 +166,7 @@ def coulomb_kernel_name(prec, variant):
     from simbuca_gb300 import abi
     if prec != abi.SG_PREC_FP32C:
         return "coulomb_fp64_kernel"
-    return "coulomb_fp32c_sorted_kernel" if variant in (4, 7, 8, 9) else "coulomb_fp32c_kernel"
+    return "coulomb_fp32c_sorted_kernel" if variant in (4, 7, 8, 9, 12, 13) else "coulomb_fp32c_kernel"
 
 
 def run_ours(args, dist: Dist):

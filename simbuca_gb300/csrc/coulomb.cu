@@ -160,7 +160,8 @@ __device__ __forceinline__ double rsqrt_fp64(double r2) {
 // whole warp (lanes stride over the tile): pairs whose FP32 1/r^3 exceeded wc get their
 // exact FP64 term, minus the capped FP32 term the main loop already summed (a product
 // of two floats, exact in FP64).  Returns the warp-reduced correction (all lanes).
-__device__ __forceinline__ void close_pairs_warp(const float (*tl)[SG_TILE], int len, int j0,
+template <int TL>
+__device__ __forceinline__ void close_pairs_warp(const float (*tl)[TL], int len, int j0,
                                                  int ig, float xih, float yih, float zih,
                                                  float xil, float yil, float zil, float wc,
                                                  double invL2, const double* __restrict__ c64,
@@ -530,7 +531,7 @@ __device__ __forceinline__ void fold_partials(const f2* ax, const f2* ay, const 
     }
 }
 
-template <int NT, int IPT, int MINB, int STAGES>
+template <int NT, int IPT, int MINB, int STAGES, int TJ = SG_TILE>
 __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const float* __restrict__ c32,
                                                             const double* __restrict__ c64,
                                                             const SgWorkItem* __restrict__ items,
@@ -539,7 +540,7 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
                                                             double* __restrict__ part,
                                                             int npad_total, int* errword,
                                                             const float* __restrict__ bbox) {
-    constexpr int T = SG_TILE;
+    constexpr int T = TJ;  // j-tile: a multiple of the 128-ion leaves
     __shared__ __align__(128) float tile[STAGES][7][T];
     __shared__ __align__(8) uint64_t full[STAGES];
     __shared__ double corr[3][NT * IPT];
@@ -645,30 +646,35 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         const float* txl = tile[s][4];
         const float* tyl = tile[s][5];
         const float* tzl = tile[s][6];
-        // The tile holding this block's own ions takes the variant that keeps the self
-        // pair (dx = 0, contributes nothing) out of the close-pair flag.
-        const bool diag = (j0 < it.i0 + it.ni) && (j0 + len > it.i0);
-        float jbox[6];
-        const int jt = cl.tile0 + (j0 - cl.poff) / 128;
-        for (int q = 0; q < 6; q++) jbox[q] = bbox[8 * (size_t)jt + q];
-        const bool far = !diag && box_dist2(wbox, jbox) > dfar2;  // uniform per warp
-        // Each 32-ion FP32 partial goes straight into the compensated accumulators.  (Adding
-        // the partials of a tile first, in FP32, saved 3 % of the kernel time but raised the
-        // worst ion's error on the 65,536-ion cloud from 5.7e-7 to 8.8e-7.)
-        for (int jb = 0; jb < len; jb += flush_len) {
-            const int je = min(len, jb + flush_len);
-            f2 ax[IPT], ay[IPT], az[IPT];
+        // Per 128-ion leaf of the tile: far from this block's leaf, or not.  The leaf holding
+        // this block's own ions takes the variant that keeps the self pair (dx = 0,
+        // contributes nothing) out of the close-pair flag.
+        for (int sub = 0; sub < len; sub += SG_TILE) {
+            const int send = min(len, sub + SG_TILE);
+            const int sj0 = j0 + sub;
+            const bool diag = (sj0 < it.i0 + it.ni) && (j0 + send > it.i0);
+            float jbox[6];
+            const int jt = cl.tile0 + (sj0 - cl.poff) / 128;
+            for (int q = 0; q < 6; q++) jbox[q] = bbox[8 * (size_t)jt + q];
+            const bool far = !diag && box_dist2(wbox, jbox) > dfar2;  // uniform per warp
+            // Each 32-ion FP32 partial goes straight into the compensated accumulators.
+            // (Adding the partials of a tile first, in FP32, saved 3 % of the kernel time but
+            // raised the worst ion's error on the 65,536-ion cloud from 5.7e-7 to 8.8e-7.)
+            for (int jb = sub; jb < send; jb += flush_len) {
+                const int je = min(send, jb + flush_len);
+                f2 ax[IPT], ay[IPT], az[IPT];
 #pragma unroll
-            for (int k = 0; k < IPT; k++) ax[k] = ay[k] = az[k] = 0ull;
-            if (far)
-                tile_pairs_far<IPT>(tx, ty, tz, tq, jb, je, xh, yh, zh, tiny2, ax, ay, az);
-            else if (!diag)
-                tile_pairs<IPT, false>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh, zh,
-                                       xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
-            else
-                tile_pairs<IPT, true>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh, zh,
-                                      xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
-            fold_partials<IPT>(ax, ay, az, ks, kc, s2, !far);
+                for (int k = 0; k < IPT; k++) ax[k] = ay[k] = az[k] = 0ull;
+                if (far)
+                    tile_pairs_far<IPT>(tx, ty, tz, tq, jb, je, xh, yh, zh, tiny2, ax, ay, az);
+                else if (!diag)
+                    tile_pairs<IPT, false>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh,
+                                           zh, xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
+                else
+                    tile_pairs<IPT, true>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh,
+                                          zh, xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
+                fold_partials<IPT>(ax, ay, az, ks, kc, s2, !far);
+            }
         }
         // close pairs of this tile, one flagged ion at a time by the whole warp
 #pragma unroll
@@ -970,7 +976,8 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
 // planner sizes i-blocks as threads x ions.  Variant 0 is the default.
 static const int kC32Shapes[SG_C32_VARIANTS][2] = {{128, 4}, {128, 2}, {256, 2}, {64, 4},
                                                    {128, 4}, {64, 2}, {32, 4}, {32, 4},
-                                                   {64, 2}, {128, 1}, {32, 2}, {32, 1}};
+                                                   {64, 2}, {128, 1}, {32, 2}, {32, 1},
+                                                   {128, 1}, {64, 2}};
 
 int sg_coulomb_fp32c_ib(int variant) {
     if (variant < 0 || variant >= SG_C32_VARIANTS) variant = 0;
@@ -1016,6 +1023,15 @@ cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s) {
             break;
         case 9:
             coulomb_fp32c_sorted_kernel<128, 1, 8, 3><<<a.n_items, 128, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            break;
+        case 12:
+            // as 9 with 256-ion j-tiles: half the ring waits and barriers per pair
+            coulomb_fp32c_sorted_kernel<128, 1, 8, 3, 256><<<a.n_items, 128, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            break;
+        case 13:
+            coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256><<<a.n_items, 64, 0, s>>>(
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 10:
