@@ -175,17 +175,18 @@ inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 // cloud carrying the most pair work decides.  Measured on GB300 (simbuca_gb300/tune.py,
 // Coulomb kernel time per call): one-warp blocks of 32 x 1 ions up to a few thousand ions
 // per cloud (0.022 ms at 1,024 against 0.032 for 64 x 2), 64 x 2 to ~16k (also the
-// better shape for the 512-cloud scan of up to 8,192 ions each); above that the k-d ordered forms with one 128-ion leaf per block, whose far tile
-// pairs take the high parts only: the leaf over four warps up to ~100k ions (0.53 vs
-// 0.67 ms at 32,768; 1.86 vs 2.54 ms at 65,536), over two warps beyond (28.1 vs 41.7 ms
-// at 262,144).
+// better shape for the 512-cloud scan of up to 8,192 ions each); above that the k-d
+// ordered forms with one 128-ion leaf per block, whose far tile pairs take the high
+// parts only: the leaf over four warps for tens of thousands of ions (0.525 vs 0.684 ms
+// at 32,768), the leaf over two warps with 256-ion j-tiles beyond (1.86 vs 2.54 ms at
+// 65,536; 27.9 vs 41.8 ms at 262,144).
 int auto_variant(const std::vector<int>& counts, int requested) {
     if (requested >= 0) return requested;
     int big = 0;
     for (int n : counts) big = std::max(big, n);
     if (big <= 6000) return 11;
     if (big < 24000) return 5;
-    return big < 131072 ? 9 : 8;
+    return big < 48000 ? 9 : 13;
 }
 
 // Partition clouds into row blocks and Coulomb work items.  Items are sized so that
