@@ -215,6 +215,7 @@ void plan(Problem& P, int n_sm) {
     for (int c = 0; c < C; c++) {
         SgCloud& cl = P.hc[c];
         memset(&cl, 0, sizeof cl);
+        cl.qscale = 1.0;
         cl.fp = fps[c];
         cl.off = off;
         cl.n = P.counts[c];
@@ -779,6 +780,19 @@ void fill_info(const Problem& P, sg_step_info* info) {
     }
 }
 
+// FP32c charge scale of each cloud from its charges (caller order): one common nonzero
+// charge q gives qscale = q and normalized charges 1, so that the Coulomb kernels can skip
+// the charge product; otherwise qscale = 1.
+void set_charge_scale(Problem& P, const double* q) {
+    for (int c = 0; c < P.n_clouds; c++) {
+        SgCloud& cl = P.hc[c];
+        bool uni = cl.n > 0 && q[cl.off] != 0.0;
+        for (int i = cl.off + 1; uni && i < cl.off + cl.n; i++) uni = q[i] == q[cl.off];
+        cl.quniform = uni ? 1 : 0;
+        cl.qscale = uni ? q[cl.off] : 1.0;
+    }
+}
+
 // Per-ion constants of the reference: q e/m (force.cpp:71) and the Coulomb factor
 // coulomb_scale*ke*e*q*e/m written in the order of force.cpp:153.
 void ion_constants(const Problem& P, const double* mass, const int* charge,
@@ -970,6 +984,7 @@ int sg_coulomb_accel(sg_ctx* ctx, int precision, int n, const double* pos, const
     if (st != SG_OK) return st;
     Problem& P = ctx->solo;
     CK(cudaMemcpyAsync(P.qd0, q, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    set_charge_scale(P, q);
     CK(cudaMemcpyAsync(P.kq0, kq, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     st = upload_state(ctx, P, pos, nullptr);
     if (st != SG_OK) return st;
@@ -998,6 +1013,7 @@ int sg_force(sg_ctx* ctx, int precision, int n, const double* pos, const double*
     Problem& P = ctx->solo;
     std::vector<double> kq, qm, qd;
     ion_constants(P, mass, charge, kq, qm, qd);
+    set_charge_scale(P, qd.data());
     CK(cudaMemcpyAsync(P.qd0, qd.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(P.kq0, kq.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(P.qm0, qm.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
@@ -1096,6 +1112,7 @@ int sg_batch_upload(sg_ctx* ctx, const double* pos, const double* vel, const dou
     CK(cudaSetDevice(ctx->device));
     std::vector<double> kq, qm, qd;
     ion_constants(P, mass, charge, kq, qm, qd);
+    set_charge_scale(P, qd.data());
     const size_t N = (size_t)P.n;
     CK(cudaMemcpyAsync(P.kq0, kq.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(P.qm0, qm.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));

@@ -164,7 +164,8 @@ template <int TL>
 __device__ __forceinline__ void close_pairs_warp(const float (*tl)[TL], int len, int j0,
                                                  int ig, float xih, float yih, float zih,
                                                  float xil, float yil, float zil, float wc,
-                                                 double invL2, const double* __restrict__ c64,
+                                                 double invL2, double qscale,
+                                                 const double* __restrict__ c64,
                                                  int npad_total, double& ox, double& oy,
                                                  double& oz) {
     const int lane = threadIdx.x & 31;
@@ -182,9 +183,10 @@ __device__ __forceinline__ void close_pairs_warp(const float (*tl)[TL], int len,
             const double r2d = rx * rx + ry * ry + rz * rz;
             const double inv = rsqrt_fp64(r2d);
             const double wq = c64[3 * (size_t)npad_total + jg] * inv * inv * inv;
-            cx += wq * rx + invL2 * ((double)wf * (double)p.dx);
-            cy += wq * ry + invL2 * ((double)wf * (double)p.dy);
-            cz += wq * rz + invL2 * ((double)wf * (double)p.dz);
+            const double wsc = invL2 * qscale * (double)wf;
+            cx += wq * rx + wsc * (double)p.dx;
+            cy += wq * ry + wsc * (double)p.dy;
+            cz += wq * rz + wsc * (double)p.dz;
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -200,7 +202,7 @@ __device__ __forceinline__ void close_pairs_warp(const float (*tl)[TL], int len,
 // Main loop over one shared-memory j-tile for the IPT ions of a thread: packed FP32x2
 // over consecutive j pairs.  DIAG: the tile contains the thread's own ions, whose self
 // pair must not raise the close-pair flag.
-template <int IPT, bool DIAG>
+template <int IPT, bool DIAG, bool NOQ = false>
 __device__ __forceinline__ void tile_pairs(const float* tx, const float* ty, const float* tz,
                                            const float* tq, const float* txl, const float* tyl,
                                            const float* tzl, int jb, int je, int j0,
@@ -213,7 +215,7 @@ __device__ __forceinline__ void tile_pairs(const float* tx, const float* ty, con
         const f2 Xj = *reinterpret_cast<const f2*>(tx + jj);
         const f2 Yj = *reinterpret_cast<const f2*>(ty + jj);
         const f2 Zj = *reinterpret_cast<const f2*>(tz + jj);
-        const f2 Qj = *reinterpret_cast<const f2*>(tq + jj);
+        const f2 Qj = NOQ ? 0ull : *reinterpret_cast<const f2*>(tq + jj);
         const f2 XLj = *reinterpret_cast<const f2*>(txl + jj);
         const f2 YLj = *reinterpret_cast<const f2*>(tyl + jj);
         const f2 ZLj = *reinterpret_cast<const f2*>(tzl + jj);
@@ -238,7 +240,8 @@ __device__ __forceinline__ void tile_pairs(const float* tx, const float* ty, con
             } else {
                 y3max[k] = fmaxf(y3max[k], fmaxf(ua, ub));
             }
-            const f2 w = mul2(Qj, pk(fminf(ua, wc), fminf(ub, wc)));
+            const f2 wy = pk(fminf(ua, wc), fminf(ub, wc));
+            const f2 w = NOQ ? wy : mul2(Qj, wy);
             ax[k] = fma2(w, dx, ax[k]);
             ay[k] = fma2(w, dy, ay[k]);
             az[k] = fma2(w, dz, az[k]);
@@ -278,7 +281,7 @@ __device__ __forceinline__ float box_dist2(const float* a, const float* b) {
 }
 
 // Far tiles: packed FP32x2 over j pairs, high parts only, no close pairs possible.
-template <int IPT>
+template <int IPT, bool NOQ = false>
 __device__ __forceinline__ void tile_pairs_far(const float* tx, const float* ty, const float* tz,
                                                const float* tq, int jb, int je, const f2* xh,
                                                const f2* yh, const f2* zh, f2 tiny2, f2* ax,
@@ -289,7 +292,7 @@ __device__ __forceinline__ void tile_pairs_far(const float* tx, const float* ty,
         const f2 Xj = *reinterpret_cast<const f2*>(tx + jj);
         const f2 Yj = *reinterpret_cast<const f2*>(ty + jj);
         const f2 Zj = *reinterpret_cast<const f2*>(tz + jj);
-        const f2 Qj = *reinterpret_cast<const f2*>(tq + jj);
+        const f2 Qj = NOQ ? 0ull : *reinterpret_cast<const f2*>(tq + jj);
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             const f2 dx = sub2(Xj, xh[k]);
@@ -301,7 +304,8 @@ __device__ __forceinline__ void tile_pairs_far(const float* tx, const float* ty,
             float ra, rb;
             upk(r2, ra, rb);
             const f2 y = pk(rsqrt_approx(ra), rsqrt_approx(rb));
-            const f2 w = mul2(Qj, mul2(mul2(y, y), y));
+            const f2 y3 = mul2(mul2(y, y), y);
+            const f2 w = NOQ ? y3 : mul2(Qj, y3);
             ax[k] = fma2(w, dx, ax[k]);
             ay[k] = fma2(w, dy, ay[k]);
             az[k] = fma2(w, dz, az[k]);
@@ -331,6 +335,10 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
     const SgCloud& cl = clouds[it.cloud];
     const float wc = cl.wc;
     const double invL2 = cl.invL * cl.invL;
+    // uniform-charge clouds hold q_j / qscale (1 for ions, 0 for padding): tiles without
+    // padding skip the charge product and the sums are scaled once at the end
+    const double qscale = cl.qscale;
+    const int j_real_end = cl.poff + cl.n;
     const int tid = threadIdx.x;
     const float* X = c32;
     const float* Y = c32 + npad_total;
@@ -470,7 +478,7 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
                 const float zil = __shfl_sync(0xffffffffu, a, src);
                 const int igs = __shfl_sync(0xffffffffu, ipad[k], src);
                 double ox, oy, oz;
-                close_pairs_warp(tile[s], len, j0, igs, xih, yih, zih, xil, yil, zil, wc, invL2,
+                close_pairs_warp(tile[s], len, j0, igs, xih, yih, zih, xil, yil, zil, wc, invL2, qscale,
                                  c64, npad_total, ox, oy, oz);
                 if ((tid & 31) == src) {
                     const int li = tid + k * NT;
@@ -498,12 +506,13 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
         if (ipad[k] < 0) continue;
         const int li = tid + k * NT;
         const int ig = ipad[k];
-        P[3 * (size_t)npad_total + ig] = (double)s2[k];
-        // P_i = sum q_j (x_i - x_j)/r^3 = -invL^2 sum w (u_j - u_i) + close-pair terms
-        P[ig] = -invL2 * ((double)ks[k][0] - (double)kc[k][0]) + corr[0][li];
-        P[npad_total + ig] = -invL2 * ((double)ks[k][1] - (double)kc[k][1]) + corr[1][li];
-        P[2 * (size_t)npad_total + ig] =
-            -invL2 * ((double)ks[k][2] - (double)kc[k][2]) + corr[2][li];
+        P[3 * (size_t)npad_total + ig] = (double)s2[k] * (qscale * qscale);
+        // P_i = sum q_j (x_i - x_j)/r^3 = -invL^2 qscale sum w (u_j - u_i) + close-pair
+        // terms, w carrying the charges q_j / qscale
+        const double sc = -invL2 * qscale;
+        P[ig] = sc * ((double)ks[k][0] - (double)kc[k][0]) + corr[0][li];
+        P[npad_total + ig] = sc * ((double)ks[k][1] - (double)kc[k][1]) + corr[1][li];
+        P[2 * (size_t)npad_total + ig] = sc * ((double)ks[k][2] - (double)kc[k][2]) + corr[2][li];
     }
 }
 
@@ -550,6 +559,10 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
     const SgCloud& cl = clouds[it.cloud];
     const float wc = cl.wc;
     const double invL2 = cl.invL * cl.invL;
+    // uniform-charge clouds hold q_j / qscale (1 for ions, 0 for padding): tiles without
+    // padding skip the charge product and the sums are scaled once at the end
+    const double qscale = cl.qscale;
+    const int j_real_end = cl.poff + cl.n;
     const int tid = threadIdx.x;
     const float* X = c32;
     const float* Y = c32 + npad_total;
@@ -649,6 +662,8 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         // Per 128-ion leaf of the tile: far from this block's leaf, or not.  The leaf holding
         // this block's own ions takes the variant that keeps the self pair (dx = 0,
         // contributes nothing) out of the close-pair flag.
+        // no padding ions in this tile: their normalized charge 0 is the only one not 1
+        const bool noq = cl.quniform && j0 + len <= j_real_end;
         for (int sub = 0; sub < len; sub += SG_TILE) {
             const int send = min(len, sub + SG_TILE);
             const int sj0 = j0 + sub;
@@ -665,8 +680,14 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
                 f2 ax[IPT], ay[IPT], az[IPT];
 #pragma unroll
                 for (int k = 0; k < IPT; k++) ax[k] = ay[k] = az[k] = 0ull;
-                if (far)
-                    tile_pairs_far<IPT>(tx, ty, tz, tq, jb, je, xh, yh, zh, tiny2, ax, ay, az);
+                if (far && noq)
+                    tile_pairs_far<IPT, true>(tx, ty, tz, tq, jb, je, xh, yh, zh, tiny2, ax, ay, az);
+                else if (far)
+                    tile_pairs_far<IPT, false>(tx, ty, tz, tq, jb, je, xh, yh, zh, tiny2, ax, ay, az);
+                else if (!diag && noq)
+                    tile_pairs<IPT, false, true>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad,
+                                                 xh, yh, zh, xl, yl, zl, tiny2, wc, ax, ay, az,
+                                                 y3max);
                 else if (!diag)
                     tile_pairs<IPT, false>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh,
                                            zh, xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
@@ -698,7 +719,7 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
                 const float zil = __shfl_sync(0xffffffffu, a, src);
                 const int igs = __shfl_sync(0xffffffffu, ipad[k], src);
                 double ox, oy, oz;
-                close_pairs_warp(tile[s], len, j0, igs, xih, yih, zih, xil, yil, zil, wc, invL2,
+                close_pairs_warp(tile[s], len, j0, igs, xih, yih, zih, xil, yil, zil, wc, invL2, qscale,
                                  c64, npad_total, ox, oy, oz);
                 if ((tid & 31) == src) {
                     const int li = IPT * tid + k;
@@ -726,12 +747,13 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         if (ipad[k] < 0) continue;
         const int li = IPT * tid + k;
         const int ig = ipad[k];
-        P[3 * (size_t)npad_total + ig] = (double)s2[k];
-        // P_i = sum q_j (x_i - x_j)/r^3 = -invL^2 sum w (u_j - u_i) + close-pair terms
-        P[ig] = -invL2 * ((double)ks[k][0] - (double)kc[k][0]) + corr[0][li];
-        P[npad_total + ig] = -invL2 * ((double)ks[k][1] - (double)kc[k][1]) + corr[1][li];
-        P[2 * (size_t)npad_total + ig] =
-            -invL2 * ((double)ks[k][2] - (double)kc[k][2]) + corr[2][li];
+        P[3 * (size_t)npad_total + ig] = (double)s2[k] * (qscale * qscale);
+        // P_i = sum q_j (x_i - x_j)/r^3 = -invL^2 qscale sum w (u_j - u_i) + close-pair
+        // terms, w carrying the charges q_j / qscale
+        const double sc = -invL2 * qscale;
+        P[ig] = sc * ((double)ks[k][0] - (double)kc[k][0]) + corr[0][li];
+        P[npad_total + ig] = sc * ((double)ks[k][1] - (double)kc[k][1]) + corr[1][li];
+        P[2 * (size_t)npad_total + ig] = sc * ((double)ks[k][2] - (double)kc[k][2]) + corr[2][li];
     }
 }
 
@@ -928,9 +950,10 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
                     const double rx = xi - c64[jg], ry = yi - c64[NP + jg], rz = zi - c64[2 * NP + jg];
                     const double inv = rsqrt_fp64(rx * rx + ry * ry + rz * rz);
                     const double wq = c64[3 * NP + jg] * inv * inv * inv;
-                    ax += wq * rx + invL2 * ((double)wf * (double)p.dx);
-                    ay += wq * ry + invL2 * ((double)wf * (double)p.dy);
-                    az += wq * rz + invL2 * ((double)wf * (double)p.dz);
+                    const double wsc = invL2 * (double)cl.qscale * (double)wf;
+                    ax += wq * rx + wsc * (double)p.dx;
+                    ay += wq * ry + wsc * (double)p.dy;
+                    az += wq * rz + wsc * (double)p.dz;
                 }
             }
             for (int o = 16; o > 0; o >>= 1) {

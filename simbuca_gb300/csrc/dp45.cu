@@ -545,7 +545,7 @@ __global__ void __launch_bounds__(SG_ROWS) coords_from_state_kernel(DpArgs a,
         const int ig = cl.poff + (i - cl.off);
         write_coords(a, cl, ig, a.y[i], a.y[N + i], a.y[2 * N + i], hu);
         a.c64[3 * (size_t)a.npad + ig] = q[i];
-        if (a.fp32c) a.c32[3 * (size_t)a.npad + ig] = (float)q[i];
+        if (a.fp32c) a.c32[3 * (size_t)a.npad + ig] = (float)(q[i] / cl.qscale);
     }
     if (a.fp32c && a.bbox) tile_bounds(a, cl, rb, li < rb.n, hu[0], hu[1], hu[2]);
     if (last) {

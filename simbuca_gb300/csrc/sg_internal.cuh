@@ -71,6 +71,10 @@ struct SgCloud {
     long long rec_off;   // recorder: first double of this cloud's record ring
     int32_t nsel;        // recorder: ions kept per record (every stride-th in caller order)
     int32_t rec_len;     // recorder: doubles per record
+    // FP32c charges: the FP32 coordinate array holds q / qscale; with all ions of the cloud
+    // at one charge q, qscale = q (quniform = 1) and the normalized charges are 1
+    double qscale;
+    int32_t quniform, pad4;
 };
 
 // Per-cloud Dormand-Prince controller (the scalar part of _ode_vars, bin/ode.h:58-97).

@@ -140,3 +140,23 @@ def test_every_launch_shape(ctx, variant, n):
         ctx.set_coulomb_variant(-1)
     e = rel_err_per_ion(a, ref)
     assert e.max() <= 1e-6, (variant, n, summary(e))
+
+
+@pytest.mark.parametrize("variant", [5, 9, 13])
+@pytest.mark.parametrize("qval", [1.0, 2.0, -1.0, 3.0])
+def test_uniform_charge(ctx, qval, variant):
+    """Clouds whose ions share one charge hold normalized charges and skip the charge
+    product away from the padding tile; 3,001 ions leave padding in the last tile."""
+    n = 3001
+    rng = np.random.default_rng(int(10 * qval) + variant + 50)
+    pos = rng.normal(0, 5e-4, (n, 3))
+    q = np.full(n, qval)
+    kq = kq_of(np.full(n, 132.905 * oracle.AMU), q)
+    ref = oracle.coulomb_kq(pos, q, kq)
+    ctx.set_coulomb_variant(variant)
+    try:
+        a = ctx.coulomb_accel(pos, q, kq, SG_PREC_FP32C)
+    finally:
+        ctx.set_coulomb_variant(-1)
+    e = rel_err_per_ion(a, ref)
+    assert e.max() <= 1e-6, (qval, variant, summary(e))
