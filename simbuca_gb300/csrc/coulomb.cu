@@ -428,12 +428,17 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
         // The tile holding this block's own ions takes the variant that keeps the self
         // pair (dx = 0, contributes nothing) out of the close-pair flag.
         const bool diag = (j0 < it.i0 + it.ni) && (j0 + len > it.i0);
+        // no padding ions in this tile: their normalized charge 0 is the only one not 1
+        const bool noq = cl.quniform && j0 + len <= j_real_end;
         for (int jb = 0; jb < len; jb += flush_len) {
             const int je = min(len, jb + flush_len);
             f2 ax[IPT], ay[IPT], az[IPT];
 #pragma unroll
             for (int k = 0; k < IPT; k++) ax[k] = ay[k] = az[k] = 0ull;
-            if (!diag)
+            if (!diag && noq)
+                tile_pairs<IPT, false, true>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh,
+                                             yh, zh, xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
+            else if (!diag)
                 tile_pairs<IPT, false>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh, zh,
                                        xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
             else
