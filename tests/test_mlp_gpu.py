@@ -107,3 +107,32 @@ def test_proposer_in_the_loop(ctx):
         assert r["status"] == 0 and r["sim_us"] >= 3.0
     # the proposer is never far from the reference controller's step sizes
     assert 0.5 < mlp["mean_h"] / ref["mean_h"] < 2.0
+
+
+def test_mlp_beats_the_controller_rule_on_held_out_steps(ctx):
+    """What the trained network gains over the method without it, measured on steps it
+    has not seen: the reference controller sets the next step from the last error ratio
+    alone, h_k/h_{k-1} = err^-0.2 (up to its constant safety factor); the MLP predicts the
+    same target, log(h_k err_k^-0.2 / h_{k-1}), from the cloud moments and step history.
+    Its mean-squared error on held-out accepted steps must be lower."""
+    X, y = [], []
+    for w, n in ((configs.penning_1k(), 700), (configs.learned_4k(n=1024, seed=5), 700)):
+        xi, yi = proposer.collect(ctx, w, n)
+        X.append(xi)
+        y.append(yi)
+    X, y = np.concatenate(X), np.concatenate(y)
+    assert len(y) > 1000
+    test = np.random.default_rng(0).random(len(y)) < 0.2
+    wts, hist = ctx.mlp_train(X[~test], y[~test], proposer.init_weights(0), iters=1500,
+                              batch=256, lr=2e-3)
+    pred = ctx.mlp_forward(X[test], wts)
+    mse_mlp = float(np.mean((pred - y[test]) ** 2))
+    # the controller rule: log ratio = -0.2 ln(err_{k-1}); feature 10 is log10 of that error
+    rule = -0.2 * math.log(10.0) * X[test, 10]
+    mse_rule = float(np.mean((rule - y[test]) ** 2))
+    # and the best constant shift of that rule (its safety factor fitted to these data)
+    shift = float(np.mean(y[~test] + 0.2 * math.log(10.0) * X[~test, 10]))
+    mse_rule_fit = float(np.mean((rule + shift - y[test]) ** 2))
+    print(f"held-out MSE: MLP {mse_mlp:.4g}, controller rule {mse_rule:.4g}, "
+          f"rule with fitted safety {mse_rule_fit:.4g}")
+    assert mse_mlp < min(mse_rule, mse_rule_fit)
