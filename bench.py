@@ -305,7 +305,9 @@ def run_ours(args, dist: Dist):
                 "mean_h": sum(a["t"] - b["t"] for a, b in zip(e_after, e_before)) /
                 max(1, sum(a["steps"] - b["steps"] for a, b in zip(e_after, e_before)))},
         "mean_h": sim_us * 1e-6 / max(1, sum(a["steps"] - b["steps"] for a, b in zip(s_after, s_before))),
-        "gpu_launches": int(attempts * 21),
+        # per attempt: 7 stages, 6 Coulomb sums, 6 reductions, control, commit, and with
+        # FP32c the 6 fix-up launches of the conditioning work list
+        "gpu_launches": int(attempts * (27 if prec == abi.SG_PREC_FP32C else 21)),
         "fixup_ions_per_coulomb_call": fixups / max(1, kt["coulomb_launches"]),
         "attempts": int(attempts),
         "interactions_per_s": kt["interactions"] / (kt["coulomb_ms"] * 1e-3) if kt["coulomb_ms"] else None,
@@ -452,7 +454,7 @@ def run_batched(args, dist: Dist):
                    "precision": args.precision, "attempts_per_step": per_step,
                    "parallelism": f"replicas x{dist.world}",
                    "l2": "flushed (256 MB write) between timed steps"},
-        "gpu_launches": int(21 * per_step * args.steps),
+        "gpu_launches": int((27 if args.precision == "fp32c" else 21) * per_step * args.steps),
         "attempts": int(attempts),
         "coulomb_interactions_per_s": sum(
             6.0 * n * (n - 1) * ((a["steps"] + a["rejects"]) - (b["steps"] + b["rejects"]))

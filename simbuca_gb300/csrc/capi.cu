@@ -69,6 +69,8 @@ struct Problem {
     std::vector<int> hspec0;
     std::vector<double> hmass0;
     double *pmass = nullptr, *pmass0 = nullptr;  // print masses (dissociation), both orders
+    int* fix_list = nullptr;   // FP32c fix-up work list: count, then (ion, cloud) pairs
+    double* fix_pf = nullptr;
     // operation sequence
     std::vector<sg_field_params> fp0;  // field parameters as created / set by the caller
     std::vector<SgOp> hops;
@@ -155,6 +157,8 @@ void free_problem(Problem& P) {
     cudaFree(P.spec);
     cudaFree(P.pmass);
     cudaFree(P.pmass0);
+    cudaFree(P.fix_list);
+    cudaFree(P.fix_pf);
     cudaFree(P.dops);
     cudaFree(P.dis_spec);
     cudaFree(P.dis_mass);
@@ -399,6 +403,9 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(cudaMemset(P.spec, 0, N * sizeof(int)));
     CK(dalloc(&P.pmass, N));
     CK(dalloc(&P.pmass0, N));
+    CK(dalloc(&P.fix_list, 1 + 2 * N));
+    CK(dalloc(&P.fix_pf, N));
+    CK(cudaMemset(P.fix_list, 0, sizeof(int)));
     CK(cudaMemset(P.pmass, 0, N * sizeof(double)));
     CK(cudaMemset(P.pmass0, 0, N * sizeof(double)));
     CK(dalloc(&P.bbox, (size_t)std::max(P.ntiles, 1) * 8));
@@ -588,6 +595,8 @@ int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter, double
     ca.errword = P.flags;
     ca.variant = P.variant;
     ca.bbox = P.bbox;
+    ca.fix_list = P.fix_list;
+    ca.fix_pf = P.fix_pf;
     TimedLaunch tl{nullptr, nullptr, inter};
     const int cap = ctx->capture_events;
     if (cap >= 0) {

@@ -845,20 +845,18 @@ constexpr double kKappa2 = 2.25;
 
 // tiles listed for the fix-up scan of one ion in k-d order
 constexpr int kNearCap = 1024;
+// blocks of the fix-up kernel (each takes every kFixupBlocks-th flagged ion)
+constexpr int kFixupBlocks = 256;
 
+// Sums the j-chunk partials of each ion (x, y, z and the FP32c conditioning estimate s2)
+// into out.  FP32c: an ion whose terms cancel strongly (sqrt(s2) > 1.5 |P|) is put on the
+// fix-up work list; coulomb_fixup_kernel then re-evaluates its dominant pairs in FP64.
 template <bool F32>
 __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     const SgRowBlock* __restrict__ rows, const SgCloud* __restrict__ clouds,
-    const SgCtrl* __restrict__ ctrl, const double* __restrict__ part,
-    const float* __restrict__ c32, const double* __restrict__ c64, int npad_total,
+    const SgCtrl* __restrict__ ctrl, const double* __restrict__ part, int npad_total,
     double* __restrict__ out, int n_total, int* __restrict__ counters,
-    const float* __restrict__ bbox) {
-    __shared__ int list[SG_ROWS];
-    __shared__ int nl;
-    __shared__ double cx[SG_ROWS], cy[SG_ROWS], cz[SG_ROWS], pm[SG_ROWS];
-    __shared__ double wsum[SG_ROWS / 32][3];
-    __shared__ int wcnt[SG_ROWS / 32];
-    __shared__ int near_tiles[kNearCap];
+    int* __restrict__ fix_list, double* __restrict__ fix_pf) {
     const SgRowBlock rb = rows[blockIdx.x];
     if (ctrl != nullptr &&
         (ctrl[rb.cloud].done || ctrl[rb.cloud].hold || ctrl[rb.cloud].status != SG_OK))
@@ -866,135 +864,144 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     const SgCloud& cl = clouds[rb.cloud];
     if (!(cl.fp.flags & SG_F_COULOMB)) return;
     const int li = threadIdx.x;
-    if (li == 0) nl = 0;
-    __syncthreads();
-    const bool act = li < rb.n;
-    const int i = rb.i0 + (act ? li : 0);
+    if (li >= rb.n) return;
+    const int i = rb.i0 + li;
     const int ig = cl.poff + (i - cl.off);
     const size_t NP = (size_t)npad_total;
     double px = 0.0, py = 0.0, pz = 0.0, s2 = 0.0;
-    if (act) {
-        for (int sl = 0; sl < cl.nslots; sl++) {
-            const double* P = part + (size_t)sl * 4 * NP;
-            px += P[ig];
-            py += P[NP + ig];
-            pz += P[2 * NP + ig];
-            s2 += P[3 * NP + ig];
+    for (int sl = 0; sl < cl.nslots; sl++) {
+        const double* P = part + (size_t)sl * 4 * NP;
+        px += P[ig];
+        py += P[NP + ig];
+        pz += P[2 * NP + ig];
+        s2 += P[3 * NP + ig];
+    }
+    out[i] = px;
+    out[(size_t)n_total + i] = py;
+    out[2 * (size_t)n_total + i] = pz;
+    if (F32) {
+        const double pf = sqrt(px * px + py * py + pz * pz) * (cl.L * cl.L);  // frame units
+        if (s2 > kKappa2 * pf * pf) {
+            const int at = atomicAdd(fix_list, 1);
+            fix_list[1 + 2 * at] = i;
+            fix_list[2 + 2 * at] = rb.cloud;
+            fix_pf[at] = pf;
+            if (counters != nullptr) atomicAdd(counters, 1);
         }
     }
-    if (F32) {
-        cx[li] = cy[li] = cz[li] = 0.0;
-        const double pf = sqrt(px * px + py * py + pz * pz) * (cl.L * cl.L);  // frame units
-        pm[li] = pf;
-        if (act && s2 > kKappa2 * pf * pf) list[atomicAdd(&nl, 1)] = li;
-        __syncthreads();
-        const int warp = li >> 5, lane = li & 31;
+}
+
+// FP64 fix-up of the flagged ions, one block per ion (blocks stride over the list): the
+// pairs with |f_ij| > |P_i| / 10 are re-evaluated in FP64 and their FP32 terms, as the
+// Coulomb kernel summed them, removed.  Each ion is corrected by one block, in a fixed
+// order of its j-ions, so results do not depend on the order of the list.
+__global__ void __launch_bounds__(SG_ROWS) coulomb_fixup_kernel(
+    const SgCloud* __restrict__ clouds, const float* __restrict__ c32,
+    const double* __restrict__ c64, int npad_total, double* __restrict__ out, int n_total,
+    const int* __restrict__ fix_list, const double* __restrict__ fix_pf,
+    const float* __restrict__ bbox) {
+    __shared__ double wsum[SG_ROWS / 32][3];
+    __shared__ int wcnt[SG_ROWS / 32];
+    __shared__ int near_tiles[kNearCap];
+    const int li = threadIdx.x;
+    const int warp = li >> 5, lane = li & 31;
+    const size_t NP = (size_t)npad_total;
+    const int count = fix_list[0];
+    for (int k = blockIdx.x; k < count; k += gridDim.x) {
+        const int i = fix_list[1 + 2 * k];
+        const SgCloud& cl = clouds[fix_list[2 + 2 * k]];
+        const int igk = cl.poff + (i - cl.off);
         const double invL2 = cl.invL * cl.invL;
         const float wc = cl.wc;
-        // flagged ions one at a time, the whole block striding over the cloud's j-ions
-        for (int k = 0; k < nl; k++) {
-            const int lk = list[k];
-            const int igk = cl.poff + (rb.i0 + lk - cl.off);
-            const double tq = 0.1 * pm[lk];
-            const float thr3 = (float)(tq * sqrt(tq));  // (|P|/10)^(3/2): |f_ij| > |P|/10
-            const float xih = c32[igk], yih = c32[NP + igk], zih = c32[2 * NP + igk];
-            const float xil = c32[4 * NP + igk], yil = c32[5 * NP + igk], zil = c32[6 * NP + igk];
-            const double xi = c64[igk], yi = c64[NP + igk], zi = c64[2 * NP + igk];
-            double ax = 0.0, ay = 0.0, az = 0.0;
-            const float* ibox = bbox ? bbox + 8 * (size_t)(cl.tile0 + (igk - cl.poff) / 128) : nullptr;
-            // k-d ordered clouds: scan only the tiles near the ion's own tile, listed in
-            // order by a block-wide ballot (far tiles were summed from the high parts and
-            // are left as they are); the whole cloud if the list would overflow
-            int n_near = 0;
-            if (ibox != nullptr) {
-                const int nt = (cl.npad + 127) / 128, itile = (igk - cl.poff) / 128;
-                const float dfar2 = cl.dfar * cl.dfar;
-                for (int t0 = 0; t0 < nt; t0 += SG_ROWS) {
-                    const int t = t0 + li;
-                    const bool nr = t < nt && (t == itile ||
-                                               box_dist2(ibox, bbox + 8 * (size_t)(cl.tile0 + t)) <= dfar2);
-                    const unsigned m = __ballot_sync(0xffffffffu, nr);
-                    if (lane == 0) wcnt[warp] = __popc(m);
-                    __syncthreads();
-                    int off = n_near, tot = 0;
-                    for (int w = 0; w < SG_ROWS / 32; w++) {
-                        if (w < warp) off += wcnt[w];
-                        tot += wcnt[w];
-                    }
-                    if (nr) {
-                        const int at = off + __popc(m & ((1u << lane) - 1u));
-                        if (at < kNearCap) near_tiles[at] = t;
-                    }
-                    __syncthreads();
-                    n_near += tot;
-                }
-            }
-            const bool listed = ibox != nullptr && n_near <= kNearCap;
-            const int n_scan = listed ? n_near * 128 : cl.npad;
-            for (int qj = li; qj < n_scan; qj += SG_ROWS) {
-                const int j = listed ? near_tiles[qj >> 7] * 128 + (qj & 127) : qj;
-                if (j >= cl.npad) continue;
-                const int jg = cl.poff + j;
-                PairF p = pair_f32(c32[jg], c32[NP + jg], c32[2 * NP + jg], c32[4 * NP + jg],
-                                   c32[5 * NP + jg], c32[6 * NP + jg], xih, yih, zih, xil, yil,
-                                   zil);
-                if (ibox != nullptr && !listed) {
-                    // the sorted kernel summed this pair from the high parts if its tiles are far
-                    const float* jbox = bbox + 8 * (size_t)(cl.tile0 + j / 128);
-                    const bool same = (igk - cl.poff) / 128 == j / 128;
-                    if (!same && box_dist2(ibox, jbox) > cl.dfar * cl.dfar) {
-                        const PairH q = pair_hi(c32[jg], c32[NP + jg], c32[2 * NP + jg], xih, yih, zih);
-                        p.dx = q.dx;
-                        p.dy = q.dy;
-                        p.dz = q.dz;
-                        p.y3 = q.y3;
-                    }
-                }
-                if (p.y3 > thr3 && p.y3 <= wc && jg != igk) {
-                    const float wf = __fmul_rn(c32[3 * NP + jg], p.y3);
-                    const double rx = xi - c64[jg], ry = yi - c64[NP + jg], rz = zi - c64[2 * NP + jg];
-                    const double inv = rsqrt_fp64(rx * rx + ry * ry + rz * rz);
-                    const double wq = c64[3 * NP + jg] * inv * inv * inv;
-                    const double wsc = invL2 * (double)cl.qscale * (double)wf;
-                    ax += wq * rx + wsc * (double)p.dx;
-                    ay += wq * ry + wsc * (double)p.dy;
-                    az += wq * rz + wsc * (double)p.dz;
-                }
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                ax += __shfl_down_sync(0xffffffffu, ax, o);
-                ay += __shfl_down_sync(0xffffffffu, ay, o);
-                az += __shfl_down_sync(0xffffffffu, az, o);
-            }
-            if (lane == 0) {
-                wsum[warp][0] = ax;
-                wsum[warp][1] = ay;
-                wsum[warp][2] = az;
-            }
-            __syncthreads();
-            if (li == 0) {
-                double sx = 0.0, sy = 0.0, sz = 0.0;
+        const double tq = 0.1 * fix_pf[k];
+        const float thr3 = (float)(tq * sqrt(tq));  // (|P|/10)^(3/2): |f_ij| > |P|/10
+        const float xih = c32[igk], yih = c32[NP + igk], zih = c32[2 * NP + igk];
+        const float xil = c32[4 * NP + igk], yil = c32[5 * NP + igk], zil = c32[6 * NP + igk];
+        const double xi = c64[igk], yi = c64[NP + igk], zi = c64[2 * NP + igk];
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        const float* ibox = bbox ? bbox + 8 * (size_t)(cl.tile0 + (igk - cl.poff) / 128) : nullptr;
+        // k-d ordered clouds: scan only the tiles near the ion's own tile, listed in
+        // order by a block-wide ballot (far tiles were summed from the high parts and
+        // are left as they are); the whole cloud if the list would overflow
+        int n_near = 0;
+        if (ibox != nullptr) {
+            const int nt = (cl.npad + 127) / 128, itile = (igk - cl.poff) / 128;
+            const float dfar2 = cl.dfar * cl.dfar;
+            for (int t0 = 0; t0 < nt; t0 += SG_ROWS) {
+                const int t = t0 + li;
+                const bool nr = t < nt && (t == itile ||
+                                           box_dist2(ibox, bbox + 8 * (size_t)(cl.tile0 + t)) <= dfar2);
+                const unsigned m = __ballot_sync(0xffffffffu, nr);
+                if (lane == 0) wcnt[warp] = __popc(m);
+                __syncthreads();
+                int off = n_near, tot = 0;
                 for (int w = 0; w < SG_ROWS / 32; w++) {
-                    sx += wsum[w][0];
-                    sy += wsum[w][1];
-                    sz += wsum[w][2];
+                    if (w < warp) off += wcnt[w];
+                    tot += wcnt[w];
                 }
-                cx[lk] = sx;
-                cy[lk] = sy;
-                cz[lk] = sz;
+                if (nr) {
+                    const int at = off + __popc(m & ((1u << lane) - 1u));
+                    if (at < kNearCap) near_tiles[at] = t;
+                }
+                __syncthreads();
+                n_near += tot;
             }
-            __syncthreads();
+        }
+        const bool listed = ibox != nullptr && n_near <= kNearCap;
+        const int n_scan = listed ? n_near * 128 : cl.npad;
+        for (int qj = li; qj < n_scan; qj += SG_ROWS) {
+            const int j = listed ? near_tiles[qj >> 7] * 128 + (qj & 127) : qj;
+            if (j >= cl.npad) continue;
+            const int jg = cl.poff + j;
+            PairF p = pair_f32(c32[jg], c32[NP + jg], c32[2 * NP + jg], c32[4 * NP + jg],
+                               c32[5 * NP + jg], c32[6 * NP + jg], xih, yih, zih, xil, yil,
+                               zil);
+            if (ibox != nullptr && !listed) {
+                // the sorted kernel summed this pair from the high parts if its tiles are far
+                const float* jbox = bbox + 8 * (size_t)(cl.tile0 + j / 128);
+                const bool same = (igk - cl.poff) / 128 == j / 128;
+                if (!same && box_dist2(ibox, jbox) > cl.dfar * cl.dfar) {
+                    const PairH q = pair_hi(c32[jg], c32[NP + jg], c32[2 * NP + jg], xih, yih, zih);
+                    p.dx = q.dx;
+                    p.dy = q.dy;
+                    p.dz = q.dz;
+                    p.y3 = q.y3;
+                }
+            }
+            if (p.y3 > thr3 && p.y3 <= wc && jg != igk) {
+                const float wf = __fmul_rn(c32[3 * NP + jg], p.y3);
+                const double rx = xi - c64[jg], ry = yi - c64[NP + jg], rz = zi - c64[2 * NP + jg];
+                const double inv = rsqrt_fp64(rx * rx + ry * ry + rz * rz);
+                const double wq = c64[3 * NP + jg] * inv * inv * inv;
+                const double wsc = invL2 * (double)cl.qscale * (double)wf;
+                ax += wq * rx + wsc * (double)p.dx;
+                ay += wq * ry + wsc * (double)p.dy;
+                az += wq * rz + wsc * (double)p.dz;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            ax += __shfl_down_sync(0xffffffffu, ax, o);
+            ay += __shfl_down_sync(0xffffffffu, ay, o);
+            az += __shfl_down_sync(0xffffffffu, az, o);
+        }
+        if (lane == 0) {
+            wsum[warp][0] = ax;
+            wsum[warp][1] = ay;
+            wsum[warp][2] = az;
         }
         __syncthreads();
-        if (li == 0 && nl > 0 && counters != nullptr) atomicAdd(counters, nl);
-        px += cx[li];
-        py += cy[li];
-        pz += cz[li];
-    }
-    if (act) {
-        out[i] = px;
-        out[(size_t)n_total + i] = py;
-        out[2 * (size_t)n_total + i] = pz;
+        if (li == 0) {
+            double sx = 0.0, sy = 0.0, sz = 0.0;
+            for (int w = 0; w < SG_ROWS / 32; w++) {
+                sx += wsum[w][0];
+                sy += wsum[w][1];
+                sz += wsum[w][2];
+            }
+            out[i] += sx;
+            out[(size_t)n_total + i] += sy;
+            out[2 * (size_t)n_total + i] += sz;
+        }
+        __syncthreads();
     }
 }
 
@@ -1088,13 +1095,20 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
                                      int fp32c, double* out, int n_total, int* counters,
                                      cudaStream_t s) {
     if (n_rows <= 0) return cudaSuccess;
-    if (fp32c)
+    if (fp32c) {
+        cudaError_t e = cudaMemsetAsync(a.fix_list, 0, sizeof(int), s);
+        if (e != cudaSuccess) return e;
         coulomb_reduce_kernel<true><<<n_rows, SG_ROWS, 0, s>>>(
-            rows, a.clouds, a.ctrl, a.part, a.c32, a.c64, a.npad_total, out, n_total, counters,
+            rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, a.fix_list,
+            a.fix_pf);
+        // a block per flagged ion: a fixed grid that strides over however many there are
+        coulomb_fixup_kernel<<<kFixupBlocks, SG_ROWS, 0, s>>>(
+            a.clouds, a.c32, a.c64, a.npad_total, out, n_total, a.fix_list, a.fix_pf,
             sg_variant_sorted(a.variant) ? a.bbox : nullptr);
-    else
+    } else {
         coulomb_reduce_kernel<false><<<n_rows, SG_ROWS, 0, s>>>(
-            rows, a.clouds, a.ctrl, a.part, a.c32, a.c64, a.npad_total, out, n_total, counters,
+            rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, nullptr,
             nullptr);
+    }
     return cudaGetLastError();
 }

@@ -315,6 +315,10 @@ struct SgCoulombArgs {
     int* errword;
     int variant;             // FP32c launch shape (sg_coulomb_fp32c_ib)
     const float* bbox;       // [tiles][8] tile bounds (sorted variant)
+    // FP32c conditioning fix-up work list, filled by the reduction: [0] count, then
+    // per flagged ion its global index and cloud (ints) and |P| in frame units
+    int* fix_list;
+    double* fix_pf;
 };
 
 #define SG_C32_VARIANTS 14
