@@ -1102,7 +1102,9 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
             rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, a.fix_list,
             a.fix_pf);
         // a block per flagged ion: a fixed grid that strides over however many there are
-        coulomb_fixup_kernel<<<kFixupBlocks, SG_ROWS, 0, s>>>(
+        // (flagged ions are a small fraction: small batches get a small grid)
+        const int grid = n_total / 256 < 1 ? 1 : (n_total / 256 > kFixupBlocks ? kFixupBlocks : n_total / 256);
+        coulomb_fixup_kernel<<<grid, SG_ROWS, 0, s>>>(
             a.clouds, a.c32, a.c64, a.npad_total, out, n_total, a.fix_list, a.fix_pf,
             sg_variant_sorted(a.variant) ? a.bbox : nullptr);
     } else {
