@@ -107,6 +107,7 @@ struct sg_ctx {
     cudaEvent_t gev[16] = {nullptr};
     int capture_events = -1;  // next event pair while capturing the timed graph, else -1
     cudaEvent_t t0 = nullptr, t1 = nullptr;
+    int* herr = nullptr;  // pinned host word for the device error word
     float* probe_sink = nullptr;
     // MLP training buffers
     float *mlp_wm = nullptr, *mlp_m1 = nullptr, *mlp_m2 = nullptr, *mlp_grad = nullptr,
@@ -262,11 +263,19 @@ void plan(Problem& P, int n_sm) {
         S[c] = std::max(1, (int)std::ceil(cl.npad / jmax));
         items += (long long)((cl.n + ib - 1) / ib) * S[c];
     }
+    // j-chunks are whole 128-ion tiles, or 32-ion ones (plain shapes only: the k-d
+    // ordered kernels test whole tiles) when 128-ion chunks would leave fewer than two
+    // blocks per SM -- a 1,000-ion cloud then runs 1,024 one-warp blocks instead of 256
+    long long full_split = 0;
+    for (int c = 0; c < C; c++)
+        if (S[c] > 0)
+            full_split += (long long)((P.hc[c].n + ib - 1) / ib) * std::max(1, P.hc[c].npad / 128);
+    const int jgran = (!P.sorted && full_split < 2LL * n_sm) ? 32 : 128;
     const double target = conc * 4.0;
     if (items > 0 && items < target) {
         const int f = (int)std::ceil(target / (double)items);
         for (int c = 0; c < C; c++)
-            if (S[c] > 0) S[c] = std::min(S[c] * f, std::max(1, P.hc[c].npad / 128));
+            if (S[c] > 0) S[c] = std::min(S[c] * f, std::max(1, P.hc[c].npad / jgran));
     }
     P.max_slots = 0;
     for (int c = 0; c < C; c++) {
@@ -276,7 +285,7 @@ void plan(Problem& P, int n_sm) {
             continue;
         }
         P.any_coulomb = true;
-        const int jc = round_up((cl.npad + S[c] - 1) / S[c], 128);
+        const int jc = round_up((cl.npad + S[c] - 1) / S[c], jgran);
         int slot = 0;
         for (int j0 = 0; j0 < cl.npad; j0 += jc, slot++) {
             const int nj = std::min(jc, cl.npad - j0);
@@ -760,10 +769,10 @@ int run_attempts(sg_ctx* ctx, Problem& P, int n) {
 int sync_ctrl(sg_ctx* ctx, Problem& P) {
     CK(cudaMemcpyAsync(P.hctrl, P.dctrl, sizeof(SgCtrl) * P.n_clouds, cudaMemcpyDeviceToHost,
                        ctx->stream));
-    int errword = 0;
-    CK(cudaMemcpyAsync(&errword, P.flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->herr, P.flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     flush_timing(ctx);
+    const int errword = *ctx->herr;
     if (errword != 0) return errword;
     return drain_records(ctx, P);
 }
@@ -933,7 +942,8 @@ int sg_create(int device, sg_ctx** out) {
     cudaDeviceProp prop;
     if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) ctx->n_sm = prop.multiProcessorCount;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&ctx->t0) != cudaSuccess || cudaEventCreate(&ctx->t1) != cudaSuccess) {
+        cudaEventCreate(&ctx->t0) != cudaSuccess || cudaEventCreate(&ctx->t1) != cudaSuccess ||
+        cudaMallocHost((void**)&ctx->herr, sizeof(int)) != cudaSuccess) {
         delete ctx;
         return SG_CUDA_ERR;
     }
@@ -965,6 +975,7 @@ int sg_destroy(sg_ctx* ctx) {
     cudaFree(ctx->cb_xi);
     cudaFree(ctx->cb_ai);
     if (ctx->cb_host) cudaFreeHost(ctx->cb_host);
+    cudaFreeHost(ctx->herr);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return SG_OK;
@@ -1210,8 +1221,8 @@ int sg_dp45_step(sg_ctx* ctx, sg_step_info* info) {
     Problem& P = ctx->batch;
     if (!P.uploaded) return SG_NOT_READY;
     CK(cudaSetDevice(ctx->device));
-    const int one = 1, zero = 0;
-    CK(cudaMemcpyAsync(P.flags + 1, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    // hold-on-accept on (any nonzero word) without a host-to-device copy
+    CK(cudaMemsetAsync(P.flags + 1, 1, sizeof(int), ctx->stream));
     int st = SG_OK;
     // every cloud that is active now takes exactly one accepted step (or fails)
     for (long long guard = 0; guard < (1ll << 40); guard++) {
@@ -1226,10 +1237,16 @@ int sg_dp45_step(sg_ctx* ctx, sg_step_info* info) {
         }
         if (all) break;
     }
-    CK(cudaMemcpyAsync(P.flags + 1, &zero, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(P.flags + 1, 0, sizeof(int), ctx->stream));
     CK(sg_clear_hold(P.dctrl, P.n_clouds, ctx->stream));
-    int st2 = sync_ctrl(ctx, P);
-    if (st == SG_OK) st = st2;
+    if (st == SG_OK) {
+        // the host copy is current from the last sync: clear its hold bit the same way
+        // instead of reading the control blocks back once more
+        for (int c = 0; c < P.n_clouds; c++) P.hctrl[c].hold &= ~1;
+    } else {
+        int st2 = sync_ctrl(ctx, P);
+        (void)st2;
+    }
     fill_info(P, info);
     if (st != SG_OK) return st;
     for (int c = 0; c < P.n_clouds; c++)

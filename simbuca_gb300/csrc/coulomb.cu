@@ -839,7 +839,7 @@ __global__ void __launch_bounds__(NT) coulomb_fp64_kernel(const double* __restri
 // 2.5e-7 * sqrt(s2).  An ion whose FP32 terms cancel strongly (sqrt(s2) > 1.5 |P_i|,
 // e.g. near the centre of a cloud) gets its dominant pairs -- those with
 // |f_ij| > 0.1 |P_i| that the main kernel did not already take in FP64 -- re-evaluated
-// in FP64 here, one warp per flagged ion over the cloud's j-range.
+// in FP64, one block per flagged ion over the cloud's j-range.
 // ---------------------------------------------------------------------------
 constexpr double kKappa2 = 2.25;
 
@@ -847,73 +847,35 @@ constexpr double kKappa2 = 2.25;
 constexpr int kNearCap = 1024;
 // blocks of the fix-up kernel (each takes every kFixupBlocks-th flagged ion)
 constexpr int kFixupBlocks = 256;
+// batches up to this many ions fix their flagged ions inside the reduction's blocks
+constexpr int kInBlockFixupMax = 8192;
 
-// Sums the j-chunk partials of each ion (x, y, z and the FP32c conditioning estimate s2)
-// into out.  FP32c: an ion whose terms cancel strongly (sqrt(s2) > 1.5 |P|) is put on the
-// fix-up work list; coulomb_fixup_kernel then re-evaluates its dominant pairs in FP64.
-template <bool F32>
-__global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
-    const SgRowBlock* __restrict__ rows, const SgCloud* __restrict__ clouds,
-    const SgCtrl* __restrict__ ctrl, const double* __restrict__ part, int npad_total,
-    double* __restrict__ out, int n_total, int* __restrict__ counters,
-    int* __restrict__ fix_list, double* __restrict__ fix_pf) {
-    const SgRowBlock rb = rows[blockIdx.x];
-    if (ctrl != nullptr &&
-        (ctrl[rb.cloud].done || ctrl[rb.cloud].hold || ctrl[rb.cloud].status != SG_OK))
-        return;
-    const SgCloud& cl = clouds[rb.cloud];
-    if (!(cl.fp.flags & SG_F_COULOMB)) return;
-    const int li = threadIdx.x;
-    if (li >= rb.n) return;
-    const int i = rb.i0 + li;
-    const int ig = cl.poff + (i - cl.off);
-    const size_t NP = (size_t)npad_total;
-    double px = 0.0, py = 0.0, pz = 0.0, s2 = 0.0;
-    for (int sl = 0; sl < cl.nslots; sl++) {
-        const double* P = part + (size_t)sl * 4 * NP;
-        px += P[ig];
-        py += P[NP + ig];
-        pz += P[2 * NP + ig];
-        s2 += P[3 * NP + ig];
-    }
-    out[i] = px;
-    out[(size_t)n_total + i] = py;
-    out[2 * (size_t)n_total + i] = pz;
-    if (F32) {
-        const double pf = sqrt(px * px + py * py + pz * pz) * (cl.L * cl.L);  // frame units
-        if (s2 > kKappa2 * pf * pf) {
-            const int at = atomicAdd(fix_list, 1);
-            fix_list[1 + 2 * at] = i;
-            fix_list[2 + 2 * at] = rb.cloud;
-            fix_pf[at] = pf;
-            if (counters != nullptr) atomicAdd(counters, 1);
-        }
-    }
-}
+// FP64 fix-up of one flagged ion i (frame-unit force magnitude pf) by the whole block of
+// SG_ROWS threads: the pairs with |f_ij| > |P_i| / 10 are re-evaluated in FP64 and their
+// FP32 terms, as the Coulomb kernel summed them, removed; thread 0 adds the correction to
+// out.  The j-ions are taken in a fixed order, so the result does not depend on which
+// block runs it or when.
+struct FixupShared {
+    double wsum[SG_ROWS / 32][3];
+    int wcnt[SG_ROWS / 32];
+    int near_tiles[kNearCap];
+};
 
-// FP64 fix-up of the flagged ions, one block per ion (blocks stride over the list): the
-// pairs with |f_ij| > |P_i| / 10 are re-evaluated in FP64 and their FP32 terms, as the
-// Coulomb kernel summed them, removed.  Each ion is corrected by one block, in a fixed
-// order of its j-ions, so results do not depend on the order of the list.
-__global__ void __launch_bounds__(SG_ROWS) coulomb_fixup_kernel(
-    const SgCloud* __restrict__ clouds, const float* __restrict__ c32,
-    const double* __restrict__ c64, int npad_total, double* __restrict__ out, int n_total,
-    const int* __restrict__ fix_list, const double* __restrict__ fix_pf,
-    const float* __restrict__ bbox) {
-    __shared__ double wsum[SG_ROWS / 32][3];
-    __shared__ int wcnt[SG_ROWS / 32];
-    __shared__ int near_tiles[kNearCap];
+__device__ void fixup_ion(const SgCloud& cl, int i, double pf, const float* __restrict__ c32,
+                          const double* __restrict__ c64, int npad_total,
+                          double* __restrict__ out, int n_total, const float* __restrict__ bbox,
+                          FixupShared& sh) {
+    double (*wsum)[3] = sh.wsum;
+    int* wcnt = sh.wcnt;
+    int* near_tiles = sh.near_tiles;
     const int li = threadIdx.x;
     const int warp = li >> 5, lane = li & 31;
     const size_t NP = (size_t)npad_total;
-    const int count = fix_list[0];
-    for (int k = blockIdx.x; k < count; k += gridDim.x) {
-        const int i = fix_list[1 + 2 * k];
-        const SgCloud& cl = clouds[fix_list[2 + 2 * k]];
+    {
         const int igk = cl.poff + (i - cl.off);
         const double invL2 = cl.invL * cl.invL;
         const float wc = cl.wc;
-        const double tq = 0.1 * fix_pf[k];
+        const double tq = 0.1 * pf;
         const float thr3 = (float)(tq * sqrt(tq));  // (|P|/10)^(3/2): |f_ij| > |P|/10
         const float xih = c32[igk], yih = c32[NP + igk], zih = c32[2 * NP + igk];
         const float xil = c32[4 * NP + igk], yil = c32[5 * NP + igk], zil = c32[6 * NP + igk];
@@ -1003,6 +965,89 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_fixup_kernel(
         }
         __syncthreads();
     }
+}
+
+// Sums the j-chunk partials of each ion (x, y, z and the FP32c conditioning estimate s2)
+// into out.  FP32c: an ion whose terms cancel strongly (sqrt(s2) > 1.5 |P|) gets its
+// dominant pairs re-evaluated in FP64 (fixup_ion): INBLOCK, by this block right away
+// (small batches, where a second launch costs more than the work); otherwise it is put
+// on the work list of coulomb_fixup_kernel.
+template <bool F32, bool INBLOCK>
+__global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
+    const SgRowBlock* __restrict__ rows, const SgCloud* __restrict__ clouds,
+    const SgCtrl* __restrict__ ctrl, const double* __restrict__ part, int npad_total,
+    double* __restrict__ out, int n_total, int* __restrict__ counters,
+    int* __restrict__ fix_list, double* __restrict__ fix_pf, const float* __restrict__ c32,
+    const double* __restrict__ c64, const float* __restrict__ bbox) {
+    const SgRowBlock rb = rows[blockIdx.x];
+    if (ctrl != nullptr &&
+        (ctrl[rb.cloud].done || ctrl[rb.cloud].hold || ctrl[rb.cloud].status != SG_OK))
+        return;
+    const SgCloud& cl = clouds[rb.cloud];
+    if (!(cl.fp.flags & SG_F_COULOMB)) return;
+    const int li = threadIdx.x;
+    const int i = rb.i0 + li;
+    bool flag = false;
+    double pf = 0.0;
+    if (li < rb.n) {
+        const int ig = cl.poff + (i - cl.off);
+        const size_t NP = (size_t)npad_total;
+        double px = 0.0, py = 0.0, pz = 0.0, s2 = 0.0;
+        for (int sl = 0; sl < cl.nslots; sl++) {
+            const double* P = part + (size_t)sl * 4 * NP;
+            px += P[ig];
+            py += P[NP + ig];
+            pz += P[2 * NP + ig];
+            s2 += P[3 * NP + ig];
+        }
+        out[i] = px;
+        out[(size_t)n_total + i] = py;
+        out[2 * (size_t)n_total + i] = pz;
+        if (F32) {
+            pf = sqrt(px * px + py * py + pz * pz) * (cl.L * cl.L);  // frame units
+            flag = s2 > kKappa2 * pf * pf;
+        }
+    }
+    if (!F32) return;
+    if (!INBLOCK) {
+        if (flag) {
+            const int at = atomicAdd(fix_list, 1);
+            fix_list[1 + 2 * at] = i;
+            fix_list[2 + 2 * at] = rb.cloud;
+            fix_pf[at] = pf;
+            if (counters != nullptr) atomicAdd(counters, 1);
+        }
+        return;
+    }
+    __shared__ FixupShared sh;
+    __shared__ int nflag;
+    __shared__ int flist[SG_ROWS];
+    __shared__ double fpf[SG_ROWS];
+    if (li == 0) nflag = 0;
+    __syncthreads();
+    if (flag) {
+        const int at = atomicAdd(&nflag, 1);
+        flist[at] = i;
+        fpf[at] = pf;
+        if (counters != nullptr) atomicAdd(counters, 1);
+    }
+    __syncthreads();  // also orders this block's writes of out before the corrections
+    const int nf = nflag;
+    for (int k = 0; k < nf; k++)
+        fixup_ion(cl, flist[k], fpf[k], c32, c64, npad_total, out, n_total, bbox, sh);
+}
+
+// The flagged ions of a whole batch, one block per ion (blocks stride over the list).
+__global__ void __launch_bounds__(SG_ROWS) coulomb_fixup_kernel(
+    const SgCloud* __restrict__ clouds, const float* __restrict__ c32,
+    const double* __restrict__ c64, int npad_total, double* __restrict__ out, int n_total,
+    const int* __restrict__ fix_list, const double* __restrict__ fix_pf,
+    const float* __restrict__ bbox) {
+    __shared__ FixupShared sh;
+    const int count = fix_list[0];
+    for (int k = blockIdx.x; k < count; k += gridDim.x)
+        fixup_ion(clouds[fix_list[2 + 2 * k]], fix_list[1 + 2 * k], fix_pf[k], c32, c64,
+                  npad_total, out, n_total, bbox, sh);
 }
 
 }  // namespace
@@ -1096,21 +1141,27 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
                                      cudaStream_t s) {
     if (n_rows <= 0) return cudaSuccess;
     if (fp32c) {
+        const float* bbox = sg_variant_sorted(a.variant) ? a.bbox : nullptr;
+        if (n_total <= kInBlockFixupMax) {
+            coulomb_reduce_kernel<true, true><<<n_rows, SG_ROWS, 0, s>>>(
+                rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, nullptr,
+                nullptr, a.c32, a.c64, bbox);
+            return cudaGetLastError();
+        }
         cudaError_t e = cudaMemsetAsync(a.fix_list, 0, sizeof(int), s);
         if (e != cudaSuccess) return e;
-        coulomb_reduce_kernel<true><<<n_rows, SG_ROWS, 0, s>>>(
+        coulomb_reduce_kernel<true, false><<<n_rows, SG_ROWS, 0, s>>>(
             rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, a.fix_list,
-            a.fix_pf);
+            a.fix_pf, nullptr, nullptr, nullptr);
         // a block per flagged ion: a fixed grid that strides over however many there are
         // (flagged ions are a small fraction: small batches get a small grid)
         const int grid = n_total / 256 < 1 ? 1 : (n_total / 256 > kFixupBlocks ? kFixupBlocks : n_total / 256);
         coulomb_fixup_kernel<<<grid, SG_ROWS, 0, s>>>(
-            a.clouds, a.c32, a.c64, a.npad_total, out, n_total, a.fix_list, a.fix_pf,
-            sg_variant_sorted(a.variant) ? a.bbox : nullptr);
+            a.clouds, a.c32, a.c64, a.npad_total, out, n_total, a.fix_list, a.fix_pf, bbox);
     } else {
-        coulomb_reduce_kernel<false><<<n_rows, SG_ROWS, 0, s>>>(
+        coulomb_reduce_kernel<false, false><<<n_rows, SG_ROWS, 0, s>>>(
             rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, nullptr,
-            nullptr);
+            nullptr, nullptr, nullptr, nullptr);
     }
     return cudaGetLastError();
 }
