@@ -166,7 +166,8 @@ def coulomb_kernel_name(prec, variant):
     from simbuca_gb300 import abi
     if prec != abi.SG_PREC_FP32C:
         return "coulomb_fp64_kernel"
-    return "coulomb_fp32c_sorted_kernel" if variant in (4, 7, 8, 9, 12, 13) else "coulomb_fp32c_kernel"
+    sorted_shapes = (4, 7, 8, 9, 12, 13, 14, 15, 16)
+    return "coulomb_fp32c_sorted_kernel" if variant in sorted_shapes else "coulomb_fp32c_kernel"
 
 
 def run_ours(args, dist: Dist):
@@ -416,6 +417,8 @@ def run_batched(args, dist: Dist):
     allc = w.concat()
     prec = abi.SG_PREC_FP32C if args.precision == "fp32c" else abi.SG_PREC_FP64
     ctx = Context(dist.local)
+    if args.variant >= 0:
+        ctx.set_coulomb_variant(args.variant)
     batch = Batch(ctx, w.counts, w.fields, w.odes, prec)
     batch.upload(allc.pos, allc.vel, allc.mass, allc.charge)
     per_step = 10  # attempts of every cloud per bench step (one graph replay each)

@@ -209,7 +209,8 @@ int sg_fixup_count(sg_ctx* ctx, int64_t* count);
  * order and far tile pairs summed from the high parts of the coordinates, 5 = 64 x 2,
  * 6 = 32 x 4, 7 = the k-d ordered form with one 128-ion leaf per block (32 x 4), 8 = the
  * same with the leaf over two warps (64 x 2), 9 = over four warps (128 x 1), 10 = 32 x 2,
- * 11 = 32 x 1, 12 and 13 = 9 and 8 with 256-ion j-tiles. */
+ * 11 = 32 x 1, 12 and 13 = 9 and 8 with 256-ion j-tiles, 14 = 13 with four j pairs in
+ * flight on far tiles, 15 = 7 with 256-ion j-tiles, 16 = 13 with a 4-stage copy ring. */
 int sg_set_coulomb_variant(sg_ctx* ctx, int variant);
 /* Launch shape the resident batch was planned with (0..4; 0 for FP64 batches). */
 int sg_batch_variant(sg_ctx* ctx, int* variant);

@@ -185,13 +185,23 @@ inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 // parts only: the leaf over four warps for tens of thousands of ions (0.525 vs 0.684 ms
 // at 32,768), the leaf over two warps with 256-ion j-tiles beyond (1.86 vs 2.54 ms at
 // 65,536; 27.9 vs 41.8 ms at 262,144).
+// Thresholds from the launch-shape tuner (simbuca_gb300/tune.py) on GB300: one cloud of
+// up to ~6k ions is latency-bound and runs best as one-warp blocks of 32 ions (11);
+// 64 x 2 blocks (5) to ~24k; the k-d ordered shapes beyond (9; 14 from ~48k).  A batch
+// whose pair work fills the GPU on its own (the 512-cloud scan: 3.5e9 pairs per call)
+// takes the k-d ordered leaf shape whatever its largest cloud.
 int auto_variant(const std::vector<int>& counts, int requested) {
     if (requested >= 0) return requested;
     int big = 0;
-    for (int n : counts) big = std::max(big, n);
+    double pairs = 0.0;
+    for (int n : counts) {
+        big = std::max(big, n);
+        pairs += (double)n * (double)n;
+    }
+    if (big >= 48000) return 14;
+    if (pairs >= 2e9) return 9;
     if (big <= 6000) return 11;
-    if (big < 24000) return 5;
-    return big < 48000 ? 9 : 13;
+    return big < 24000 ? 5 : 9;
 }
 
 // Partition clouds into row blocks and Coulomb work items.  Items are sized so that

@@ -281,12 +281,13 @@ __device__ __forceinline__ float box_dist2(const float* a, const float* b) {
 }
 
 // Far tiles: packed FP32x2 over j pairs, high parts only, no close pairs possible.
-template <int IPT, bool NOQ = false>
+// FU: j pairs unrolled (0: 4 for one ion per thread, else 2).
+template <int IPT, bool NOQ = false, int FU = 0>
 __device__ __forceinline__ void tile_pairs_far(const float* tx, const float* ty, const float* tz,
                                                const float* tq, int jb, int je, const f2* xh,
                                                const f2* yh, const f2* zh, f2 tiny2, f2* ax,
                                                f2* ay, f2* az) {
-    constexpr int kFarUnroll = IPT == 1 ? 4 : 2;  // one ion per thread: more j pairs in flight
+    constexpr int kFarUnroll = FU > 0 ? FU : (IPT == 1 ? 4 : 2);  // more j pairs in flight
 #pragma unroll kFarUnroll
     for (int jj = jb; jj < je; jj += 2) {
         const f2 Xj = *reinterpret_cast<const f2*>(tx + jj);
@@ -545,7 +546,7 @@ __device__ __forceinline__ void fold_partials(const f2* ax, const f2* ay, const 
     }
 }
 
-template <int NT, int IPT, int MINB, int STAGES, int TJ = SG_TILE>
+template <int NT, int IPT, int MINB, int STAGES, int TJ = SG_TILE, int FU = 0>
 __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const float* __restrict__ c32,
                                                             const double* __restrict__ c64,
                                                             const SgWorkItem* __restrict__ items,
@@ -686,9 +687,11 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
 #pragma unroll
                 for (int k = 0; k < IPT; k++) ax[k] = ay[k] = az[k] = 0ull;
                 if (far && noq)
-                    tile_pairs_far<IPT, true>(tx, ty, tz, tq, jb, je, xh, yh, zh, tiny2, ax, ay, az);
+                    tile_pairs_far<IPT, true, FU>(tx, ty, tz, tq, jb, je, xh, yh, zh, tiny2, ax, ay,
+                                                  az);
                 else if (far)
-                    tile_pairs_far<IPT, false>(tx, ty, tz, tq, jb, je, xh, yh, zh, tiny2, ax, ay, az);
+                    tile_pairs_far<IPT, false, FU>(tx, ty, tz, tq, jb, je, xh, yh, zh, tiny2, ax, ay,
+                                                   az);
                 else if (!diag && noq)
                     tile_pairs<IPT, false, true>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad,
                                                  xh, yh, zh, xl, yl, zl, tiny2, wc, ax, ay, az,
@@ -1057,7 +1060,8 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_fixup_kernel(
 static const int kC32Shapes[SG_C32_VARIANTS][2] = {{128, 4}, {128, 2}, {256, 2}, {64, 4},
                                                    {128, 4}, {64, 2}, {32, 4}, {32, 4},
                                                    {64, 2}, {128, 1}, {32, 2}, {32, 1},
-                                                   {128, 1}, {64, 2}};
+                                                   {128, 1}, {64, 2}, {64, 2}, {32, 4},
+                                                   {64, 2}};
 
 int sg_coulomb_fp32c_ib(int variant) {
     if (variant < 0 || variant >= SG_C32_VARIANTS) variant = 0;
@@ -1112,6 +1116,21 @@ cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s) {
             break;
         case 13:
             coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256><<<a.n_items, 64, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            break;
+        case 14:
+            // as 13 with four j pairs in flight per ion on far tiles
+            coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256, 4><<<a.n_items, 64, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            break;
+        case 15:
+            // the leaf in one warp (4 ions per thread), 256-ion j-tiles
+            coulomb_fp32c_sorted_kernel<32, 4, 16, 3, 256><<<a.n_items, 32, 0, s>>>(
+                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            break;
+        case 16:
+            // as 13 with a 4-stage ring
+            coulomb_fp32c_sorted_kernel<64, 2, 8, 4, 256><<<a.n_items, 64, 0, s>>>(
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 10:

@@ -321,13 +321,13 @@ struct SgCoulombArgs {
     double* fix_pf;
 };
 
-#define SG_C32_VARIANTS 14
+#define SG_C32_VARIANTS 17
 // variant 4: ions in k-d tree order, far tile pairs from the high parts only
 #define SG_C32_SORTED 4
 #define SG_C32_SORTED_LEAF 7
 // launch shapes that keep ions in k-d tree order
 __host__ __device__ inline bool sg_variant_sorted(int v) {
-    return v == SG_C32_SORTED || (v >= SG_C32_SORTED_LEAF && v <= 9) || v == 12 || v == 13;
+    return v == SG_C32_SORTED || (v >= SG_C32_SORTED_LEAF && v <= 9) || (v >= 12 && v <= 16);
 }
 int sg_coulomb_fp32c_ib(int variant);
 cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s);

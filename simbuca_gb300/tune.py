@@ -21,7 +21,8 @@ from .constants import EL_CHARGE, KE
 
 VARIANTS = {0: "128x4", 1: "128x2", 2: "256x2", 3: "64x4", 4: "sorted128x4", 5: "64x2",
             6: "32x4", 7: "sorted32x4", 8: "sorted64x2", 9: "sorted128x1", 10: "32x2",
-            11: "32x1", 12: "sorted128x1t256", 13: "sorted64x2t256"}
+            11: "32x1", 12: "sorted128x1t256", 13: "sorted64x2t256", 14: "sorted64x2t256u4",
+            15: "sorted32x4t256", 16: "sorted64x2t256s4"}
 TABLE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
 
 

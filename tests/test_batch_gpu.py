@@ -29,16 +29,22 @@ def small_scan(n_clouds=6, sim_time=0.3e-6):
     return w
 
 
-@pytest.mark.parametrize("prec", [SG_PREC_FP64, SG_PREC_FP32C])
-def test_batch_matches_single_runs(ctx, prec):
+@pytest.mark.parametrize("prec,variant", [(SG_PREC_FP64, -1), (SG_PREC_FP32C, -1),
+                                          (SG_PREC_FP32C, 9), (SG_PREC_FP32C, 14)])
+def test_batch_matches_single_runs(ctx, prec, variant):
     """Each cloud of the batch against the oracle replaying that cloud's accepted steps,
-    and against the oracle's own adaptive run for the step count."""
+    and against the oracle's own adaptive run for the step count; also with every cloud
+    in k-d order (the launch shapes large scans take)."""
     w = small_scan()
     allc = w.concat()
-    b = Batch(ctx, w.counts, w.fields, w.odes, prec)
-    b.upload(allc.pos, allc.vel, allc.mass, allc.charge)
-    ts, hs, info = run_recording(b)
-    p, v = b.download()
+    ctx.set_coulomb_variant(variant)
+    try:
+        b = Batch(ctx, w.counts, w.fields, w.odes, prec)
+        b.upload(allc.pos, allc.vel, allc.mass, allc.charge)
+        ts, hs, info = run_recording(b)
+        p, v = b.download()
+    finally:
+        ctx.set_coulomb_variant(-1)
     off = 0
     tol = 1e-12 if prec == SG_PREC_FP64 else 1e-9
     for k, c in enumerate(w.clouds):

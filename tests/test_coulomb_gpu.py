@@ -103,7 +103,7 @@ def test_bad_arguments(ctx):
     assert L.sg_coulomb_accel(ctx.handle, 0, -1, None, None, None, None) == abi.SG_BAD_ARG
 
 
-@pytest.mark.parametrize("variant", [4, 7, 8, 9, 12, 13])
+@pytest.mark.parametrize("variant", [4, 7, 8, 9, 12, 13, 14, 15, 16])
 @pytest.mark.parametrize("n", [100, 1000, 5000, 20000])
 def test_sorted_variant(ctx, n, variant):
     """Ions in k-d tree order, far tile pairs from the high parts only: same accuracy,
@@ -124,7 +124,7 @@ def test_sorted_variant(ctx, n, variant):
     assert e.max() <= 1e-6, summary(e)
 
 
-@pytest.mark.parametrize("variant", list(range(14)))
+@pytest.mark.parametrize("variant", list(range(17)))
 @pytest.mark.parametrize("n", [33, 1000, 3000])
 def test_every_launch_shape(ctx, variant, n):
     """Every FP32c launch shape (sg_set_coulomb_variant) on small and mid-size clouds."""
