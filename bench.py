@@ -170,6 +170,31 @@ def coulomb_kernel_name(prec, variant):
     return "coulomb_fp32c_sorted_kernel" if variant in sorted_shapes else "coulomb_fp32c_kernel"
 
 
+# Algorithmic HBM traffic of one Dormand-Prince attempt per ion in the O(N) kernels:
+# stage s = 1..6 combines read y and k_1..k_s and write y_s (48(s+2) B), the final
+# combine with the error norm moves 384 B (FP64 SoA, 48 B per 6-vector).
+STAGE_BYTES_PER_ION = 48 * sum(s + 2 for s in range(1, 7)) + 384  # 1968
+
+
+def stage_roofline(args, w, st, attempts):
+    """The O(N) kernels of the kernel-timing pass (7 stage combines, control, commit):
+    algorithmic bytes / event-timed duration against the measured HBM copy rate."""
+    if args.method != 5 or not st["stage_ms"] or not attempts:
+        return None
+    peak = None
+    try:
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+        src = "MEASURED_PEAKS.json hbm_gbs (measured copy)"
+    except (OSError, ValueError, KeyError):
+        peak, src = 6800.0, "fallback 6.8 TB/s"
+    byts = STAGE_BYTES_PER_ION * w.n_total * attempts
+    achieved = byts / (st["stage_ms"] * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "bytes_per_ion_attempt": STAGE_BYTES_PER_ION,
+            "launches": st["stage_launches"], "ms": st["stage_ms"], "peak_source": src,
+            "note": "per-attempt working set below the 129 MB L2 reads partly from L2"}
+
+
 def run_ours(args, dist: Dist):
     import torch
     from simbuca_gb300 import abi, configs
@@ -244,6 +269,7 @@ def run_ours(args, dist: Dist):
         kt_ms.append(ctx.timer_stop())
     ctx.sync()
     kt = ctx.kernel_timing()
+    st = ctx.stage_timing()
     ctx.set_kernel_timing(False)
     kt_total_ms = sum(kt_ms)
     kt_attempts = sum((a["steps"] + a["rejects"]) - (b["steps"] + b["rejects"])
@@ -344,6 +370,7 @@ def run_ours(args, dist: Dist):
                      "coulomb_share_of_step": kt["coulomb_ms"] / kt_total_ms if kt_total_ms else None,
                      "timing_pass": {"steps": args.steps, "attempts": int(kt_attempts),
                                      "ms": kt_total_ms}},
+        "stage_roofline": stage_roofline(args, w, st, kt_attempts),
         "peaks_measured": {k: v / 1e3 for k, v in peaks.items()},
         "clocks": clk,
     }

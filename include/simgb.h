@@ -200,6 +200,9 @@ int sg_batch_set_t_end(sg_ctx* ctx, int cloud, double t_end);
 int sg_set_kernel_timing(sg_ctx* ctx, int on);
 int sg_kernel_timing(sg_ctx* ctx, double* coulomb_ms, int64_t* coulomb_launches,
                      double* coulomb_interactions);
+/* The O(N) kernels of the attempts run with kernel timing on (stage combines, control,
+ * commit; graph-replayed attempts only): summed milliseconds and launches. */
+int sg_stage_timing(sg_ctx* ctx, double* ms, int64_t* launches);
 /* FP32c conditioning fix-ups (ions whose dominant pairs were re-evaluated in FP64 by
  * the reduction kernel) since the last call; resets the count. */
 int sg_fixup_count(sg_ctx* ctx, int64_t* count);

@@ -95,7 +95,8 @@ EXPORTED = [
     "sg_batch_create", "sg_batch_upload",
     "sg_batch_set_state", "sg_batch_download", "sg_batch_attempts", "sg_dp45_step",
     "sg_batch_run", "sg_batch_info", "sg_batch_set_field", "sg_batch_set_t_end",
-    "sg_set_kernel_timing", "sg_kernel_timing", "sg_fixup_count", "sg_set_coulomb_variant",
+    "sg_set_kernel_timing", "sg_kernel_timing", "sg_stage_timing", "sg_fixup_count",
+    "sg_set_coulomb_variant",
     "sg_batch_variant", "sg_init_cloud", "sg_batch_set_recorder", "sg_batch_record_now",
     "sg_batch_records", "sg_batch_read_records", "sg_batch_write_text",
     "sg_batch_set_operations", "sg_batch_operation_index",
@@ -141,6 +142,7 @@ def _declare(L):
     L.sg_batch_set_t_end.argtypes = [_vp, ctypes.c_int, ctypes.c_double]
     L.sg_set_kernel_timing.argtypes = [_vp, ctypes.c_int]
     L.sg_kernel_timing.argtypes = [_vp, _dp, ctypes.POINTER(ctypes.c_int64), _dp]
+    L.sg_stage_timing.argtypes = [_vp, _dp, ctypes.POINTER(ctypes.c_int64)]
     L.sg_set_use_graph.argtypes = [_vp, ctypes.c_int]
     L.sg_fixup_count.argtypes = [_vp, ctypes.POINTER(ctypes.c_int64)]
     L.sg_set_coulomb_variant.argtypes = [_vp, ctypes.c_int]

@@ -99,6 +99,14 @@ class Context:
                                        ctypes.byref(inter)), "sg_kernel_timing")
         return {"coulomb_ms": ms.value, "coulomb_launches": n.value, "interactions": inter.value}
 
+    def stage_timing(self):
+        """Milliseconds and launches of the O(N) kernels timed since kernel timing was
+        switched on (graph-replayed attempts)."""
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        check(self._L.sg_stage_timing(self._h, ctypes.byref(ms), ctypes.byref(n)),
+              "sg_stage_timing")
+        return {"stage_ms": ms.value, "stage_launches": n.value}
+
     def fixup_count(self) -> int:
         c = ctypes.c_int64()
         check(self._L.sg_fixup_count(self._h, ctypes.byref(c)), "sg_fixup_count")

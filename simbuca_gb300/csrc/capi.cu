@@ -87,6 +87,9 @@ struct TimedLaunch {
 
 }  // namespace
 
+// O(N) kernels of one attempt timed by the kernel-timing graph (at most)
+constexpr int kStageMarks = 12;
+
 struct sg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -106,6 +109,12 @@ struct sg_ctx {
     cudaGraphExec_t graph_timed = nullptr;
     cudaEvent_t gev[16] = {nullptr};
     int capture_events = -1;  // next event pair while capturing the timed graph, else -1
+    // the same for the O(N) kernels of an attempt (stages, control, commit)
+    cudaEvent_t sev[2 * kStageMarks] = {nullptr};
+    int capture_stage = -1;
+    int stage_pairs = 0;  // pairs recorded by the timed graph
+    double stage_ms = 0.0;
+    long long stage_launches = 0;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     int* herr = nullptr;  // pinned host word for the device error word
     float* probe_sink = nullptr;
@@ -651,36 +660,55 @@ double active_interactions(Problem& P) {
     return s;
 }
 
+// External event pair around an O(N) kernel while the timed graph is being captured.
+int stage_mark(sg_ctx* ctx, bool end) {
+    const int k = ctx->capture_stage;
+    if (k < 0 || k >= kStageMarks) return SG_OK;
+    CK(cudaEventRecordWithFlags(ctx->sev[2 * k + (end ? 1 : 0)], ctx->stream,
+                                cudaEventRecordExternal));
+    if (end) ctx->capture_stage = k + 1;
+    return SG_OK;
+}
+
+#define STAGE_TIMED(call)                          \
+    do {                                           \
+        int s_ = stage_mark(ctx, false);           \
+        if (s_ != SG_OK) return s_;                \
+        CK(call);                                  \
+        s_ = stage_mark(ctx, true);                \
+        if (s_ != SG_OK) return s_;                \
+    } while (0)
+
 // One Dormand-Prince attempt of every active cloud (bin/ode.cpp:61-218, 426-494).
 int enqueue_attempt(sg_ctx* ctx, Problem& P) {
     SgDpArgs a = dp_args(P);
     const double inter = ctx->timing ? active_interactions(P) : 0.0;
     if (P.method == 1) {
         // Gear: predict, one force evaluation at the predicted state, correct
-        CK(sg_gear_stage(a, 0, P.n_rows, ctx->stream));
+        STAGE_TIMED(sg_gear_stage(a, 0, P.n_rows, ctx->stream));
         int st = launch_coulomb(ctx, P, true, inter, P.coulS);
         if (st != SG_OK) return st;
-        CK(sg_gear_stage(a, 1, P.n_rows, ctx->stream));
+        STAGE_TIMED(sg_gear_stage(a, 1, P.n_rows, ctx->stream));
     } else if (P.method == 4) {
         // Cash-Karp: the step start is no stage of the previous step, so its Coulomb
         // inputs are rebuilt and all six stages take a Coulomb sum
-        CK(sg_coords_from_state(a, P.qd, P.n_rows, ctx->stream));
+        STAGE_TIMED(sg_coords_from_state(a, P.qd, P.n_rows, ctx->stream));
         for (int s = 1; s <= 6; s++) {
             int st = launch_coulomb(ctx, P, true, inter, P.coulS);
             if (st != SG_OK) return st;
-            CK(sg_ck_stage(a, s, P.n_rows, ctx->stream));
+            STAGE_TIMED(sg_ck_stage(a, s, P.n_rows, ctx->stream));
         }
     } else {
-        CK(sg_dp_stage(a, 1, P.n_rows, ctx->stream));
+        STAGE_TIMED(sg_dp_stage(a, 1, P.n_rows, ctx->stream));
         for (int s = 2; s <= 7; s++) {
             int st = launch_coulomb(ctx, P, true, inter, P.coulS);
             if (st != SG_OK) return st;
-            CK(sg_dp_stage(a, s, P.n_rows, ctx->stream));
+            STAGE_TIMED(sg_dp_stage(a, s, P.n_rows, ctx->stream));
         }
     }
-    CK(sg_dp_control(P.dc, P.dctrl, P.err_part, P.y, P.n_clouds, P.flags + 1, P.dops,
-                     ctx->stream));
-    CK(sg_dp_commit(a, P.n_rows, ctx->stream));
+    STAGE_TIMED(sg_dp_control(P.dc, P.dctrl, P.err_part, P.y, P.n_clouds, P.flags + 1, P.dops,
+                              ctx->stream));
+    STAGE_TIMED(sg_dp_commit(a, P.n_rows, ctx->stream));
     if (P.rec_cap > 0) CK(sg_record(rec_args(P), P.n_rows, P.n_clouds, ctx->stream));
     if (P.n_dis > 0)
         CK(sg_dissociate(rec_args(P), P.pmass, P.spec0, P.pmass0, P.n_rows, ctx->stream));
@@ -718,13 +746,19 @@ int drop_graph(sg_ctx* ctx) {
 
 int capture_attempt(sg_ctx* ctx, Problem& P, bool timed, cudaGraphExec_t* out) {
     cudaGraph_t g = nullptr;
-    if (timed)
+    if (timed) {
         for (int k = 0; k < 12; k++)
             if (!ctx->gev[k]) CK(cudaEventCreate(&ctx->gev[k]));
+        for (int k = 0; k < 2 * kStageMarks; k++)
+            if (!ctx->sev[k]) CK(cudaEventCreate(&ctx->sev[k]));
+    }
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     ctx->capture_events = timed ? 0 : -1;
+    ctx->capture_stage = timed ? 0 : -1;
     int st = enqueue_attempt(ctx, P);
     ctx->capture_events = -1;
+    if (timed) ctx->stage_pairs = ctx->capture_stage;
+    ctx->capture_stage = -1;
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (st != SG_OK) {
         if (g) cudaGraphDestroy(g);
@@ -744,7 +778,8 @@ int run_attempts(sg_ctx* ctx, Problem& P, int n) {
             int st = capture_attempt(ctx, P, true, &ctx->graph_timed);
             if (st != SG_OK) return st;
         }
-        const int pairs = P.any_coulomb ? 6 : 0;
+        const int pairs = P.any_coulomb ? (P.method == 1 ? 1 : 6) : 0;
+        const int spairs = ctx->stage_pairs;
         for (int i = 0; i < n; i++) {
             const double inter = active_interactions(P);
             CK(cudaGraphLaunch(ctx->graph_timed, ctx->stream));
@@ -756,6 +791,15 @@ int run_attempts(sg_ctx* ctx, Problem& P, int n) {
                     ctx->coul_ms += ms;
                     ctx->coul_launches += 1;
                     ctx->coul_inter += inter;
+                }
+            }
+            if (spairs) {
+                CK(cudaEventSynchronize(ctx->sev[2 * spairs - 1]));
+                for (int k = 0; k < spairs; k++) {
+                    float ms = 0.f;
+                    CK(cudaEventElapsedTime(&ms, ctx->sev[2 * k], ctx->sev[2 * k + 1]));
+                    ctx->stage_ms += ms;
+                    ctx->stage_launches += 1;
                 }
             }
         }
@@ -971,6 +1015,8 @@ int sg_destroy(sg_ctx* ctx) {
     free_problem(ctx->solo);
     for (cudaEvent_t e : ctx->free_ev) cudaEventDestroy(e);
     for (cudaEvent_t e : ctx->gev)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->sev)
         if (e) cudaEventDestroy(e);
     cudaEventDestroy(ctx->t0);
     cudaEventDestroy(ctx->t1);
@@ -1615,6 +1661,16 @@ int sg_set_kernel_timing(sg_ctx* ctx, int on) {
     ctx->coul_ms = 0.0;
     ctx->coul_inter = 0.0;
     ctx->coul_launches = 0;
+    ctx->stage_ms = 0.0;
+    ctx->stage_launches = 0;
+    return SG_OK;
+}
+
+int sg_stage_timing(sg_ctx* ctx, double* ms, int64_t* launches) {
+    if (!ctx) return SG_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ms) *ms = ctx->stage_ms;
+    if (launches) *launches = ctx->stage_launches;
     return SG_OK;
 }
 

@@ -116,6 +116,7 @@ __global__ void __launch_bounds__(SG_ROWS) dp_stage_kernel(DpArgs a) {
     const double h = cs.h;
     const bool frozen = (cl.fp.flags & SG_F_FROZEN_T) != 0;
     const double ts = frozen ? cs.t : cs.t + c_c[S] * h;
+    const SgFieldCoef fk = sg_field_coef_block(cl.fp, ts);
 
     double acc2 = 0.0;
     float hu[3] = {0.f, 0.f, 0.f};
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(SG_ROWS) dp_stage_kernel(DpArgs a) {
             }
         }
         double fx, fy, fz;
-        sg_field_accel(cl.fp, ts, a.qm[i], px, py, pz, vx, vy, vz, fx, fy, fz);
+        sg_field_apply(cl.fp, fk, a.qm[i], px, py, pz, vx, vy, vz, fx, fy, fz);
         const double kqi = a.kq[i];
         double* kS = a.k + (size_t)(S - 1) * 6 * N;
         kS[i] = vx;
@@ -234,6 +235,7 @@ __global__ void __launch_bounds__(SG_ROWS) ck_stage_kernel(DpArgs a) {
     const double h = cs.h;
     const bool frozen = (cl.fp.flags & SG_F_FROZEN_T) != 0;
     const double ts = frozen ? cs.t : cs.t + c_ck_c[S] * h;
+    const SgFieldCoef fk = sg_field_coef_block(cl.fp, ts);
     double acc2 = 0.0;
     float hu[3] = {0.f, 0.f, 0.f};
     if (active) {
@@ -247,7 +249,7 @@ __global__ void __launch_bounds__(SG_ROWS) ck_stage_kernel(DpArgs a) {
             cz = a.coulS[2 * N + i];
         }
         double fx, fy, fz;
-        sg_field_accel(cl.fp, ts, a.qm[i], px, py, pz, vx, vy, vz, fx, fy, fz);
+        sg_field_apply(cl.fp, fk, a.qm[i], px, py, pz, vx, vy, vz, fx, fy, fz);
         const double kqi = a.kq[i];
         double* kS = a.k + (size_t)(S - 1) * 6 * N;
         kS[i] = vx;

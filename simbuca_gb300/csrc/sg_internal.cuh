@@ -164,40 +164,71 @@ struct SgProposerState {
 
 // ---- field terms ---------------------------------------------------------------
 // Paul/TOF follow bin/force.cpp:40-44,70-80; the Penning trap, the RF excitations and
-// friction follow the formulas of include/simgb.h.
-__device__ __forceinline__ void sg_field_accel(const sg_field_params& fp, double t, double qm,
-                                               double x, double y, double z, double vx,
-                                               double vy, double vz, double& ax, double& ay,
-                                               double& az) {
+// friction follow the formulas of include/simgb.h.  The factors that depend only on
+// the cloud and the time (divisions by trap dimensions, the drive cosines) are one
+// SgFieldCoef, computed once per block by the stage kernels: GB300 runs FP64 at a small
+// fraction of its FP32 rate, and a division plus a cosine per ion and stage made the
+// O(N) kernels FP64-bound.  The per-ion arithmetic is unchanged.
+struct SgFieldCoef {
+    double paul_x, paul_y, paul_z;  // (kVdc/z0^2 -+ Vrf cos(w t)/r0^2), -2 kVdc/z0^2
+    double kp;                      // V0 / (2 d0^2)
+    double gq;                      // quadrupole factor at t (0 when off)
+    double ed;                      // dipole field at t (0 when off)
+    int quad_on, dip_on;
+};
+
+__device__ __forceinline__ SgFieldCoef sg_field_coef(const sg_field_params& fp, double t) {
+    SgFieldCoef k;
+    const uint32_t f = fp.flags;
+    k.paul_x = k.paul_y = k.paul_z = 0.0;
+    k.kp = k.gq = k.ed = 0.0;
+    k.quad_on = k.dip_on = 0;
+    if (f & SG_F_PAUL) {
+        const double kVdc = fp.kappa * fp.Vdc;
+        const double r02 = fp.r0 * fp.r0, z02 = fp.z0 * fp.z0;
+        const double c = fp.Vrf * cos(fp.freq_rf * 2 * SG_PI * t) / r02;
+        k.paul_x = kVdc / z02 - c;
+        k.paul_y = kVdc / z02 + c;
+        k.paul_z = -2.0 * kVdc / z02;
+    }
+    if (f & SG_F_PENNING) k.kp = fp.V0 / (2.0 * fp.d0 * fp.d0);
+    if ((f & SG_F_QUAD) && t >= fp.tq_on && t < fp.tq_off) {
+        k.quad_on = 1;
+        k.gq = (2.0 * fp.Uq / (fp.r_el * fp.r_el)) * cos(2.0 * SG_PI * fp.nu_q * t + fp.phi_q);
+    }
+    if ((f & SG_F_DIPOLE) && t >= fp.td_on && t < fp.td_off) {
+        k.dip_on = 1;
+        k.ed = (fp.Ud / fp.r_el) * cos(2.0 * SG_PI * fp.nu_d * t + fp.phi_d);
+    }
+    return k;
+}
+
+__device__ __forceinline__ void sg_field_apply(const sg_field_params& fp, const SgFieldCoef& k,
+                                               double qm, double x, double y, double z,
+                                               double vx, double vy, double vz, double& ax,
+                                               double& ay, double& az) {
     const uint32_t f = fp.flags;
     ax = 0.0;
     ay = 0.0;
     az = 0.0;
     if (f & SG_F_PAUL) {
-        const double kVdc = fp.kappa * fp.Vdc;
-        const double r02 = fp.r0 * fp.r0, z02 = fp.z0 * fp.z0;
-        const double c = fp.Vrf * cos(fp.freq_rf * 2 * SG_PI * t) / r02;
-        ax += qm * (kVdc / z02 - c) * x;
-        ay += qm * (kVdc / z02 + c) * y;
-        az += qm * (-2.0 * kVdc / z02) * z;
+        ax += qm * k.paul_x * x;
+        ay += qm * k.paul_y * y;
+        az += qm * k.paul_z * z;
     }
     if (f & SG_F_TOF) ax += qm * fp.E_kick;
     if (f & (SG_F_PENNING | SG_F_QUAD | SG_F_DIPOLE)) {
         double ex = 0.0, ey = 0.0, ez = 0.0;
         if (f & SG_F_PENNING) {
-            const double kp = fp.V0 / (2.0 * fp.d0 * fp.d0);
-            ex = kp * x + fp.B * vy;
-            ey = kp * y - fp.B * vx;
-            ez = -2.0 * kp * z;
+            ex = k.kp * x + fp.B * vy;
+            ey = k.kp * y - fp.B * vx;
+            ez = -2.0 * k.kp * z;
         }
-        if ((f & SG_F_QUAD) && t >= fp.tq_on && t < fp.tq_off) {
-            const double g = (2.0 * fp.Uq / (fp.r_el * fp.r_el)) *
-                             cos(2.0 * SG_PI * fp.nu_q * t + fp.phi_q);
-            ex += g * y;
-            ey += g * x;
+        if (k.quad_on) {
+            ex += k.gq * y;
+            ey += k.gq * x;
         }
-        if ((f & SG_F_DIPOLE) && t >= fp.td_on && t < fp.td_off)
-            ex += (fp.Ud / fp.r_el) * cos(2.0 * SG_PI * fp.nu_d * t + fp.phi_d);
+        if (k.dip_on) ex += k.ed;
         ax += qm * ex;
         ay += qm * ey;
         az += qm * ez;
@@ -207,6 +238,22 @@ __device__ __forceinline__ void sg_field_accel(const sg_field_params& fp, double
         ay -= fp.delta * vy;
         az -= fp.delta * vz;
     }
+}
+
+__device__ __forceinline__ void sg_field_accel(const sg_field_params& fp, double t, double qm,
+                                               double x, double y, double z, double vx,
+                                               double vy, double vz, double& ax, double& ay,
+                                               double& az) {
+    sg_field_apply(fp, sg_field_coef(fp, t), qm, x, y, z, vx, vy, vz, ax, ay, az);
+}
+
+// The block's field coefficients at time t, computed by thread 0 (every thread of the
+// block must call this: it synchronises the block).
+__device__ __forceinline__ SgFieldCoef sg_field_coef_block(const sg_field_params& fp, double t) {
+    __shared__ SgFieldCoef sk;
+    if (threadIdx.x == 0) sk = sg_field_coef(fp, t);
+    __syncthreads();
+    return sk;
 }
 
 // ---- Dormand-Prince 5(4) tableau (bin/ode.cpp:76-86) ------------------------------
