@@ -173,7 +173,7 @@ struct SgFieldCoef {
     double paul_x, paul_y, paul_z;  // (kVdc/z0^2 -+ Vrf cos(w t)/r0^2), -2 kVdc/z0^2
     double kp;                      // V0 / (2 d0^2)
     double gq;                      // quadrupole factor at t (0 when off)
-    double ed;                      // dipole field at t (0 when off)
+    double ed_a, ed_c;              // dipole field at t = ed_a * ed_c: Ud / r_el, cosine
     int quad_on, dip_on;
 };
 
@@ -181,7 +181,7 @@ __device__ __forceinline__ SgFieldCoef sg_field_coef(const sg_field_params& fp, 
     SgFieldCoef k;
     const uint32_t f = fp.flags;
     k.paul_x = k.paul_y = k.paul_z = 0.0;
-    k.kp = k.gq = k.ed = 0.0;
+    k.kp = k.gq = k.ed_a = k.ed_c = 0.0;
     k.quad_on = k.dip_on = 0;
     if (f & SG_F_PAUL) {
         const double kVdc = fp.kappa * fp.Vdc;
@@ -198,7 +198,9 @@ __device__ __forceinline__ SgFieldCoef sg_field_coef(const sg_field_params& fp, 
     }
     if ((f & SG_F_DIPOLE) && t >= fp.td_on && t < fp.td_off) {
         k.dip_on = 1;
-        k.ed = (fp.Ud / fp.r_el) * cos(2.0 * SG_PI * fp.nu_d * t + fp.phi_d);
+        // kept as two factors: the per-ion sum takes their product in one rounding
+        k.ed_a = fp.Ud / fp.r_el;
+        k.ed_c = cos(2.0 * SG_PI * fp.nu_d * t + fp.phi_d);
     }
     return k;
 }
@@ -228,7 +230,7 @@ __device__ __forceinline__ void sg_field_apply(const sg_field_params& fp, const 
             ex += k.gq * y;
             ey += k.gq * x;
         }
-        if (k.dip_on) ex += k.ed;
+        if (k.dip_on) ex += k.ed_a * k.ed_c;
         ax += qm * ex;
         ay += qm * ey;
         az += qm * ez;
