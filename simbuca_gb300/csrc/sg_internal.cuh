@@ -173,16 +173,17 @@ struct SgFieldCoef {
     double paul_x, paul_y, paul_z;  // (kVdc/z0^2 -+ Vrf cos(w t)/r0^2), -2 kVdc/z0^2
     double kp;                      // V0 / (2 d0^2)
     double gq;                      // quadrupole factor at t (0 when off)
-    double ed_a, ed_c;              // dipole field at t = ed_a * ed_c: Ud / r_el, cosine
-    int quad_on, dip_on;
+    double gd;                      // dipole field at t (0 when off)
 };
 
+// Products and sums below are rounded one operation at a time, in the order of the
+// oracle's restatement (compiled without contraction), so that the FP64 path's field
+// terms are the oracle's to the last bit; only the cosines may differ by an ulp.
 __device__ __forceinline__ SgFieldCoef sg_field_coef(const sg_field_params& fp, double t) {
     SgFieldCoef k;
     const uint32_t f = fp.flags;
     k.paul_x = k.paul_y = k.paul_z = 0.0;
-    k.kp = k.gq = k.ed_a = k.ed_c = 0.0;
-    k.quad_on = k.dip_on = 0;
+    k.kp = k.gq = k.gd = 0.0;
     if (f & SG_F_PAUL) {
         const double kVdc = fp.kappa * fp.Vdc;
         const double r02 = fp.r0 * fp.r0, z02 = fp.z0 * fp.z0;
@@ -192,16 +193,12 @@ __device__ __forceinline__ SgFieldCoef sg_field_coef(const sg_field_params& fp, 
         k.paul_z = -2.0 * kVdc / z02;
     }
     if (f & SG_F_PENNING) k.kp = fp.V0 / (2.0 * fp.d0 * fp.d0);
-    if ((f & SG_F_QUAD) && t >= fp.tq_on && t < fp.tq_off) {
-        k.quad_on = 1;
-        k.gq = (2.0 * fp.Uq / (fp.r_el * fp.r_el)) * cos(2.0 * SG_PI * fp.nu_q * t + fp.phi_q);
-    }
-    if ((f & SG_F_DIPOLE) && t >= fp.td_on && t < fp.td_off) {
-        k.dip_on = 1;
-        // kept as two factors: the per-ion sum takes their product in one rounding
-        k.ed_a = fp.Ud / fp.r_el;
-        k.ed_c = cos(2.0 * SG_PI * fp.nu_d * t + fp.phi_d);
-    }
+    if ((f & SG_F_QUAD) && t >= fp.tq_on && t < fp.tq_off)
+        k.gq = __dmul_rn(2.0 * fp.Uq / (fp.r_el * fp.r_el),
+                         cos(__dadd_rn(__dmul_rn(2.0 * SG_PI * fp.nu_q, t), fp.phi_q)));
+    if ((f & SG_F_DIPOLE) && t >= fp.td_on && t < fp.td_off)
+        k.gd = __dmul_rn(fp.Ud / fp.r_el,
+                         cos(__dadd_rn(__dmul_rn(2.0 * SG_PI * fp.nu_d, t), fp.phi_d)));
     return k;
 }
 
@@ -214,31 +211,28 @@ __device__ __forceinline__ void sg_field_apply(const sg_field_params& fp, const 
     ay = 0.0;
     az = 0.0;
     if (f & SG_F_PAUL) {
-        ax += qm * k.paul_x * x;
-        ay += qm * k.paul_y * y;
-        az += qm * k.paul_z * z;
+        ax = __dmul_rn(__dmul_rn(qm, k.paul_x), x);
+        ay = __dmul_rn(__dmul_rn(qm, k.paul_y), y);
+        az = __dmul_rn(__dmul_rn(qm, k.paul_z), z);
     }
-    if (f & SG_F_TOF) ax += qm * fp.E_kick;
+    if (f & SG_F_TOF) ax = __dadd_rn(ax, __dmul_rn(qm, fp.E_kick));
     if (f & (SG_F_PENNING | SG_F_QUAD | SG_F_DIPOLE)) {
         double ex = 0.0, ey = 0.0, ez = 0.0;
         if (f & SG_F_PENNING) {
-            ex = k.kp * x + fp.B * vy;
-            ey = k.kp * y - fp.B * vx;
-            ez = -2.0 * k.kp * z;
+            ex = __dadd_rn(__dmul_rn(k.kp, x), __dmul_rn(fp.B, vy));
+            ey = __dsub_rn(__dmul_rn(k.kp, y), __dmul_rn(fp.B, vx));
+            ez = __dmul_rn(__dmul_rn(-2.0, k.kp), z);
         }
-        if (k.quad_on) {
-            ex += k.gq * y;
-            ey += k.gq * x;
-        }
-        if (k.dip_on) ex += k.ed_a * k.ed_c;
-        ax += qm * ex;
-        ay += qm * ey;
-        az += qm * ez;
+        ex = __dadd_rn(ex, __dadd_rn(__dmul_rn(k.gq, y), k.gd));
+        ey = __dadd_rn(ey, __dmul_rn(k.gq, x));
+        ax = __dadd_rn(ax, __dmul_rn(qm, ex));
+        ay = __dadd_rn(ay, __dmul_rn(qm, ey));
+        az = __dadd_rn(az, __dmul_rn(qm, ez));
     }
     if (f & SG_F_FRICTION) {
-        ax -= fp.delta * vx;
-        ay -= fp.delta * vy;
-        az -= fp.delta * vz;
+        ax = __dsub_rn(ax, __dmul_rn(fp.delta, vx));
+        ay = __dsub_rn(ay, __dmul_rn(fp.delta, vy));
+        az = __dsub_rn(az, __dmul_rn(fp.delta, vz));
     }
 }
 

@@ -212,7 +212,11 @@ def test_penning_drive_vs_oracle(ctx, prec):
     ho = hist[hist[:, 3] == 1][:, 1]
     if prec == SG_PREC_FP64:
         assert last[0]["steps"] == cr.steps
-        np.testing.assert_allclose(hs[0][:20], ho[:20], rtol=1e-6)
+        # The first step (h0 = 1 ns) has an embedded error near the rounding level of
+        # the stage derivatives, so the second step size follows the last bits of the
+        # Coulomb sums, which the device adds in another order: 1e-5 there, 1e-6 after.
+        np.testing.assert_allclose(hs[0][:2], ho[:2], rtol=1e-5)
+        np.testing.assert_allclose(hs[0][2:20], ho[2:20], rtol=1e-6)
     else:
         assert abs(last[0]["steps"] - cr.steps) <= max(2, cr.steps // 10)
         np.testing.assert_allclose(np.mean(hs[0][3:]), np.mean(ho[3:]), rtol=0.05)
