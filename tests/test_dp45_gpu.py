@@ -330,3 +330,26 @@ def test_kernel_timing_in_graph_and_direct(ctx):
         assert kt["coulomb_launches"] == 6 * attempts
         assert kt["coulomb_ms"] > 0 and kt["interactions"] == 6 * attempts * 700 * 699
     ctx.set_use_graph(True)
+
+
+@pytest.mark.parametrize("method,coul,stages", [(5, 6, 9), (4, 6, 9), (1, 1, 4)])
+def test_kernel_timing_counts(ctx, method, coul, stages):
+    """Kernel timing of graph-replayed attempts: one event pair per Coulomb launch and per
+    O(N) launch (stages, control, commit) for each integrator, all with positive times."""
+    w = configs.penning_1k(n=600, seed=31)
+    c = w.clouds[0]
+    fp = configs.penning_field(delta=1e3)
+    b = one_cloud(ctx, c.pos, c.vel, c.mass, c.charge, fp, 1e-9, 1e-15, 2e-9, 1.0,
+                  SG_PREC_FP32C, adaptive=(method != 1), method=method)
+    b.attempts(2)
+    ctx.set_kernel_timing(True)
+    try:
+        b.attempts(5)
+        kt = ctx.kernel_timing()
+        st = ctx.stage_timing()
+    finally:
+        ctx.set_kernel_timing(False)
+    assert kt["coulomb_launches"] == 5 * coul and kt["coulomb_ms"] > 0
+    assert kt["interactions"] == pytest.approx(5 * coul * 600 * 599)
+    assert st["stage_launches"] == 5 * stages and st["stage_ms"] > 0
+    assert b.info()[0]["status"] == 0
