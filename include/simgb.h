@@ -38,7 +38,8 @@ enum {
     SG_NO_DEVICE = 6,        /* no usable CUDA device                                  */
     SG_TOO_MANY_REJECTS = 7, /* a step exceeded its reject budget                      */
     SG_NOT_READY = 8,        /* call order violated (e.g. step before upload)          */
-    SG_TOO_LARGE = 9         /* size beyond a fixed capacity                           */
+    SG_TOO_LARGE = 9,        /* size beyond a fixed capacity                           */
+    SG_IO_ERR = 10           /* a file could not be opened, read, written or parsed    */
 };
 
 /* ---- arithmetic of the Coulomb sum ----------------------------------------- */
@@ -350,6 +351,30 @@ int sg_batch_operation_index(sg_ctx* ctx, int* index);
  * pos (m) and vel (m/s) are written AoS [n][3]. */
 int sg_init_cloud(int n, const double* ev_max, int n_ev, uint32_t seed, const double* semiaxis,
                   const double* offset, const double* mass, double* pos, double* vel);
+
+/* ---- state files ----------------------------------------------------------------
+ * Binary state file, for restarts: the 8 bytes "SGSTATE1", uint32 version (1), uint32 n,
+ * double t, then pos [n][3], vel [n][3], mass [n] (f64), charge [n], species [n] (i32),
+ * all little-endian.  species may be NULL (written as 0).  sg_state_info reads the
+ * header; sg_state_load needs cap >= n (SG_TOO_LARGE otherwise).  SG_IO_ERR on a file
+ * that cannot be opened, is truncated or is not a state file. */
+int sg_state_save(const char* path, int n, double t, const double* pos, const double* vel,
+                  const double* mass, const int* charge, const int* species);
+int sg_state_info(const char* path, int* n, double* t);
+int sg_state_load(const char* path, int cap, double* t, double* pos, double* vel, double* mass,
+                  int* charge, int* species);
+
+/* Restart from the reference's particle output (PrintParticles, bin/ioncloud.cpp:85-111:
+ * per ion "ID name t[ms] x y z[mm] vx vy vz[m/s] E[eV]", one block of lines per print
+ * time): the ions of the last print time, in file order.  The reference's own importer
+ * (ImportData, bin/parser.cpp:102) expects other columns and cannot read this output.
+ * Names are looked up in names[0..n_names) for species, mass (kg) and charge.  *n is the
+ * number of ions read (SG_TOO_LARGE if more than cap); SG_BAD_ARG for an unknown name,
+ * SG_IO_ERR for an unreadable or malformed file. */
+int sg_particles_text_last(const char* path, const char* const* names, const double* masses,
+                           const int* charges, int n_names, int cap, int* n, double* t,
+                           int* ids, double* pos, double* vel, double* mass, int* charge,
+                           int* species);
 
 /* ---- drop-in slot of the reference's CUNBODY backend ------------------------
  * Same symbols and argument meaning as the closed library (bin/cunbody.h:11-33):

@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(PKG, "libsimgb.so")
 
 # status codes
 SG_OK, SG_BAD_ARG, SG_CUDA_ERR, SG_H_UNDERFLOW, SG_NONFINITE, SG_TIMEOUT, SG_NO_DEVICE, \
-    SG_TOO_MANY_REJECTS, SG_NOT_READY, SG_TOO_LARGE = range(10)
+    SG_TOO_MANY_REJECTS, SG_NOT_READY, SG_TOO_LARGE, SG_IO_ERR = range(11)
 SG_PREC_FP64, SG_PREC_FP32C = 0, 1
 
 # field flags
@@ -97,7 +97,8 @@ EXPORTED = [
     "sg_batch_run", "sg_batch_info", "sg_batch_set_field", "sg_batch_set_t_end",
     "sg_set_kernel_timing", "sg_kernel_timing", "sg_stage_timing", "sg_fixup_count",
     "sg_set_coulomb_variant",
-    "sg_batch_variant", "sg_init_cloud", "sg_batch_set_recorder", "sg_batch_record_now",
+    "sg_batch_variant", "sg_init_cloud", "sg_state_save", "sg_state_info", "sg_state_load",
+    "sg_particles_text_last", "sg_batch_set_recorder", "sg_batch_record_now",
     "sg_batch_records", "sg_batch_read_records", "sg_batch_write_text",
     "sg_batch_set_operations", "sg_batch_operation_index",
     "sg_set_use_graph",
@@ -160,6 +161,13 @@ def _declare(L):
     L.sg_batch_operation_index.argtypes = [_vp, ctypes.POINTER(ctypes.c_int)]
     L.sg_init_cloud.argtypes = [ctypes.c_int, _dp, ctypes.c_int, ctypes.c_uint32, _dp, _dp, _dp,
                                 _dp, _dp]
+    L.sg_state_save.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_double, _dp, _dp, _dp,
+                                _ip, _ip]
+    L.sg_state_info.argtypes = [ctypes.c_char_p, _ip, _dp]
+    L.sg_state_load.argtypes = [ctypes.c_char_p, ctypes.c_int, _dp, _dp, _dp, _dp, _ip, _ip]
+    L.sg_particles_text_last.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_char_p), _dp,
+                                         _ip, ctypes.c_int, ctypes.c_int, _ip, _dp, _ip, _dp,
+                                         _dp, _dp, _ip, _ip]
     L.sg_timer_start.argtypes = [_vp]
     L.sg_timer_stop.argtypes = [_vp, _dp]
     L.sg_batch_moments.argtypes = [_vp, _dp]

@@ -8,6 +8,7 @@ There is no CPU fallback: every call goes through libsimgb.so.
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
@@ -351,3 +352,56 @@ def init_cloud(n: int, ev_max, seed: int, semiaxis, offset, mass):
     check(L.sg_init_cloud(int(n), dptr(ev), len(ev), int(seed) & 0xFFFFFFFF, dptr(semi),
                           dptr(off), dptr(m), dptr(pos), dptr(vel)), "sg_init_cloud")
     return pos, vel
+
+
+def save_state(path: str, pos, vel, mass, charge, t: float = 0.0, species=None):
+    """Binary restart file through sg_state_save (layout in include/simgb.h)."""
+    L = abi.load()
+    pos, vel = _f64(pos), _f64(vel)
+    mass = np.ascontiguousarray(mass, np.float64)
+    charge = np.ascontiguousarray(charge, np.int32)
+    sp = None if species is None else np.ascontiguousarray(species, np.int32)
+    check(L.sg_state_save(os.fsencode(path), len(mass), float(t), dptr(pos), dptr(vel),
+                          dptr(mass), iptr(charge), iptr(sp) if sp is not None else None),
+          "sg_state_save")
+
+
+def load_state(path: str) -> dict:
+    """A state written by save_state: pos, vel (m, m/s, [n,3]), mass (kg), charge,
+    species, t (s)."""
+    L = abi.load()
+    n, t = ctypes.c_int(0), ctypes.c_double(0.0)
+    check(L.sg_state_info(os.fsencode(path), ctypes.byref(n), ctypes.byref(t)), "sg_state_info")
+    k = n.value
+    pos, vel = np.empty((k, 3)), np.empty((k, 3))
+    mass = np.empty(k)
+    charge, species = np.empty(k, np.int32), np.empty(k, np.int32)
+    check(L.sg_state_load(os.fsencode(path), k, ctypes.byref(t), dptr(pos), dptr(vel),
+                          dptr(mass), iptr(charge), iptr(species)), "sg_state_load")
+    return {"pos": pos, "vel": vel, "mass": mass, "charge": charge, "species": species,
+            "t": t.value}
+
+
+def read_particles_text(path: str, names, masses, charges, cap: int | None = None) -> dict:
+    """The ions of the last print time of the reference's particle output
+    (PrintParticles: "ID name t[ms] x y z[mm] vx vy vz E[eV]"), in file order, through
+    sg_particles_text_last.  names/masses (kg)/charges describe the species."""
+    L = abi.load()
+    enc = [str(x).encode() for x in names]
+    arr = (ctypes.c_char_p * len(enc))(*enc)
+    m = np.ascontiguousarray(masses, np.float64)
+    q = np.ascontiguousarray(charges, np.int32)
+    if cap is None:
+        with open(path, "rb") as f:
+            cap = sum(1 for _ in f)
+    ids = np.empty(cap, np.int32)
+    pos, vel = np.empty((cap, 3)), np.empty((cap, 3))
+    mass, charge, species = np.empty(cap), np.empty(cap, np.int32), np.empty(cap, np.int32)
+    n, t = ctypes.c_int(0), ctypes.c_double(0.0)
+    check(L.sg_particles_text_last(os.fsencode(path), arr, dptr(m), iptr(q), len(enc), int(cap),
+                                   ctypes.byref(n), ctypes.byref(t), iptr(ids), dptr(pos),
+                                   dptr(vel), dptr(mass), iptr(charge), iptr(species)),
+          "sg_particles_text_last")
+    k = n.value
+    return {"ids": ids[:k], "pos": pos[:k], "vel": vel[:k], "mass": mass[:k],
+            "charge": charge[:k], "species": species[:k], "t": t.value}

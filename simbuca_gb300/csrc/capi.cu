@@ -977,6 +977,7 @@ const char* sg_status_string(int s) {
         case SG_TOO_MANY_REJECTS: return "too many rejected attempts";
         case SG_NOT_READY: return "state not uploaded";
         case SG_TOO_LARGE: return "size exceeds the fixed capacity";
+        case SG_IO_ERR: return "file could not be read or written";
         default: return "unknown status";
     }
 }

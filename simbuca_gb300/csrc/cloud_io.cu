@@ -11,6 +11,7 @@
 // writes AoS arrays ready for sg_batch_upload.
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 
 #include "../../include/simgb.h"
@@ -50,4 +51,146 @@ extern "C" int sg_init_cloud(int n, const double* ev_max, int n_ev, uint32_t see
         vel[3 * (size_t)i + 2] = v * std::cos(phi);
     }
     return SG_OK;
+}
+
+// ---- state files ------------------------------------------------------------------
+// Binary restart file (layout in simgb.h).  The host is little-endian on both machines
+// this library is built for (x86-64, aarch64); values are written as their bytes.
+namespace {
+
+const char kStateMagic[8] = {'S', 'G', 'S', 'T', 'A', 'T', 'E', '1'};
+
+struct File {
+    FILE* f;
+    explicit File(FILE* p) : f(p) {}
+    ~File() {
+        if (f) fclose(f);
+    }
+};
+
+bool put(FILE* f, const void* p, size_t bytes) { return bytes == 0 || fwrite(p, 1, bytes, f) == bytes; }
+bool get(FILE* f, void* p, size_t bytes) { return bytes == 0 || fread(p, 1, bytes, f) == bytes; }
+
+int read_header(FILE* f, uint32_t* n, double* t) {
+    char magic[8];
+    uint32_t version = 0;
+    if (!get(f, magic, 8) || memcmp(magic, kStateMagic, 8) != 0) return SG_IO_ERR;
+    if (!get(f, &version, 4) || version != 1) return SG_IO_ERR;
+    if (!get(f, n, 4) || !get(f, t, 8)) return SG_IO_ERR;
+    return SG_OK;
+}
+
+}  // namespace
+
+extern "C" int sg_state_save(const char* path, int n, double t, const double* pos,
+                             const double* vel, const double* mass, const int* charge,
+                             const int* species) {
+    if (!path || n < 0 || (n > 0 && (!pos || !vel || !mass || !charge))) return SG_BAD_ARG;
+    File fl(fopen(path, "wb"));
+    if (!fl.f) return SG_IO_ERR;
+    const uint32_t version = 1, un = (uint32_t)n;
+    bool ok = put(fl.f, kStateMagic, 8) && put(fl.f, &version, 4) && put(fl.f, &un, 4) &&
+              put(fl.f, &t, 8) && put(fl.f, pos, 24 * (size_t)n) &&
+              put(fl.f, vel, 24 * (size_t)n) && put(fl.f, mass, 8 * (size_t)n) &&
+              put(fl.f, charge, 4 * (size_t)n);
+    if (ok && species) {
+        ok = put(fl.f, species, 4 * (size_t)n);
+    } else if (ok) {
+        const int32_t zero = 0;
+        for (int i = 0; ok && i < n; i++) ok = put(fl.f, &zero, 4);
+    }
+    if (fflush(fl.f) != 0) ok = false;
+    return ok ? SG_OK : SG_IO_ERR;
+}
+
+extern "C" int sg_state_info(const char* path, int* n, double* t) {
+    if (!path || !n || !t) return SG_BAD_ARG;
+    File fl(fopen(path, "rb"));
+    if (!fl.f) return SG_IO_ERR;
+    uint32_t un = 0;
+    const int st = read_header(fl.f, &un, t);
+    if (st != SG_OK) return st;
+    if (un > 0x7fffffffu) return SG_IO_ERR;
+    *n = (int)un;
+    return SG_OK;
+}
+
+extern "C" int sg_state_load(const char* path, int cap, double* t, double* pos, double* vel,
+                             double* mass, int* charge, int* species) {
+    if (!path || !t || cap < 0) return SG_BAD_ARG;
+    File fl(fopen(path, "rb"));
+    if (!fl.f) return SG_IO_ERR;
+    uint32_t un = 0;
+    const int st = read_header(fl.f, &un, t);
+    if (st != SG_OK) return st;
+    if (un > (uint32_t)cap) return SG_TOO_LARGE;
+    const size_t n = un;
+    if (n > 0 && (!pos || !vel || !mass || !charge)) return SG_BAD_ARG;
+    bool ok = get(fl.f, pos, 24 * n) && get(fl.f, vel, 24 * n) && get(fl.f, mass, 8 * n) &&
+              get(fl.f, charge, 4 * n);
+    if (ok && species) {
+        ok = get(fl.f, species, 4 * n);
+    } else if (ok) {
+        int32_t skip = 0;
+        for (size_t i = 0; ok && i < n; i++) ok = get(fl.f, &skip, 4);
+    }
+    return ok ? SG_OK : SG_IO_ERR;
+}
+
+// ---- the reference's particle text output -------------------------------------------
+// One line per ion and print time: ID name t[ms] x y z[mm] vx vy vz[m/s] E[eV]
+// (bin/ioncloud.cpp:85-111).  Two passes: the last print time, then its lines.
+extern "C" int sg_particles_text_last(const char* path, const char* const* names,
+                                      const double* masses, const int* charges, int n_names,
+                                      int cap, int* n, double* t, int* ids, double* pos,
+                                      double* vel, double* mass, int* charge, int* species) {
+    if (!path || !names || !masses || !charges || n_names < 1 || cap < 0 || !n || !t)
+        return SG_BAD_ARG;
+    File fl(fopen(path, "r"));
+    if (!fl.f) return SG_IO_ERR;
+    char line[1024], name[256];
+    double t_last = -INFINITY;
+    bool any = false;
+    while (fgets(line, sizeof line, fl.f)) {
+        int id;
+        double tm, v[7];
+        if (line[0] == '\n' || line[0] == '\0' || line[0] == '#') continue;
+        const int got = sscanf(line, "%d %255s %lf %lf %lf %lf %lf %lf %lf %lf", &id, name, &tm,
+                               &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6]);
+        if (got != 10) return SG_IO_ERR;
+        if (!any || tm > t_last) t_last = tm;
+        any = true;
+    }
+    if (!any) return SG_IO_ERR;
+    rewind(fl.f);
+    int k = 0;
+    while (fgets(line, sizeof line, fl.f)) {
+        int id;
+        double tm, v[7];
+        if (line[0] == '\n' || line[0] == '\0' || line[0] == '#') continue;
+        if (sscanf(line, "%d %255s %lf %lf %lf %lf %lf %lf %lf %lf", &id, name, &tm, &v[0], &v[1],
+                   &v[2], &v[3], &v[4], &v[5], &v[6]) != 10)
+            return SG_IO_ERR;
+        if (tm != t_last) continue;
+        int s = -1;
+        for (int q = 0; q < n_names && s < 0; q++)
+            if (names[q] && strcmp(names[q], name) == 0) s = q;
+        if (s < 0) return SG_BAD_ARG;
+        if (k >= cap) {
+            k++;
+            continue;  // count the ions for *n, report SG_TOO_LARGE below
+        }
+        if (ids) ids[k] = id;
+        if (pos)
+            for (int c = 0; c < 3; c++) pos[3 * (size_t)k + c] = v[c] / 1000.0;
+        if (vel)
+            for (int c = 0; c < 3; c++) vel[3 * (size_t)k + c] = v[3 + c];
+        if (mass) mass[k] = masses[s];
+        if (charge) charge[k] = charges[s];
+        if (species) species[k] = s;
+        k++;
+    }
+    *n = k;
+    *t = t_last / 1000.0;
+    return k > cap ? SG_TOO_LARGE : SG_OK;
 }

@@ -135,3 +135,37 @@ def test_write_text_matches_reference(ctx, tmp_path):
             va = np.array([float(x) for x in fa[nfix:]])
             vr = np.array([float(x) for x in fr[nfix:]])
             np.testing.assert_allclose(va, vr, rtol=1.5e-6, atol=1e-300)
+
+
+def test_restart_from_written_text(ctx, tmp_path):
+    """Run, record, write the reference's text output, restart a new batch from its last
+    print time (sg_particles_text_last) and from a binary state file: both restarts hold
+    the recorded state (text: to the 7 printed digits; binary: exactly)."""
+    from simbuca_gb300.api import load_state, read_particles_text, save_state
+    n = 500
+    pos, vel, mass, charge, species = two_species(n, 12)
+    op = configs.ode(1e-9, 1e-15, 1e-9, 0.4e-6)
+    b = Batch(ctx, [n], [configs.penning_field(delta=1e3)], [op], SG_PREC_FP64)
+    b.upload(pos, vel, mass, charge)
+    b.set_recorder(0.1e-6, stride=1, capacity=16, species=species, n_species=2)
+    info, _ = b.run()
+    b.record_now()
+    p_end, v_end = b.download()
+    prefix = str(tmp_path / "run")
+    names = ["Cs133", "Rb87"]
+    b.write_text(0, prefix, names)
+    s = read_particles_text(prefix + "_pAll.txt", names,
+                            [132.905 * oracle.AMU, 86.909 * oracle.AMU], [1, 1])
+    assert len(s["ids"]) == n and np.array_equal(s["species"], species)
+    assert s["t"] == pytest.approx(info[0]["t"], rel=1e-6)
+    np.testing.assert_allclose(s["pos"], p_end, rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(s["vel"], v_end, rtol=1e-6, atol=1e-9)
+    f = str(tmp_path / "state.bin")
+    save_state(f, p_end, v_end, mass, charge, t=info[0]["t"], species=species)
+    st = load_state(f)
+    b2 = Batch(ctx, [n], [configs.penning_field(delta=1e3)],
+               [configs.ode(1e-9, 1e-15, 1e-9, 1.0, t0=st["t"])], SG_PREC_FP64)
+    b2.upload(st["pos"], st["vel"], st["mass"], st["charge"])
+    p2, v2 = b2.download()
+    assert np.array_equal(p2, p_end) and np.array_equal(v2, v_end)
+    assert b2.info()[0]["t"] == info[0]["t"]
