@@ -886,8 +886,11 @@ void ion_constants(const Problem& P, const double* mass, const int* charge,
 // the sorted kernel -- brings the per-ion constants into the same order and rebuilds the
 // Coulomb inputs.  The constants in the caller's order (kq0, qm0, qd0, mass0) must be on
 // the device already.
+// resort: a new ion order (first upload) -- the per-ion constants are gathered into it;
+// otherwise they are already in place (dissociation keeps both orders current).
+// sync: wait for the queued copies (the caller synchronises itself otherwise).
 int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel,
-                 bool resort = true) {
+                 bool resort = true, bool sync = true) {
     const size_t N = (size_t)P.n;
     if (P.sorted && resort) {
         for (int c = 0; c < P.n_clouds; c++)
@@ -900,12 +903,14 @@ int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel,
         CK(cudaMemcpyAsync(P.stage + 3 * N, vel, 3 * N * sizeof(double), cudaMemcpyHostToDevice,
                            ctx->stream));
     CK(sg_aos_to_soa(P.stage, vel ? P.stage + 3 * N : nullptr, P.dperm, P.y, P.n, ctx->stream));
-    CK(sg_gather(P.kq0, P.dperm, P.kq, P.n, ctx->stream));
-    CK(sg_gather(P.qm0, P.dperm, P.qm, P.n, ctx->stream));
-    CK(sg_gather(P.qd0, P.dperm, P.qd, P.n, ctx->stream));
-    CK(sg_gather(P.mass0, P.dperm, P.mass, P.n, ctx->stream));
-    CK(sg_gather_int(P.spec0, P.dperm, P.spec, P.n, ctx->stream));
-    CK(sg_gather(P.pmass0, P.dperm, P.pmass, P.n, ctx->stream));
+    if (resort) {
+        CK(sg_gather(P.kq0, P.dperm, P.kq, P.n, ctx->stream));
+        CK(sg_gather(P.qm0, P.dperm, P.qm, P.n, ctx->stream));
+        CK(sg_gather(P.qd0, P.dperm, P.qd, P.n, ctx->stream));
+        CK(sg_gather(P.mass0, P.dperm, P.mass, P.n, ctx->stream));
+        CK(sg_gather_int(P.spec0, P.dperm, P.spec, P.n, ctx->stream));
+        CK(sg_gather(P.pmass0, P.dperm, P.pmass, P.n, ctx->stream));
+    }
     for (int c = 0; c < P.n_clouds; c++) {
         set_frame(P.hc[c], pos, P.hc[c].off);
         double v2 = 0.0;
@@ -921,7 +926,7 @@ int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel,
     // a new state restarts the Gear history
     if (P.method == 1) CK(sg_gear_init(a, P.dperm, P.n_rows, ctx->stream));
     // the host vectors above are read by queued copies: finish before they go away
-    CK(cudaStreamSynchronize(ctx->stream));
+    if (sync) CK(cudaStreamSynchronize(ctx->stream));
     return SG_OK;
 }
 
@@ -1236,11 +1241,11 @@ int sg_batch_set_state(sg_ctx* ctx, const double* pos, const double* vel) {
     Problem& P = ctx->batch;
     if (!P.uploaded) return SG_NOT_READY;
     CK(cudaSetDevice(ctx->device));
-    // field parameters as the device has them now (a ramp may have moved them)
-    CK(pull_clouds(ctx, P));
+    // field parameters as the device has them now (only an operation sequence moves them)
+    if (!P.hops.empty()) CK(pull_clouds(ctx, P));
     // a continuing run keeps its ion order: the tile bounds are recomputed from the new
     // positions at every stage, so an older k-d order costs some far pairs, never accuracy
-    int st = upload_state(ctx, P, pos, vel, false);
+    int st = upload_state(ctx, P, pos, vel, false, false);
     if (st != SG_OK) return st;
     st = launch_coulomb(ctx, P, true, active_interactions(P), P.coul1);
     if (st != SG_OK) return st;
