@@ -365,8 +365,9 @@ int sg_state_load(const char* path, int cap, double* t, double* pos, double* vel
                   int* charge, int* species);
 
 /* Restart from the reference's particle output (PrintParticles, bin/ioncloud.cpp:85-111:
- * per ion "ID name t[ms] x y z[mm] vx vy vz[m/s] E[eV]", one block of lines per print
- * time): the ions of the last print time, in file order.  The reference's own importer
+ * per ion "ID name t[ms] x y z[mm] vx vy vz[m/s] E[eV]", one block of lines per print,
+ * IDs ascending): the ions of the last print (a print starts where the time changes or
+ * the IDs start over), in file order.  The reference's own importer
  * (ImportData, bin/parser.cpp:102) expects other columns and cannot read this output.
  * Names are looked up in names[0..n_names) for species, mass (kg) and charge.  *n is the
  * number of ions read (SG_TOO_LARGE if more than cap); SG_BAD_ARG for an unknown name,

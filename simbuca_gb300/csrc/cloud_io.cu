@@ -139,7 +139,21 @@ extern "C" int sg_state_load(const char* path, int cap, double* t, double* pos, 
 
 // ---- the reference's particle text output -------------------------------------------
 // One line per ion and print time: ID name t[ms] x y z[mm] vx vy vz[m/s] E[eV]
-// (bin/ioncloud.cpp:85-111).  Two passes: the last print time, then its lines.
+// (bin/ioncloud.cpp:85-111), the ions of a print in ID order.  A print starts where the
+// time changes or the IDs start over; the last one is read.
+namespace {
+
+bool skip_line(const char* line) { return line[0] == '\n' || line[0] == '\0' || line[0] == '#'; }
+
+int parse_particle(const char* line, int* id, char* name, double* tm, double* v) {
+    return sscanf(line, "%d %255s %lf %lf %lf %lf %lf %lf %lf %lf", id, name, tm, &v[0], &v[1],
+                  &v[2], &v[3], &v[4], &v[5], &v[6]) == 10
+               ? SG_OK
+               : SG_IO_ERR;
+}
+
+}  // namespace
+
 extern "C" int sg_particles_text_last(const char* path, const char* const* names,
                                       const double* masses, const int* charges, int n_names,
                                       int cap, int* n, double* t, int* ids, double* pos,
@@ -149,29 +163,30 @@ extern "C" int sg_particles_text_last(const char* path, const char* const* names
     File fl(fopen(path, "r"));
     if (!fl.f) return SG_IO_ERR;
     char line[1024], name[256];
-    double t_last = -INFINITY;
-    bool any = false;
-    while (fgets(line, sizeof line, fl.f)) {
+    long block = -1;
+    double t_block = 0.0, t_prev = 0.0;
+    int id_prev = 0;
+    for (;;) {
+        const long off = ftell(fl.f);
+        if (!fgets(line, sizeof line, fl.f)) break;
+        if (skip_line(line)) continue;
         int id;
         double tm, v[7];
-        if (line[0] == '\n' || line[0] == '\0' || line[0] == '#') continue;
-        const int got = sscanf(line, "%d %255s %lf %lf %lf %lf %lf %lf %lf %lf", &id, name, &tm,
-                               &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6]);
-        if (got != 10) return SG_IO_ERR;
-        if (!any || tm > t_last) t_last = tm;
-        any = true;
+        if (parse_particle(line, &id, name, &tm, v) != SG_OK) return SG_IO_ERR;
+        if (block < 0 || tm != t_prev || id <= id_prev) {
+            block = off;
+            t_block = tm;
+        }
+        t_prev = tm;
+        id_prev = id;
     }
-    if (!any) return SG_IO_ERR;
-    rewind(fl.f);
+    if (block < 0 || fseek(fl.f, block, SEEK_SET) != 0) return SG_IO_ERR;
     int k = 0;
     while (fgets(line, sizeof line, fl.f)) {
+        if (skip_line(line)) continue;
         int id;
         double tm, v[7];
-        if (line[0] == '\n' || line[0] == '\0' || line[0] == '#') continue;
-        if (sscanf(line, "%d %255s %lf %lf %lf %lf %lf %lf %lf %lf", &id, name, &tm, &v[0], &v[1],
-                   &v[2], &v[3], &v[4], &v[5], &v[6]) != 10)
-            return SG_IO_ERR;
-        if (tm != t_last) continue;
+        if (parse_particle(line, &id, name, &tm, v) != SG_OK) return SG_IO_ERR;
         int s = -1;
         for (int q = 0; q < n_names && s < 0; q++)
             if (names[q] && strcmp(names[q], name) == 0) s = q;
@@ -191,6 +206,6 @@ extern "C" int sg_particles_text_last(const char* path, const char* const* names
         k++;
     }
     *n = k;
-    *t = t_last / 1000.0;
+    *t = t_block / 1000.0;
     return k > cap ? SG_TOO_LARGE : SG_OK;
 }

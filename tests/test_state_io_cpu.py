@@ -107,6 +107,11 @@ def test_text_last_snapshot_and_errors(tmp_path):
     write_lines(p, list(early) + list(g["pall"]))
     s = read_particles_text(p, names, masses, [1, 1])
     assert len(s["ids"]) == len(g["pall"]) and s["t"] == pytest.approx(3.7e-6, rel=1e-12)
+    # the same print written twice at the same time: the last one only
+    p2 = str(tmp_path / "dup.txt")
+    write_lines(p2, list(g["pall"]) + list(g["pall"]))
+    s2 = read_particles_text(p2, names, masses, [1, 1])
+    assert len(s2["ids"]) == len(g["pall"]) and np.array_equal(s2["ids"], s["ids"])
     # capacity below the snapshot
     assert "status 9)" in status_of(read_particles_text, p, names, masses, [1, 1], 10)
     # a name missing from the table
