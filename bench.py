@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variant", type=int, default=-1,
-                    help="FP32c Coulomb launch shape (-1 automatic, 0..4 fixed)")
+                    help="FP32c Coulomb launch shape (-1 automatic, 0..16 fixed: sg_set_coulomb_variant)")
     ap.add_argument("--method", type=int, default=5, choices=[4, 5],
                     help="5 Dormand-Prince, 4 Cash-Karp")
     ap.add_argument("--settle", type=int, default=60,
