@@ -1,6 +1,6 @@
 """The learned step-size proposer: collecting step histories, training, evaluation.
 
-    python -m simbuca_gb300.proposer [--out DIR] [--quick]
+    python -m simbuca_gb300.proposer [--out DIR] [--quick] [--eval WORKLOAD --horizon S]
 
 1. collect: run the Penning-trap workloads (1,000 ions; 65,536 ions with drive and
    friction; the 1M-ion spheroid) with the reference's controller and the device-side
@@ -9,11 +9,12 @@
    tolerance exactly.
 2. train: the MLP 16 -> 64 -> 64 -> 1 (BF16 weights, FP32 accumulation) on the GPU
    with the library's own forward, backward and Adam kernels (sg_mlp_train).
-3. evaluate: the 4,096-ion cloud under a dipole drive at nu_minus then a quadrupole
-   drive at nu_c, once with the reference's controller and once with the proposer,
-   from the same state; every attempt is accepted or rejected by the Dormand-Prince
-   error estimate in both.  Reported: rejected-attempt fraction and force evaluations
-   per simulated microsecond.
+3. evaluate: by default the 4,096-ion cloud under a dipole drive at nu_minus then a
+   quadrupole drive at nu_c (--eval names another workload of configs.WORKLOADS, e.g.
+   penning_65k), once with the reference's controller and once with the proposer per
+   safety factor, from the same state; every attempt is accepted or rejected by the
+   Dormand-Prince error estimate in both.  Reported: rejected-attempt fraction, force
+   evaluations per simulated microsecond and simulated microseconds per wall second.
 """
 from __future__ import annotations
 
@@ -87,7 +88,8 @@ def run_controller(ctx: Context, w: configs.Workload, horizon: float, weights=No
             "reject_fraction": s["rejects"] / max(attempts, 1),
             "force_evals": s["force_evals"], "coulomb_evals": s["coulomb_evals"],
             "force_evals_per_sim_us": s["force_evals"] / sim_us, "sim_us": sim_us,
-            "wall_s": wall, "status": s["status"], "mean_h": sim_us * 1e-6 / max(s["steps"], 1)}
+            "wall_s": wall, "sim_us_per_wall_s": sim_us / wall, "status": s["status"],
+            "mean_h": sim_us * 1e-6 / max(s["steps"], 1)}
 
 
 def main():
@@ -96,6 +98,8 @@ def main():
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--horizon", type=float, default=1e-3)
     ap.add_argument("--safety", default="0.75,0.8,0.85,0.9")
+    ap.add_argument("--eval", default="learned_4k", choices=sorted(configs.WORKLOADS))
+    ap.add_argument("--no-fp64-eval", action="store_true")
     a = ap.parse_args()
     ctx = Context(0)
     t0 = time.perf_counter()
@@ -128,12 +132,14 @@ def main():
     # retrain on everything for the deployed weights
     wts, hist = ctx.mlp_train(X, y, w0, iters=300 if a.quick else 4000, batch=256, lr=2e-3)
     np.save(os.path.join(a.out, "proposer_weights.npy"), wts)
-    ev = configs.learned_4k(sim_time=a.horizon)
-    res = {"train_samples": int(len(y)), "train_loss_first": float(hist[0]),
+    ev = (configs.learned_4k(sim_time=a.horizon) if a.eval == "learned_4k"
+          else configs.WORKLOADS[a.eval]())
+    res = {"eval_workload": a.eval, "train_samples": int(len(y)),
+           "train_loss_first": float(hist[0]),
            "train_loss_last": float(hist[-1]), "heldout_mse_mlp": mse_mlp,
            "heldout_mse_controller_rule": mse_ctrl, "horizon_s": a.horizon,
            "reference_controller": run_controller(ctx, ev, a.horizon)}
-    if not a.quick:
+    if not a.quick and not a.no_fp64_eval:
         res["reference_controller_fp64"] = run_controller(ctx, ev, a.horizon,
                                                           precision=abi.SG_PREC_FP64)
     for s in [float(v) for v in a.safety.split(",")]:
