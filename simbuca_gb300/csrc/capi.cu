@@ -185,15 +185,6 @@ void free_problem(Problem& P) {
 
 inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
-// Launch shape for a set of clouds when the context has no explicit choice: the
-// cloud carrying the most pair work decides.  Measured on GB300 (simbuca_gb300/tune.py,
-// Coulomb kernel time per call): one-warp blocks of 32 x 1 ions up to a few thousand ions
-// per cloud (0.022 ms at 1,024 against 0.032 for 64 x 2), 64 x 2 to ~16k (also the
-// better shape for the 512-cloud scan of up to 8,192 ions each); above that the k-d
-// ordered forms with one 128-ion leaf per block, whose far tile pairs take the high
-// parts only: the leaf over four warps for tens of thousands of ions (0.525 vs 0.684 ms
-// at 32,768), the leaf over two warps with 256-ion j-tiles beyond (1.86 vs 2.54 ms at
-// 65,536; 27.9 vs 41.8 ms at 262,144).
 // Thresholds from the launch-shape tuner (simbuca_gb300/tune.py) on GB300: one cloud of
 // up to ~6k ions is latency-bound and runs best as one-warp blocks of 32 ions (11);
 // 64 x 2 blocks (5) to ~24k; the k-d ordered shapes beyond (9; 14 from ~48k).  A batch

@@ -6,8 +6,10 @@
 //   * on an accepted step, appends (features of the step start, h of the previous
 //     step, h and error norm of this step) to the cloud's log and recomputes the
 //     features from the new state;
-//   * when the proposer is on, replaces the controller's next step size by
-//     safety * h * exp(MLP(features)), clamped to [0.2, 10] x h.
+//   * when the proposer is on, replaces the controller's next step size h_c by
+//     safety * h * exp(MLP(features)), clamped to [0.2, 10] x h and to [1/2, 2] x h_c:
+//     the reference's controller stays the fallback, so features outside the training
+//     range (a tiny error norm after tiny steps, say) cannot drive h down step after step.
 // Rejected attempts keep the reference's reject rule (bin/ode.cpp:451-455): every step
 // is still accepted or rejected by the embedded Dormand-Prince error estimate.
 //
@@ -144,7 +146,9 @@ __global__ void proposer_kernel(const SgCloud* __restrict__ clouds, SgCtrl* __re
         const float o = mlp_warp(w, f);
         const double lo = log(0.2), hi = log(10.0);
         const double r = fmin(fmax((double)o, lo), hi);
-        if (lane == 0) ctrl[c].h = safety * cs.h_last * exp(r);
+        const double h_ctrl = cs.h;  // the controller's next step (bin/ode.cpp:443-446)
+        const double h_mlp = safety * cs.h_last * exp(r);
+        if (lane == 0) ctrl[c].h = fmin(fmax(h_mlp, 0.5 * h_ctrl), 2.0 * h_ctrl);
     }
     if (lane == 0) {
         for (int k = 0; k < SG_MLP_IN; k++) nps.feat[k] = f[k];

@@ -67,8 +67,10 @@ def collect(ctx: Context, w: configs.Workload, n_steps: int, precision=abi.SG_PR
 
 
 def run_controller(ctx: Context, w: configs.Workload, horizon: float, weights=None,
-                   safety=0.9, precision=abi.SG_PREC_FP32C, state=None):
-    """Advance one workload by `horizon` seconds; returns the controller's counters."""
+                   safety=0.9, precision=abi.SG_PREC_FP32C, state=None,
+                   max_attempts: int = 100000):
+    """Advance one workload by `horizon` seconds (at most max_attempts attempts; `done`
+    tells whether the horizon was reached); returns the controller's counters."""
     allc = w.concat()
     odes = [configs.ode(o.rtol, o.atol, o.h0, o.t0 + horizon, t0=o.t0) for o in w.odes]
     b = Batch(ctx, w.counts, w.fields, odes, precision)
@@ -79,7 +81,7 @@ def run_controller(ctx: Context, w: configs.Workload, horizon: float, weights=No
     if weights is not None:
         b.set_proposer(weights, safety)
     t0 = time.perf_counter()
-    info, st = b.run()
+    info, st = b.run(max_attempts=max_attempts, raise_on_error=False)
     wall = time.perf_counter() - t0
     s = info[0]
     sim_us = (s["t"] - w.odes[0].t0) * 1e6
@@ -89,6 +91,7 @@ def run_controller(ctx: Context, w: configs.Workload, horizon: float, weights=No
             "force_evals": s["force_evals"], "coulomb_evals": s["coulomb_evals"],
             "force_evals_per_sim_us": s["force_evals"] / sim_us, "sim_us": sim_us,
             "wall_s": wall, "sim_us_per_wall_s": sim_us / wall, "status": s["status"],
+            "done": s["done"],
             "mean_h": sim_us * 1e-6 / max(s["steps"], 1)}
 
 
@@ -100,6 +103,8 @@ def main():
     ap.add_argument("--safety", default="0.75,0.8,0.85,0.9")
     ap.add_argument("--eval", default="learned_4k", choices=sorted(configs.WORKLOADS))
     ap.add_argument("--no-fp64-eval", action="store_true")
+    ap.add_argument("--max-attempts", type=int, default=100000,
+                    help="attempt cap of each evaluation run")
     a = ap.parse_args()
     ctx = Context(0)
     t0 = time.perf_counter()
@@ -138,12 +143,14 @@ def main():
            "train_loss_first": float(hist[0]),
            "train_loss_last": float(hist[-1]), "heldout_mse_mlp": mse_mlp,
            "heldout_mse_controller_rule": mse_ctrl, "horizon_s": a.horizon,
-           "reference_controller": run_controller(ctx, ev, a.horizon)}
+           "reference_controller": run_controller(ctx, ev, a.horizon,
+                                                 max_attempts=a.max_attempts)}
     if not a.quick and not a.no_fp64_eval:
         res["reference_controller_fp64"] = run_controller(ctx, ev, a.horizon,
                                                           precision=abi.SG_PREC_FP64)
     for s in [float(v) for v in a.safety.split(",")]:
-        res[f"mlp_safety_{s}"] = run_controller(ctx, ev, a.horizon, weights=wts, safety=s)
+        res[f"mlp_safety_{s}"] = run_controller(ctx, ev, a.horizon, weights=wts, safety=s,
+                                                max_attempts=a.max_attempts)
     res["collect_and_train_s"] = time.perf_counter() - t0
     print(json.dumps(res, indent=1))
     with open(os.path.join(a.out, "proposer_eval.json"), "w") as f:
