@@ -249,6 +249,11 @@ int sg_mlp_train(sg_ctx* ctx, int n, const float* X, const float* Y, int iters, 
 /* Use the MLP (w != NULL) with step-size safety factor `safety` in (0, 1] for the
  * clouds of the batch, or the reference's controller (w == NULL). */
 int sg_batch_set_proposer(sg_ctx* ctx, const float* w, double safety);
+/* The reference's controller with the safety factor of its accepted-step rule
+ * (0.9, bin/ode.cpp:431,439) replaced by `safety` in (0, 1]: the ablation that separates
+ * the proposer's learning from a plain change of safety.  Replaces the proposer; the
+ * reject rule is unchanged.  sg_batch_set_proposer(ctx, NULL, ...) restores the rule. */
+int sg_batch_set_controller_safety(sg_ctx* ctx, double safety);
 /* Record up to `capacity` accepted steps per cloud: features at the step start and
  * (h_prev, h, err, t_end_of_step). */
 int sg_batch_set_log(sg_ctx* ctx, int capacity);

@@ -105,7 +105,8 @@ EXPORTED = [
     "sg_timer_start",
     "sg_timer_stop", "sg_batch_moments", "sg_probe_peaks",
     "sg_mlp_param_count", "sg_mlp_forward", "sg_mlp_grad", "sg_mlp_train",
-    "sg_batch_set_proposer", "sg_batch_set_log", "sg_batch_read_log",
+    "sg_batch_set_proposer", "sg_batch_set_controller_safety", "sg_batch_set_log",
+    "sg_batch_read_log",
     "cunbody1_force", "cunbody1_force_begin", "cunbody1_force_end",
 ]
 
@@ -178,6 +179,7 @@ def _declare(L):
     L.sg_mlp_train.argtypes = [_vp, ctypes.c_int, _fp, _fp, ctypes.c_int, ctypes.c_int,
                                ctypes.c_float, ctypes.c_uint64, _fp, _fp]
     L.sg_batch_set_proposer.argtypes = [_vp, _fp, ctypes.c_double]
+    L.sg_batch_set_controller_safety.argtypes = [_vp, ctypes.c_double]
     L.sg_batch_set_log.argtypes = [_vp, ctypes.c_int]
     L.sg_batch_read_log.argtypes = [_vp, ctypes.c_int, _fp, _dp, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_int)]

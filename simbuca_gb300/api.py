@@ -314,6 +314,13 @@ class Batch:
             check(self._L.sg_batch_set_proposer(self.ctx.handle, abi.fptr(w), float(safety)),
                   "sg_batch_set_proposer")
 
+    def set_controller_safety(self, safety: float):
+        """The reference's controller with its accepted-step safety factor 0.9 replaced
+        by `safety` (the ablation of the learned proposer)."""
+        self._live()
+        check(self._L.sg_batch_set_controller_safety(self.ctx.handle, float(safety)),
+              "sg_batch_set_controller_safety")
+
     def set_log(self, capacity: int):
         self._live()
         check(self._L.sg_batch_set_log(self.ctx.handle, int(capacity)), "sg_batch_set_log")

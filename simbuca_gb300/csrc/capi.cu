@@ -1942,6 +1942,24 @@ int sg_batch_set_proposer(sg_ctx* ctx, const float* w, double safety) {
     return SG_OK;
 }
 
+int sg_batch_set_controller_safety(sg_ctx* ctx, double safety) {
+    if (!ctx || !(safety > 0.0 && safety <= 1.0)) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    drop_graph(ctx);
+    const bool was_active = P.log_cap > 0 || P.use_mlp;
+    P.use_mlp = 2;                // proposer kernel: h <- (safety / 0.9) h_controller
+    P.safety = safety / 0.9;
+    if (!was_active && P.uploaded) {
+        int st = proposer_reset(ctx, P);
+        if (st != SG_OK) return st;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
 int sg_batch_set_log(sg_ctx* ctx, int capacity) {
     if (!ctx || capacity < 0) return SG_BAD_ARG;
     Problem& P = ctx->batch;

@@ -142,7 +142,10 @@ __global__ void proposer_kernel(const SgCloud* __restrict__ clouds, SgCtrl* __re
     nps.rejects_in_step = 0;
     float f[SG_MLP_IN];
     cloud_features(cl, cs, mom, ps, f);
-    if (use_mlp && !cs.done) {
+    if (use_mlp == 2 && !cs.done) {
+        // the controller's rule with another safety factor (the ablation of the MLP)
+        if (lane == 0) ctrl[c].h = safety * cs.h;
+    } else if (use_mlp && !cs.done) {
         const float o = mlp_warp(w, f);
         const double lo = log(0.2), hi = log(10.0);
         const double r = fmin(fmax((double)o, lo), hi);

@@ -68,7 +68,7 @@ def collect(ctx: Context, w: configs.Workload, n_steps: int, precision=abi.SG_PR
 
 def run_controller(ctx: Context, w: configs.Workload, horizon: float, weights=None,
                    safety=0.9, precision=abi.SG_PREC_FP32C, state=None,
-                   max_attempts: int = 100000):
+                   max_attempts: int = 100000, controller_safety=None):
     """Advance one workload by `horizon` seconds (at most max_attempts attempts; `done`
     tells whether the horizon was reached); returns the controller's counters."""
     allc = w.concat()
@@ -80,6 +80,8 @@ def run_controller(ctx: Context, w: configs.Workload, horizon: float, weights=No
         b.upload(state[0], state[1], allc.mass, allc.charge)
     if weights is not None:
         b.set_proposer(weights, safety)
+    elif controller_safety is not None:
+        b.set_controller_safety(controller_safety)
     t0 = time.perf_counter()
     info, st = b.run(max_attempts=max_attempts, raise_on_error=False)
     wall = time.perf_counter() - t0
@@ -151,6 +153,9 @@ def main():
     for s in [float(v) for v in a.safety.split(",")]:
         res[f"mlp_safety_{s}"] = run_controller(ctx, ev, a.horizon, weights=wts, safety=s,
                                                 max_attempts=a.max_attempts)
+        # the same safety in the reference's own rule: what learning adds beyond it
+        res[f"controller_safety_{s}"] = run_controller(ctx, ev, a.horizon, controller_safety=s,
+                                                       max_attempts=a.max_attempts)
     res["collect_and_train_s"] = time.perf_counter() - t0
     print(json.dumps(res, indent=1))
     with open(os.path.join(a.out, "proposer_eval.json"), "w") as f:

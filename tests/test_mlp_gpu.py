@@ -136,3 +136,16 @@ def test_mlp_beats_the_controller_rule_on_held_out_steps(ctx):
     print(f"held-out MSE: MLP {mse_mlp:.4g}, controller rule {mse_rule:.4g}, "
           f"rule with fitted safety {mse_rule_fit:.4g}")
     assert mse_mlp < min(mse_rule, mse_rule_fit)
+
+
+def test_controller_safety_mode(ctx):
+    """The ablation mode: the reference's rule with its own safety factor 0.9 reproduces
+    the reference controller's run exactly; a smaller factor takes smaller steps."""
+    ev = configs.learned_4k(n=512, seed=13, sim_time=1e-6)
+    ref = proposer.run_controller(ctx, ev, 1e-6)
+    same = proposer.run_controller(ctx, ev, 1e-6, controller_safety=0.9)
+    for k in ("steps", "rejects", "force_evals", "sim_us"):
+        assert same[k] == ref[k], k
+    low = proposer.run_controller(ctx, ev, 1e-6, controller_safety=0.7)
+    assert low["status"] == 0 and low["done"] == 1
+    assert low["mean_h"] < ref["mean_h"]
