@@ -41,7 +41,7 @@ FLOPS_PER_INTERACTION = 20  # convention of bin/nbody_kernel.cu:186-211
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="penning_65k")
@@ -52,6 +52,11 @@ def parse():
                     help="FP32c Coulomb launch shape (-1 automatic, 0..16 fixed: sg_set_coulomb_variant)")
     ap.add_argument("--method", type=int, default=5, choices=[4, 5],
                     help="5 Dormand-Prince, 4 Cash-Karp")
+    ap.add_argument("--proposer", default="on", choices=["on", "off"],
+                    help="learned step-size proposer (shipped weights) or the reference's "
+                         "controller")
+    ap.add_argument("--proposer-safety", type=float, default=None,
+                    help="safety factor of the proposer (default: the trained one's)")
     ap.add_argument("--settle", type=int, default=60,
                     help="at most this many steps to let the step size settle before warm-up")
     return ap.parse_args()
@@ -195,6 +200,17 @@ def stage_roofline(args, w, st, attempts):
             "note": "per-attempt working set below the 129 MB L2 reads partly from L2"}
 
 
+def apply_step_control(args, batch) -> str:
+    """The learned proposer with the shipped weights (every attempt still accepted or
+    rejected by the Dormand-Prince error estimate), or the reference's I-controller."""
+    if args.proposer == "off":
+        return "reference I-controller (bin/ode.cpp:426-457)"
+    from simbuca_gb300 import proposer
+    s = args.proposer_safety if args.proposer_safety is not None else proposer.DEFAULT_SAFETY
+    batch.set_proposer(proposer.default_weights(), s)
+    return f"learned proposer, safety {s}"
+
+
 def run_ours(args, dist: Dist):
     import torch
     from simbuca_gb300 import abi, configs
@@ -212,6 +228,7 @@ def run_ours(args, dist: Dist):
     peaks = ctx.probe_peaks()
     batch = Batch(ctx, w.counts, w.fields, w.odes, prec)
     batch.upload(allc.pos, allc.vel, allc.mass, allc.charge)
+    step_control = apply_step_control(args, batch)
 
     def info0():
         return batch.info()
@@ -346,6 +363,7 @@ def run_ours(args, dist: Dist):
                    "l2": "flushed (256 MB write) between timed steps",
                    "settle_steps": settle_steps, "h_settled": snap[0]["h"],
                    "method": "dormand-prince" if args.method == 5 else "cash-karp",
+                   "step_control": step_control,
                    "coulomb_variant": batch.variant()},
         "e2e": {"value": e2e_val, "unit": "sim-us/wall-s", "h2d_bytes_per_step": bytes_state,
                 "d2h_bytes_per_step": bytes_state, "ms_per_step": sum(e2e_ms) / args.steps,
@@ -356,8 +374,10 @@ def run_ours(args, dist: Dist):
         # per attempt: 7 stages, 6 Coulomb sums, 6 reductions, control, commit, and with
         # FP32c on batches over 8,192 ions the 6 fix-up launches of the conditioning work
         # list (smaller batches fix up inside the reduction); per step one hold reset
-        "gpu_launches": int(attempts * (27 if prec == abi.SG_PREC_FP32C and w.n_total > 8192
-                                        else 21) + args.steps),
+        # (+2 per attempt with the proposer: cloud moments and the MLP)
+        "gpu_launches": int(attempts * ((27 if prec == abi.SG_PREC_FP32C and w.n_total > 8192
+                                         else 21) + (2 if args.proposer == "on" else 0))
+                            + args.steps),
         "fixup_ions_per_coulomb_call": fixups / max(1, 6 * attempts),
         "attempts": int(attempts),
         "interactions_per_s": kt["interactions"] / (kt["coulomb_ms"] * 1e-3) if kt["coulomb_ms"] else None,
@@ -448,6 +468,7 @@ def run_batched(args, dist: Dist):
         ctx.set_coulomb_variant(args.variant)
     batch = Batch(ctx, w.counts, w.fields, w.odes, prec)
     batch.upload(allc.pos, allc.vel, allc.mass, allc.charge)
+    step_control = apply_step_control(args, batch)
     per_step = 10  # attempts of every cloud per bench step (one graph replay each)
 
     def tsum(info):
@@ -490,6 +511,7 @@ def run_batched(args, dist: Dist):
         b1 = Batch(ctx, [n], [w.fields[k]], [op], prec)
         sl = slice(off, off + n)
         b1.upload(snap_pos[sl], snap_vel[sl], allc.mass[sl], allc.charge[sl])
+        apply_step_control(args, b1)
         i0 = b1.info()
         ctx.timer_start()
         b1.attempts(per_step * args.steps)
@@ -507,9 +529,11 @@ def run_batched(args, dist: Dist):
         "data": "synthetic (seeded Gaussian clouds, Maxwell-Boltzmann velocities)",
         "config": {"workload": args.workload, "ions": w.n_total, "clouds": len(w.counts),
                    "precision": args.precision, "attempts_per_step": per_step,
+                   "step_control": step_control,
                    "parallelism": f"replicas x{dist.world}",
                    "l2": "flushed (256 MB write) between timed steps"},
-        "gpu_launches": int((27 if args.precision == "fp32c" else 21) * per_step * args.steps),
+        "gpu_launches": int(((27 if args.precision == "fp32c" else 21)
+                             + (2 if args.proposer == "on" else 0)) * per_step * args.steps),
         "attempts": int(attempts),
         "coulomb_interactions_per_s": sum(
             6.0 * n * (n - 1) * ((a["steps"] + a["rejects"]) - (b["steps"] + b["rejects"]))

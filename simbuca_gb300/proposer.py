@@ -31,6 +31,23 @@ from .api import Batch, Context
 
 NP = 64 * 16 + 64 + 64 * 64 + 64 + 64 + 1
 
+# Weights trained by `python -m simbuca_gb300.proposer --eval penning_65k --horizon 4e-7
+# --max-attempts 1000 --no-fp64-eval --safety 0.8,0.85,0.9` on a GB300 (2,303 accepted
+# steps of the 1,000-ion, 65,536-ion and 1M-ion workloads, 4,000 Adam iterations).
+DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                               "proposer_weights.npy")
+# The safety factor of the trained proposer on the 65,536-ion workload's study: fewest
+# force evaluations per simulated microsecond of 0.8, 0.85 and 0.9.
+DEFAULT_SAFETY = 0.85
+
+
+def default_weights() -> np.ndarray:
+    """The shipped trained weights (FP32 master copy, NP values)."""
+    w = np.load(DEFAULT_WEIGHTS).astype(np.float32)
+    if w.shape != (NP,) or not np.isfinite(w).all():
+        raise RuntimeError(f"{DEFAULT_WEIGHTS}: not a trained proposer")
+    return w
+
 
 def init_weights(seed: int = 0) -> np.ndarray:
     rng = np.random.default_rng(seed)
