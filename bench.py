@@ -52,9 +52,9 @@ def parse():
                     help="FP32c Coulomb launch shape (-1 automatic, 0..16 fixed: sg_set_coulomb_variant)")
     ap.add_argument("--method", type=int, default=5, choices=[4, 5],
                     help="5 Dormand-Prince, 4 Cash-Karp")
-    ap.add_argument("--proposer", default="on", choices=["on", "off"],
-                    help="learned step-size proposer (shipped weights) or the reference's "
-                         "controller")
+    ap.add_argument("--proposer", default="off", choices=["on", "off"],
+                    help="the reference's controller (default) or the learned step-size "
+                         "proposer with the shipped weights")
     ap.add_argument("--proposer-safety", type=float, default=None,
                     help="safety factor of the proposer (default: the trained one's)")
     ap.add_argument("--settle", type=int, default=60,
