@@ -160,3 +160,31 @@ def test_uniform_charge(ctx, qval, variant):
         ctx.set_coulomb_variant(-1)
     e = rel_err_per_ion(a, ref)
     assert e.max() <= 1e-6, (qval, variant, summary(e))
+
+
+def test_1m_spheroid_rows_and_momentum(ctx):
+    """The 1,048,576-ion spheroid at full size (automatic k-d ordered shape): sampled
+    oracle rows (random, nearest the centre, closest pairs) to 1e-6, and the pair sum's
+    size-independent property -- internal forces cancel: |sum_i m_i a_i| is at the
+    rounding level of sum_i |m_i a_i|."""
+    w = configs.spheroid_1m()
+    c = w.clouds[0]
+    n = len(c.mass)
+    q = c.charge.astype(np.float64)
+    kq = kq_of(c.mass, q)
+    a = ctx.coulomb_accel(c.pos, q, kq, SG_PREC_FP32C)
+    assert np.isfinite(a).all()
+    f = a * c.mass[:, None]
+    bal = np.linalg.norm(f.sum(0)) / np.linalg.norm(f, axis=1).sum()
+    print("momentum balance", bal)
+    assert bal < 1e-7
+    rng = np.random.default_rng(1)
+    r2 = (c.pos ** 2).sum(1)
+    order = np.lexsort(np.floor(c.pos / 2e-6).T)
+    d = np.linalg.norm(np.diff(c.pos[order], axis=0), axis=1)
+    rows = np.unique(np.concatenate([rng.choice(n, 40, replace=False), np.argsort(r2)[:12],
+                                     order[np.argsort(d)[:12]]]))
+    ref = np.stack([oracle.coulomb_kq_rows(c.pos, q, kq, int(i), int(i) + 1)[0] for i in rows])
+    e = rel_err_per_ion(a[rows], ref)
+    print(summary(e))
+    assert e.max() <= 1e-6, summary(e)
