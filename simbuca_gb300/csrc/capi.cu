@@ -396,7 +396,7 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(dalloc(&P.y, 6 * N));
     CK(dalloc(&P.ys, 6 * N));
     CK(dalloc(&P.k, 42 * N));
-    CK(dalloc(&P.part, (size_t)std::max(P.max_slots, 1) * 4 * NP));
+    CK(dalloc(&P.part, (size_t)std::max(P.max_slots, 1) * SG_PART_ARRAYS * NP));
     CK(dalloc(&P.coulS, 3 * N));
     CK(dalloc(&P.coul1, 3 * N));
     CK(dalloc(&P.coul7, 3 * N));
@@ -438,7 +438,7 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     for (int i = 0; i < P.n; i++) P.perm[i] = i;
     CK(cudaMemcpy(P.dperm, P.perm.data(), sizeof(int) * P.n, cudaMemcpyHostToDevice));
     CK(cudaMemset(P.coul1, 0, 3 * N * sizeof(double)));
-    CK(cudaMemset(P.part, 0, (size_t)std::max(P.max_slots, 1) * 4 * NP * sizeof(double)));
+    CK(cudaMemset(P.part, 0, (size_t)std::max(P.max_slots, 1) * SG_PART_ARRAYS * NP * sizeof(double)));
     CK(cudaMemset(P.coulS, 0, 3 * N * sizeof(double)));
     CK(cudaMallocHost((void**)&P.hctrl, sizeof(SgCtrl) * (size_t)std::max(P.n_clouds, 1)));
     CK(cudaMemcpy(P.drows, P.hrows.data(), sizeof(SgRowBlock) * P.hrows.size(),

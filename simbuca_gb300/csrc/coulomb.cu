@@ -506,13 +506,14 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
         }
     }
     if (!ok) return;
-    double* P = part + (size_t)it.slot * 4 * npad_total;
+    double* P = part + (size_t)it.slot * SG_PART_ARRAYS * npad_total;
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
         if (ipad[k] < 0) continue;
         const int li = tid + k * NT;
         const int ig = ipad[k];
         P[3 * (size_t)npad_total + ig] = (double)s2[k] * (qscale * qscale);
+        P[4 * (size_t)npad_total + ig] = 0.0;  // no far tiles in this form
         // P_i = sum q_j (x_i - x_j)/r^3 = -invL^2 qscale sum w (u_j - u_i) + close-pair
         // terms, w carrying the charges q_j / qscale
         const double sc = -invL2 * qscale;
@@ -523,13 +524,14 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
 }
 
 // Adds packed partial sums (two interleaved FP32 sums per ion and component) into the
-// compensated accumulators; with `near`, also their squares into the conditioning
-// estimate (near tiles hold the pairs the reduction's FP64 fix-up re-evaluates; in k-d
-// order the coherent sums of far tiles would flag ions for nothing).
+// compensated accumulators, and their squares into the conditioning estimate of the
+// near tiles (s2: the pairs the FP64 fix-up re-evaluates) or of the far tiles (s2f: the
+// hi-only pair terms, whose error grows with it; in k-d order a far tile's 32-ion sums
+// are coherent, so s2f is kept apart rather than flagging ions through s2).
 template <int IPT>
 __device__ __forceinline__ void fold_partials(const f2* ax, const f2* ay, const f2* az,
                                               float (*ks)[3], float (*kc)[3], float* s2,
-                                              bool near) {
+                                              float* s2f, bool near) {
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
         float a, b;
@@ -542,7 +544,10 @@ __device__ __forceinline__ void fold_partials(const f2* ax, const f2* ay, const 
         kahan_add(ks[k][0], kc[k][0], tx_);
         kahan_add(ks[k][1], kc[k][1], ty_);
         kahan_add(ks[k][2], kc[k][2], tz_);
-        if (near) s2[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2[k])));
+        if (near)
+            s2[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2[k])));
+        else
+            s2f[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2f[k])));
     }
 }
 
@@ -596,10 +601,11 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         corr[1][li] = 0.0;
         corr[2][li] = 0.0;
     }
-    float ks[IPT][3], kc[IPT][3], s2[IPT];
+    float ks[IPT][3], kc[IPT][3], s2[IPT], s2f[IPT];
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
         s2[k] = 0.f;
+        s2f[k] = 0.f;
 #pragma unroll
         for (int c = 0; c < 3; c++) ks[k][c] = kc[k][c] = 0.f;
     }
@@ -702,7 +708,7 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
                 else
                     tile_pairs<IPT, true>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh,
                                           zh, xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
-                fold_partials<IPT>(ax, ay, az, ks, kc, s2, !far);
+                fold_partials<IPT>(ax, ay, az, ks, kc, s2, s2f, !far);
             }
         }
         // close pairs of this tile, one flagged ion at a time by the whole warp
@@ -749,13 +755,14 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         }
     }
     if (!ok) return;
-    double* P = part + (size_t)it.slot * 4 * npad_total;
+    double* P = part + (size_t)it.slot * SG_PART_ARRAYS * npad_total;
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
         if (ipad[k] < 0) continue;
         const int li = IPT * tid + k;
         const int ig = ipad[k];
         P[3 * (size_t)npad_total + ig] = (double)s2[k] * (qscale * qscale);
+        P[4 * (size_t)npad_total + ig] = (double)s2f[k] * (qscale * qscale);
         // P_i = sum q_j (x_i - x_j)/r^3 = -invL^2 qscale sum w (u_j - u_i) + close-pair
         // terms, w carrying the charges q_j / qscale
         const double sc = -invL2 * qscale;
@@ -822,11 +829,12 @@ __global__ void __launch_bounds__(NT) coulomb_fp64_kernel(const double* __restri
             }
         }
     }
-    double* P = part + (size_t)it.slot * 4 * npad_total;
+    double* P = part + (size_t)it.slot * SG_PART_ARRAYS * npad_total;
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
         if (ipad[k] < 0) continue;
         P[3 * (size_t)npad_total + ipad[k]] = 0.0;
+        P[4 * (size_t)npad_total + ipad[k]] = 0.0;
         P[ipad[k]] = ax[k];
         P[npad_total + ipad[k]] = ay[k];
         P[2 * (size_t)npad_total + ipad[k]] = az[k];
@@ -843,8 +851,20 @@ __global__ void __launch_bounds__(NT) coulomb_fp64_kernel(const double* __restri
 // e.g. near the centre of a cloud) gets its dominant pairs -- those with
 // |f_ij| > 0.1 |P_i| that the main kernel did not already take in FP64 -- re-evaluated
 // in FP64, one block per flagged ion over the cloud's j-range.
+//
+// k-d ordered shapes: the far tile pairs were summed from the high FP32 parts only, an
+// error of ~1e-7 per pair that averages out unless the ion's net force is small next to
+// its far terms (the centre of a uniform cloud).  Its size tracks sqrt(s2f), the far
+// tiles' conditioning estimate: on the 1M-ion spheroid and the 65,536-ion Gaussian cloud
+// (numpy model of the kernel's arithmetic) the relative error of P_i stayed below
+// 1.3e-6 sqrt(s2f)/|P_i|.  An ion with sqrt(s2f) > 0.5 |P_i| gets the exact first-order
+// correction of every far pair term (fixup_ion), which leaves it at the near tiles'
+// FP32 accuracy.
 // ---------------------------------------------------------------------------
 constexpr double kKappa2 = 2.25;
+constexpr double kKappaFar2 = 0.25;
+// kinds of fix-up of a flagged ion
+constexpr int kFixNear = 1, kFixFar = 2;
 
 // tiles listed for the fix-up scan of one ion in k-d order
 constexpr int kNearCap = 1024;
@@ -853,21 +873,35 @@ constexpr int kFixupBlocks = 256;
 // batches up to this many ions fix their flagged ions inside the reduction's blocks
 constexpr int kInBlockFixupMax = 8192;
 
-// FP64 fix-up of one flagged ion i (frame-unit force magnitude pf) by the whole block of
-// SG_ROWS threads: the pairs with |f_ij| > |P_i| / 10 are re-evaluated in FP64 and their
-// FP32 terms, as the Coulomb kernel summed them, removed; thread 0 adds the correction to
-// out.  The j-ions are taken in a fixed order, so the result does not depend on which
-// block runs it or when.
+// Error-free difference: a - b = s + err exactly, s = fl(a - b) (Knuth's two-sum).
+__device__ __forceinline__ float two_diff_err(float a, float b, float s) {
+    const float bv = __fsub_rn(s, a);
+    const float av = __fsub_rn(s, bv);
+    return __fadd_rn(__fsub_rn(a, av), __fsub_rn(-b, bv));
+}
+
+// Fix-up of one flagged ion i (frame-unit force magnitude pf) by the whole block of
+// SG_ROWS threads.  kFixNear: the pairs with |f_ij| > |P_i| / 10 are re-evaluated in FP64
+// and their FP32 terms, as the Coulomb kernel summed them, removed.  kFixFar (k-d ordered
+// shapes): every far pair term gets the first-order change of d/r^3 under what the
+// hi-only difference dropped.  Thread 0 adds the corrections to out.  The j-ions are
+// taken in a fixed order, so the result does not depend on which block runs it or when.
 struct FixupShared {
     double wsum[SG_ROWS / 32][3];
     int wcnt[SG_ROWS / 32];
     int near_tiles[kNearCap];
 };
 
-__device__ void fixup_ion(const SgCloud& cl, int i, double pf, const float* __restrict__ c32,
-                          const double* __restrict__ c64, int npad_total,
-                          double* __restrict__ out, int n_total, const float* __restrict__ bbox,
-                          FixupShared& sh) {
+__device__ void fixup_far(const SgCloud& cl, int i, const float* __restrict__ c32,
+                          int npad_total, double* __restrict__ out, int n_total,
+                          const float* __restrict__ bbox, FixupShared& sh);
+
+__device__ void fixup_ion(const SgCloud& cl, int i, double pf, int kind,
+                          const float* __restrict__ c32, const double* __restrict__ c64,
+                          int npad_total, double* __restrict__ out, int n_total,
+                          const float* __restrict__ bbox, FixupShared& sh) {
+    if ((kind & kFixFar) && bbox != nullptr) fixup_far(cl, i, c32, npad_total, out, n_total, bbox, sh);
+    if (!(kind & kFixNear)) return;
     double (*wsum)[3] = sh.wsum;
     int* wcnt = sh.wcnt;
     int* near_tiles = sh.near_tiles;
@@ -970,11 +1004,86 @@ __device__ void fixup_ion(const SgCloud& cl, int i, double pf, const float* __re
     }
 }
 
-// Sums the j-chunk partials of each ion (x, y, z and the FP32c conditioning estimate s2)
-// into out.  FP32c: an ion whose terms cancel strongly (sqrt(s2) > 1.5 |P|) gets its
-// dominant pairs re-evaluated in FP64 (fixup_ion): INBLOCK, by this block right away
-// (small batches, where a second launch costs more than the work); otherwise it is put
-// on the work list of coulomb_fixup_kernel.
+// Far-tile correction of ion i (see fixup_ion): each warp takes whole 128-ion tiles that
+// the Coulomb kernel treated as far from the ion's own tile, and each pair term
+// f(u) = q u / |u|^3 of the hi-part difference u = fl(hi_j - hi_i) gets
+//     delta = q y3 (D - 3 y^2 (u.D) u),   D = (lo_j - lo_i) + (hi_j - hi_i - u),
+// the exact first-order change to the float-float difference (|D|/|u| ~ 1e-7, so the
+// second order is far below FP32 rounding).  y and y3 are formed as the kernel formed
+// them.  Summed in FP32 per thread (the terms are small), in FP64 across the block.
+__device__ void fixup_far(const SgCloud& cl, int i, const float* __restrict__ c32,
+                          int npad_total, double* __restrict__ out, int n_total,
+                          const float* __restrict__ bbox, FixupShared& sh) {
+    const int li = threadIdx.x;
+    const int warp = li >> 5, lane = li & 31;
+    const size_t NP = (size_t)npad_total;
+    const int igk = cl.poff + (i - cl.off);
+    const float xih = c32[igk], yih = c32[NP + igk], zih = c32[2 * NP + igk];
+    const float xil = c32[4 * NP + igk], yil = c32[5 * NP + igk], zil = c32[6 * NP + igk];
+    const int nt = (cl.npad + 127) / 128, itile = (igk - cl.poff) / 128;
+    const float* ibox = bbox + 8 * (size_t)(cl.tile0 + itile);
+    const float dfar2 = cl.dfar * cl.dfar;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    for (int t = warp; t < nt; t += SG_ROWS / 32) {
+        // the Coulomb kernel's far test for this (leaf, tile) pair, uniform per warp
+        if (t == itile || !(box_dist2(ibox, bbox + 8 * (size_t)(cl.tile0 + t)) > dfar2)) continue;
+        for (int jj = lane; jj < 128; jj += 32) {
+            const int j = t * 128 + jj;
+            if (j >= cl.npad) break;
+            const int jg = cl.poff + j;
+            const float xjh = c32[jg], yjh = c32[NP + jg], zjh = c32[2 * NP + jg];
+            const float q = c32[3 * NP + jg];
+            const float ux = __fsub_rn(xjh, xih), uy = __fsub_rn(yjh, yih), uz = __fsub_rn(zjh, zih);
+            float r2 = __fmaf_rn(ux, ux, kTiny);
+            r2 = __fmaf_rn(uy, uy, r2);
+            r2 = __fmaf_rn(uz, uz, r2);
+            const float y = rsqrt_approx(r2);
+            const float y3 = __fmul_rn(__fmul_rn(y, y), y);
+            const float dx = __fadd_rn(__fsub_rn(c32[4 * NP + jg], xil), two_diff_err(xjh, xih, ux));
+            const float dy = __fadd_rn(__fsub_rn(c32[5 * NP + jg], yil), two_diff_err(yjh, yih, uy));
+            const float dz = __fadd_rn(__fsub_rn(c32[6 * NP + jg], zil), two_diff_err(zjh, zih, uz));
+            const float ud = fmaf(ux, dx, fmaf(uy, dy, uz * dz));
+            const float s3 = 3.f * y * y * ud;
+            const float qy3 = q * y3;
+            fx = fmaf(qy3, fmaf(-s3, ux, dx), fx);
+            fy = fmaf(qy3, fmaf(-s3, uy, dy), fy);
+            fz = fmaf(qy3, fmaf(-s3, uz, dz), fz);
+        }
+    }
+    double ax = fx, ay = fy, az = fz;
+    for (int o = 16; o > 0; o >>= 1) {
+        ax += __shfl_down_sync(0xffffffffu, ax, o);
+        ay += __shfl_down_sync(0xffffffffu, ay, o);
+        az += __shfl_down_sync(0xffffffffu, az, o);
+    }
+    if (lane == 0) {
+        sh.wsum[warp][0] = ax;
+        sh.wsum[warp][1] = ay;
+        sh.wsum[warp][2] = az;
+    }
+    __syncthreads();
+    if (li == 0) {
+        double sx = 0.0, sy = 0.0, sz = 0.0;
+        for (int w = 0; w < SG_ROWS / 32; w++) {
+            sx += sh.wsum[w][0];
+            sy += sh.wsum[w][1];
+            sz += sh.wsum[w][2];
+        }
+        // frame sums of q u / r^3 -> P (SI), as the kernel's epilogue scales them
+        const double sc = -(cl.invL * cl.invL) * cl.qscale;
+        out[i] += sc * sx;
+        out[(size_t)n_total + i] += sc * sy;
+        out[2 * (size_t)n_total + i] += sc * sz;
+    }
+    __syncthreads();
+}
+
+// Sums the j-chunk partials of each ion (x, y, z and the FP32c conditioning estimates
+// s2, s2f) into out.  FP32c: an ion whose near terms cancel strongly (sqrt(s2) > 1.5 |P|)
+// or whose far terms are large next to |P| (sqrt(s2f) > 0.5 |P|) is fixed up
+// (fixup_ion): INBLOCK, by this block right away (small batches, where a second launch
+// costs more than the work); otherwise it is put on the work list of
+// coulomb_fixup_kernel (ion index; cloud | kind << 28; |P| in frame units).
 template <bool F32, bool INBLOCK>
 __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     const SgRowBlock* __restrict__ rows, const SgCloud* __restrict__ clouds,
@@ -990,33 +1099,37 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     if (!(cl.fp.flags & SG_F_COULOMB)) return;
     const int li = threadIdx.x;
     const int i = rb.i0 + li;
-    bool flag = false;
+    int kind = 0;
     double pf = 0.0;
     if (li < rb.n) {
         const int ig = cl.poff + (i - cl.off);
         const size_t NP = (size_t)npad_total;
-        double px = 0.0, py = 0.0, pz = 0.0, s2 = 0.0;
+        double px = 0.0, py = 0.0, pz = 0.0, s2 = 0.0, s2f = 0.0;
         for (int sl = 0; sl < cl.nslots; sl++) {
-            const double* P = part + (size_t)sl * 4 * NP;
+            const double* P = part + (size_t)sl * SG_PART_ARRAYS * NP;
             px += P[ig];
             py += P[NP + ig];
             pz += P[2 * NP + ig];
-            s2 += P[3 * NP + ig];
+            if (F32) {
+                s2 += P[3 * NP + ig];
+                s2f += P[4 * NP + ig];
+            }
         }
         out[i] = px;
         out[(size_t)n_total + i] = py;
         out[2 * (size_t)n_total + i] = pz;
         if (F32) {
             pf = sqrt(px * px + py * py + pz * pz) * (cl.L * cl.L);  // frame units
-            flag = s2 > kKappa2 * pf * pf;
+            kind = (s2 > kKappa2 * pf * pf ? kFixNear : 0) |
+                   (s2f > kKappaFar2 * pf * pf ? kFixFar : 0);
         }
     }
     if (!F32) return;
     if (!INBLOCK) {
-        if (flag) {
+        if (kind) {
             const int at = atomicAdd(fix_list, 1);
             fix_list[1 + 2 * at] = i;
-            fix_list[2 + 2 * at] = rb.cloud;
+            fix_list[2 + 2 * at] = rb.cloud | (kind << 28);
             fix_pf[at] = pf;
             if (counters != nullptr) atomicAdd(counters, 1);
         }
@@ -1025,19 +1138,21 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     __shared__ FixupShared sh;
     __shared__ int nflag;
     __shared__ int flist[SG_ROWS];
+    __shared__ int fkind[SG_ROWS];
     __shared__ double fpf[SG_ROWS];
     if (li == 0) nflag = 0;
     __syncthreads();
-    if (flag) {
+    if (kind) {
         const int at = atomicAdd(&nflag, 1);
         flist[at] = i;
+        fkind[at] = kind;
         fpf[at] = pf;
         if (counters != nullptr) atomicAdd(counters, 1);
     }
     __syncthreads();  // also orders this block's writes of out before the corrections
     const int nf = nflag;
     for (int k = 0; k < nf; k++)
-        fixup_ion(cl, flist[k], fpf[k], c32, c64, npad_total, out, n_total, bbox, sh);
+        fixup_ion(cl, flist[k], fpf[k], fkind[k], c32, c64, npad_total, out, n_total, bbox, sh);
 }
 
 // The flagged ions of a whole batch, one block per ion (blocks stride over the list).
@@ -1048,9 +1163,11 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_fixup_kernel(
     const float* __restrict__ bbox) {
     __shared__ FixupShared sh;
     const int count = fix_list[0];
-    for (int k = blockIdx.x; k < count; k += gridDim.x)
-        fixup_ion(clouds[fix_list[2 + 2 * k]], fix_list[1 + 2 * k], fix_pf[k], c32, c64,
+    for (int k = blockIdx.x; k < count; k += gridDim.x) {
+        const int ck = fix_list[2 + 2 * k];
+        fixup_ion(clouds[ck & 0x0FFFFFFF], fix_list[1 + 2 * k], fix_pf[k], ck >> 28, c32, c64,
                   npad_total, out, n_total, bbox, sh);
+    }
 }
 
 }  // namespace

@@ -28,6 +28,9 @@
 #define SG_PAD 32
 // O(N) kernels: ions per block.
 #define SG_ROWS 256
+// Arrays of a Coulomb partial-sum slot: x, y, z, and the FP32c conditioning estimates
+// of the near tiles and of the far tiles (sums of squared 32-ion partial sums).
+#define SG_PART_ARRAYS 5
 
 // Bounded device waits: a wait gives up after this many nanoseconds of
 // %globaltimer and raises SG_TIMEOUT in the context's error word.
