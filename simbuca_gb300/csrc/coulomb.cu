@@ -881,25 +881,28 @@ __device__ __forceinline__ float two_diff_err(float a, float b, float s) {
 }
 
 // Fix-up of one flagged ion i (frame-unit force magnitude pf) by the whole block of
-// SG_ROWS threads.  kFixNear: the pairs with |f_ij| > |P_i| / 10 are re-evaluated in FP64
+// NTH threads.  kFixNear: the pairs with |f_ij| > |P_i| / 10 are re-evaluated in FP64
 // and their FP32 terms, as the Coulomb kernel summed them, removed.  kFixFar (k-d ordered
 // shapes): every far pair term gets the first-order change of d/r^3 under what the
 // hi-only difference dropped.  Thread 0 adds the corrections to out.  The j-ions are
 // taken in a fixed order, so the result does not depend on which block runs it or when.
+template <int NTH>
 struct FixupShared {
-    double wsum[SG_ROWS / 32][3];
-    int wcnt[SG_ROWS / 32];
+    double wsum[NTH / 32][3];
+    int wcnt[NTH / 32];
     int near_tiles[kNearCap];
 };
 
+template <int NTH>
 __device__ void fixup_far(const SgCloud& cl, int i, const float* __restrict__ c32,
                           int npad_total, double* __restrict__ out, int n_total,
-                          const float* __restrict__ bbox, FixupShared& sh);
+                          const float* __restrict__ bbox, FixupShared<NTH>& sh);
 
+template <int NTH>
 __device__ void fixup_ion(const SgCloud& cl, int i, double pf, int kind,
                           const float* __restrict__ c32, const double* __restrict__ c64,
                           int npad_total, double* __restrict__ out, int n_total,
-                          const float* __restrict__ bbox, FixupShared& sh) {
+                          const float* __restrict__ bbox, FixupShared<NTH>& sh) {
     if ((kind & kFixFar) && bbox != nullptr) fixup_far(cl, i, c32, npad_total, out, n_total, bbox, sh);
     if (!(kind & kFixNear)) return;
     double (*wsum)[3] = sh.wsum;
@@ -926,7 +929,7 @@ __device__ void fixup_ion(const SgCloud& cl, int i, double pf, int kind,
         if (ibox != nullptr) {
             const int nt = (cl.npad + 127) / 128, itile = (igk - cl.poff) / 128;
             const float dfar2 = cl.dfar * cl.dfar;
-            for (int t0 = 0; t0 < nt; t0 += SG_ROWS) {
+            for (int t0 = 0; t0 < nt; t0 += NTH) {
                 const int t = t0 + li;
                 const bool nr = t < nt && (t == itile ||
                                            box_dist2(ibox, bbox + 8 * (size_t)(cl.tile0 + t)) <= dfar2);
@@ -934,7 +937,7 @@ __device__ void fixup_ion(const SgCloud& cl, int i, double pf, int kind,
                 if (lane == 0) wcnt[warp] = __popc(m);
                 __syncthreads();
                 int off = n_near, tot = 0;
-                for (int w = 0; w < SG_ROWS / 32; w++) {
+                for (int w = 0; w < NTH / 32; w++) {
                     if (w < warp) off += wcnt[w];
                     tot += wcnt[w];
                 }
@@ -948,7 +951,7 @@ __device__ void fixup_ion(const SgCloud& cl, int i, double pf, int kind,
         }
         const bool listed = ibox != nullptr && n_near <= kNearCap;
         const int n_scan = listed ? n_near * 128 : cl.npad;
-        for (int qj = li; qj < n_scan; qj += SG_ROWS) {
+        for (int qj = li; qj < n_scan; qj += NTH) {
             const int j = listed ? near_tiles[qj >> 7] * 128 + (qj & 127) : qj;
             if (j >= cl.npad) continue;
             const int jg = cl.poff + j;
@@ -991,7 +994,7 @@ __device__ void fixup_ion(const SgCloud& cl, int i, double pf, int kind,
         __syncthreads();
         if (li == 0) {
             double sx = 0.0, sy = 0.0, sz = 0.0;
-            for (int w = 0; w < SG_ROWS / 32; w++) {
+            for (int w = 0; w < NTH / 32; w++) {
                 sx += wsum[w][0];
                 sy += wsum[w][1];
                 sz += wsum[w][2];
@@ -1011,9 +1014,10 @@ __device__ void fixup_ion(const SgCloud& cl, int i, double pf, int kind,
 // the exact first-order change to the float-float difference (|D|/|u| ~ 1e-7, so the
 // second order is far below FP32 rounding).  y and y3 are formed as the kernel formed
 // them.  Summed in FP32 per thread (the terms are small), in FP64 across the block.
+template <int NTH>
 __device__ void fixup_far(const SgCloud& cl, int i, const float* __restrict__ c32,
                           int npad_total, double* __restrict__ out, int n_total,
-                          const float* __restrict__ bbox, FixupShared& sh) {
+                          const float* __restrict__ bbox, FixupShared<NTH>& sh) {
     const int li = threadIdx.x;
     const int warp = li >> 5, lane = li & 31;
     const size_t NP = (size_t)npad_total;
@@ -1024,7 +1028,7 @@ __device__ void fixup_far(const SgCloud& cl, int i, const float* __restrict__ c3
     const float* ibox = bbox + 8 * (size_t)(cl.tile0 + itile);
     const float dfar2 = cl.dfar * cl.dfar;
     float fx = 0.f, fy = 0.f, fz = 0.f;
-    for (int t = warp; t < nt; t += SG_ROWS / 32) {
+    for (int t = warp; t < nt; t += NTH / 32) {
         // the Coulomb kernel's far test for this (leaf, tile) pair, uniform per warp
         if (t == itile || !(box_dist2(ibox, bbox + 8 * (size_t)(cl.tile0 + t)) > dfar2)) continue;
         for (int jj = lane; jj < 128; jj += 32) {
@@ -1064,7 +1068,7 @@ __device__ void fixup_far(const SgCloud& cl, int i, const float* __restrict__ c3
     __syncthreads();
     if (li == 0) {
         double sx = 0.0, sy = 0.0, sz = 0.0;
-        for (int w = 0; w < SG_ROWS / 32; w++) {
+        for (int w = 0; w < NTH / 32; w++) {
             sx += sh.wsum[w][0];
             sy += sh.wsum[w][1];
             sz += sh.wsum[w][2];
@@ -1135,7 +1139,7 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
         }
         return;
     }
-    __shared__ FixupShared sh;
+    __shared__ FixupShared<SG_ROWS> sh;
     __shared__ int nflag;
     __shared__ int flist[SG_ROWS];
     __shared__ int fkind[SG_ROWS];
@@ -1156,12 +1160,15 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
 }
 
 // The flagged ions of a whole batch, one block per ion (blocks stride over the list).
-__global__ void __launch_bounds__(SG_ROWS) coulomb_fixup_kernel(
+// Larger blocks than the reduction's: a far fix-up scans the whole cloud, and with one
+// block per SM its dependent chains need the warps.
+constexpr int kFixupThreads = 1024;
+__global__ void __launch_bounds__(kFixupThreads) coulomb_fixup_kernel(
     const SgCloud* __restrict__ clouds, const float* __restrict__ c32,
     const double* __restrict__ c64, int npad_total, double* __restrict__ out, int n_total,
     const int* __restrict__ fix_list, const double* __restrict__ fix_pf,
     const float* __restrict__ bbox) {
-    __shared__ FixupShared sh;
+    __shared__ FixupShared<kFixupThreads> sh;
     const int count = fix_list[0];
     for (int k = blockIdx.x; k < count; k += gridDim.x) {
         const int ck = fix_list[2 + 2 * k];
@@ -1292,7 +1299,7 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
         // a block per flagged ion: a fixed grid that strides over however many there are
         // (flagged ions are a small fraction: small batches get a small grid)
         const int grid = n_total / 256 < 1 ? 1 : (n_total / 256 > kFixupBlocks ? kFixupBlocks : n_total / 256);
-        coulomb_fixup_kernel<<<grid, SG_ROWS, 0, s>>>(
+        coulomb_fixup_kernel<<<grid, kFixupThreads, 0, s>>>(
             a.clouds, a.c32, a.c64, a.npad_total, out, n_total, a.fix_list, a.fix_pf, bbox);
     } else {
         coulomb_reduce_kernel<false, false><<<n_rows, SG_ROWS, 0, s>>>(
