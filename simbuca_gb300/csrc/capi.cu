@@ -600,7 +600,12 @@ void flush_timing(sg_ctx* ctx) {
 // Coulomb sums of the current Coulomb inputs into out[3][N]: the pair kernel over the
 // work items, then the per-ion reduction of the partial-sum slots (with the FP32c
 // conditioning fix-up).
-int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter, double* out) {
+// far_estimate: recompute the far tiles' conditioning estimate in this call (the first
+// Coulomb sum of an attempt and every stand-alone one); later stages of the attempt
+// reuse it -- the ions barely move within a step, and only the choice of which ions to
+// fix up depends on it.
+int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter, double* out,
+                   bool far_estimate = true) {
     if (!P.any_coulomb || P.n_items == 0) return SG_OK;
     SgCoulombArgs ca;
     ca.c32 = P.c32;
@@ -616,6 +621,7 @@ int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter, double
     ca.bbox = P.bbox;
     ca.fix_list = P.fix_list;
     ca.fix_pf = P.fix_pf;
+    ca.far_estimate = far_estimate ? 1 : 0;
     TimedLaunch tl{nullptr, nullptr, inter};
     const int cap = ctx->capture_events;
     if (cap >= 0) {
@@ -685,14 +691,14 @@ int enqueue_attempt(sg_ctx* ctx, Problem& P) {
         // inputs are rebuilt and all six stages take a Coulomb sum
         STAGE_TIMED(sg_coords_from_state(a, P.qd, P.n_rows, ctx->stream));
         for (int s = 1; s <= 6; s++) {
-            int st = launch_coulomb(ctx, P, true, inter, P.coulS);
+            int st = launch_coulomb(ctx, P, true, inter, P.coulS, s == 1);
             if (st != SG_OK) return st;
             STAGE_TIMED(sg_ck_stage(a, s, P.n_rows, ctx->stream));
         }
     } else {
         STAGE_TIMED(sg_dp_stage(a, 1, P.n_rows, ctx->stream));
         for (int s = 2; s <= 7; s++) {
-            int st = launch_coulomb(ctx, P, true, inter, P.coulS);
+            int st = launch_coulomb(ctx, P, true, inter, P.coulS, s == 2);
             if (st != SG_OK) return st;
             STAGE_TIMED(sg_dp_stage(a, s, P.n_rows, ctx->stream));
         }

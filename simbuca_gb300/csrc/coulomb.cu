@@ -528,7 +528,7 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
 // near tiles (s2: the pairs the FP64 fix-up re-evaluates) or of the far tiles (s2f: the
 // hi-only pair terms, whose error grows with it; in k-d order a far tile's 32-ion sums
 // are coherent, so s2f is kept apart rather than flagging ions through s2).
-template <int IPT>
+template <int IPT, bool S2F = true>
 __device__ __forceinline__ void fold_partials(const f2* ax, const f2* ay, const f2* az,
                                               float (*ks)[3], float (*kc)[3], float* s2,
                                               float* s2f, bool near) {
@@ -546,12 +546,12 @@ __device__ __forceinline__ void fold_partials(const f2* ax, const f2* ay, const 
         kahan_add(ks[k][2], kc[k][2], tz_);
         if (near)
             s2[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2[k])));
-        else
+        else if (S2F)
             s2f[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2f[k])));
     }
 }
 
-template <int NT, int IPT, int MINB, int STAGES, int TJ = SG_TILE, int FU = 0>
+template <int NT, int IPT, int MINB, int STAGES, int TJ = SG_TILE, int FU = 0, bool S2F = true>
 __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const float* __restrict__ c32,
                                                             const double* __restrict__ c64,
                                                             const SgWorkItem* __restrict__ items,
@@ -708,7 +708,7 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
                 else
                     tile_pairs<IPT, true>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh,
                                           zh, xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
-                fold_partials<IPT>(ax, ay, az, ks, kc, s2, s2f, !far);
+                fold_partials<IPT, S2F>(ax, ay, az, ks, kc, s2, s2f, !far);
             }
         }
         // close pairs of this tile, one flagged ion at a time by the whole warp
@@ -762,7 +762,7 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         const int li = IPT * tid + k;
         const int ig = ipad[k];
         P[3 * (size_t)npad_total + ig] = (double)s2[k] * (qscale * qscale);
-        P[4 * (size_t)npad_total + ig] = (double)s2f[k] * (qscale * qscale);
+        if (S2F) P[4 * (size_t)npad_total + ig] = (double)s2f[k] * (qscale * qscale);
         // P_i = sum q_j (x_i - x_j)/r^3 = -invL^2 qscale sum w (u_j - u_i) + close-pair
         // terms, w carrying the charges q_j / qscale
         const double sc = -invL2 * qscale;
@@ -1230,22 +1230,38 @@ cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s) {
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 9:
-            coulomb_fp32c_sorted_kernel<128, 1, 8, 3><<<a.n_items, 128, 0, s>>>(
-                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            if (a.far_estimate)
+                coulomb_fp32c_sorted_kernel<128, 1, 8, 3><<<a.n_items, 128, 0, s>>>(
+                    a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            else
+                coulomb_fp32c_sorted_kernel<128, 1, 8, 3, SG_TILE, 0, false><<<a.n_items, 128, 0, s>>>(
+                    a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 12:
             // as 9 with 256-ion j-tiles: half the ring waits and barriers per pair
-            coulomb_fp32c_sorted_kernel<128, 1, 8, 3, 256><<<a.n_items, 128, 0, s>>>(
-                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            if (a.far_estimate)
+                coulomb_fp32c_sorted_kernel<128, 1, 8, 3, 256><<<a.n_items, 128, 0, s>>>(
+                    a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            else
+                coulomb_fp32c_sorted_kernel<128, 1, 8, 3, 256, 0, false><<<a.n_items, 128, 0, s>>>(
+                    a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 13:
-            coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256><<<a.n_items, 64, 0, s>>>(
-                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            if (a.far_estimate)
+                coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256><<<a.n_items, 64, 0, s>>>(
+                    a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            else
+                coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256, 0, false><<<a.n_items, 64, 0, s>>>(
+                    a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 14:
             // as 13 with four j pairs in flight per ion on far tiles
-            coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256, 4><<<a.n_items, 64, 0, s>>>(
-                a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            if (a.far_estimate)
+                coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256, 4><<<a.n_items, 64, 0, s>>>(
+                    a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
+            else
+                coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256, 4, false><<<a.n_items, 64, 0, s>>>(
+                    a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 15:
             // the leaf in one warp (4 ions per thread), 256-ion j-tiles

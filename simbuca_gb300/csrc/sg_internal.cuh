@@ -356,7 +356,7 @@ struct SgCoulombArgs {
     int n_items;
     const SgCloud* clouds;
     const SgCtrl* ctrl;      // may be null (stand-alone calls)
-    double* part;            // [slots][4][Npad]: x, y, z sums and the FP32c s2 estimate
+    double* part;            // [slots][SG_PART_ARRAYS][Npad]: x, y, z sums, FP32c s2, s2f
     int npad_total;
     int* errword;
     int variant;             // FP32c launch shape (sg_coulomb_fp32c_ib)
@@ -365,6 +365,9 @@ struct SgCoulombArgs {
     // per flagged ion its global index and cloud (ints) and |P| in frame units
     int* fix_list;
     double* fix_pf;
+    // k-d ordered shapes: accumulate the far tiles' conditioning estimate s2f in this
+    // call (it costs the kernel ~4 %); otherwise the slots keep the last call's values
+    int far_estimate;
 };
 
 #define SG_C32_VARIANTS 17
