@@ -71,6 +71,8 @@ struct Problem {
     double *pmass = nullptr, *pmass0 = nullptr;  // print masses (dissociation), both orders
     int* fix_list = nullptr;   // FP32c fix-up work list: count, then (ion, cloud) pairs
     double* fix_pf = nullptr;
+    double* fix_part = nullptr;  // fix-up work units' corrections [listed][units][3]
+    int* fix_done = nullptr;     // finished units per listed ion (zero between calls)
     // operation sequence
     std::vector<sg_field_params> fp0;  // field parameters as created / set by the caller
     std::vector<SgOp> hops;
@@ -169,6 +171,8 @@ void free_problem(Problem& P) {
     cudaFree(P.pmass0);
     cudaFree(P.fix_list);
     cudaFree(P.fix_pf);
+    cudaFree(P.fix_part);
+    cudaFree(P.fix_done);
     cudaFree(P.dops);
     cudaFree(P.dis_spec);
     cudaFree(P.dis_mass);
@@ -425,6 +429,9 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(dalloc(&P.fix_list, 1 + 2 * N));
     CK(dalloc(&P.fix_pf, N));
     CK(cudaMemset(P.fix_list, 0, sizeof(int)));
+    CK(dalloc(&P.fix_part, (size_t)SG_FIX_CHUNKED_CAP * SG_FIX_UNITS * 3));
+    CK(dalloc(&P.fix_done, SG_FIX_CHUNKED_CAP));
+    CK(cudaMemset(P.fix_done, 0, sizeof(int) * SG_FIX_CHUNKED_CAP));
     CK(cudaMemset(P.pmass, 0, N * sizeof(double)));
     CK(cudaMemset(P.pmass0, 0, N * sizeof(double)));
     CK(dalloc(&P.bbox, (size_t)std::max(P.ntiles, 1) * 8));
@@ -621,6 +628,8 @@ int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter, double
     ca.bbox = P.bbox;
     ca.fix_list = P.fix_list;
     ca.fix_pf = P.fix_pf;
+    ca.fix_part = P.fix_part;
+    ca.fix_done = P.fix_done;
     ca.far_estimate = far_estimate ? 1 : 0;
     TimedLaunch tl{nullptr, nullptr, inter};
     const int cap = ctx->capture_events;

@@ -868,8 +868,11 @@ constexpr int kFixNear = 1, kFixFar = 2;
 
 // tiles listed for the fix-up scan of one ion in k-d order
 constexpr int kNearCap = 1024;
-// blocks of the fix-up kernel (each takes every kFixupBlocks-th flagged ion)
+// blocks of the fix-up kernel (each takes every kFixupBlocks-th work unit)
 constexpr int kFixupBlocks = 256;
+// work units of one listed ion in the fix-up kernel, and the listed ions that get them
+constexpr int kFarChunks = SG_FIX_UNITS;
+constexpr int kChunkedCap = SG_FIX_CHUNKED_CAP;
 // batches up to this many ions fix their flagged ions inside the reduction's blocks
 constexpr int kInBlockFixupMax = 8192;
 
@@ -880,12 +883,6 @@ __device__ __forceinline__ float two_diff_err(float a, float b, float s) {
     return __fadd_rn(__fsub_rn(a, av), __fsub_rn(-b, bv));
 }
 
-// Fix-up of one flagged ion i (frame-unit force magnitude pf) by the whole block of
-// NTH threads.  kFixNear: the pairs with |f_ij| > |P_i| / 10 are re-evaluated in FP64
-// and their FP32 terms, as the Coulomb kernel summed them, removed.  kFixFar (k-d ordered
-// shapes): every far pair term gets the first-order change of d/r^3 under what the
-// hi-only difference dropped.  Thread 0 adds the corrections to out.  The j-ions are
-// taken in a fixed order, so the result does not depend on which block runs it or when.
 template <int NTH>
 struct FixupShared {
     double wsum[NTH / 32][3];
@@ -893,131 +890,133 @@ struct FixupShared {
     int near_tiles[kNearCap];
 };
 
-template <int NTH>
-__device__ void fixup_far(const SgCloud& cl, int i, const float* __restrict__ c32,
-                          int npad_total, double* __restrict__ out, int n_total,
-                          const float* __restrict__ bbox, FixupShared<NTH>& sh);
+struct Corr3 {
+    double x, y, z;
+};
 
+// Block-wide sum of one value per thread and component; the result is thread 0's.
 template <int NTH>
-__device__ void fixup_ion(const SgCloud& cl, int i, double pf, int kind,
-                          const float* __restrict__ c32, const double* __restrict__ c64,
-                          int npad_total, double* __restrict__ out, int n_total,
-                          const float* __restrict__ bbox, FixupShared<NTH>& sh) {
-    if ((kind & kFixFar) && bbox != nullptr) fixup_far(cl, i, c32, npad_total, out, n_total, bbox, sh);
-    if (!(kind & kFixNear)) return;
-    double (*wsum)[3] = sh.wsum;
+__device__ Corr3 block_sum3(double ax, double ay, double az, FixupShared<NTH>& sh) {
+    const int li = threadIdx.x, warp = li >> 5, lane = li & 31;
+    for (int o = 16; o > 0; o >>= 1) {
+        ax += __shfl_down_sync(0xffffffffu, ax, o);
+        ay += __shfl_down_sync(0xffffffffu, ay, o);
+        az += __shfl_down_sync(0xffffffffu, az, o);
+    }
+    if (lane == 0) {
+        sh.wsum[warp][0] = ax;
+        sh.wsum[warp][1] = ay;
+        sh.wsum[warp][2] = az;
+    }
+    __syncthreads();
+    Corr3 r{0.0, 0.0, 0.0};
+    if (li == 0)
+        for (int w = 0; w < NTH / 32; w++) {
+            r.x += sh.wsum[w][0];
+            r.y += sh.wsum[w][1];
+            r.z += sh.wsum[w][2];
+        }
+    __syncthreads();
+    return r;
+}
+
+// Near fix-up of ion i (frame-unit force magnitude pf) by the whole block of NTH threads:
+// the pairs with |f_ij| > |P_i| / 10 are re-evaluated in FP64 and their FP32 terms, as
+// the Coulomb kernel summed them, removed.  Returns the correction of P_i (thread 0).
+template <int NTH>
+__device__ Corr3 fixup_near(const SgCloud& cl, int i, double pf, const float* __restrict__ c32,
+                            const double* __restrict__ c64, int npad_total,
+                            const float* __restrict__ bbox, FixupShared<NTH>& sh) {
     int* wcnt = sh.wcnt;
     int* near_tiles = sh.near_tiles;
     const int li = threadIdx.x;
     const int warp = li >> 5, lane = li & 31;
     const size_t NP = (size_t)npad_total;
-    {
-        const int igk = cl.poff + (i - cl.off);
-        const double invL2 = cl.invL * cl.invL;
-        const float wc = cl.wc;
-        const double tq = 0.1 * pf;
-        const float thr3 = (float)(tq * sqrt(tq));  // (|P|/10)^(3/2): |f_ij| > |P|/10
-        const float xih = c32[igk], yih = c32[NP + igk], zih = c32[2 * NP + igk];
-        const float xil = c32[4 * NP + igk], yil = c32[5 * NP + igk], zil = c32[6 * NP + igk];
-        const double xi = c64[igk], yi = c64[NP + igk], zi = c64[2 * NP + igk];
-        double ax = 0.0, ay = 0.0, az = 0.0;
-        const float* ibox = bbox ? bbox + 8 * (size_t)(cl.tile0 + (igk - cl.poff) / 128) : nullptr;
-        // k-d ordered clouds: scan only the tiles near the ion's own tile, listed in
-        // order by a block-wide ballot (far tiles were summed from the high parts and
-        // are left as they are); the whole cloud if the list would overflow
-        int n_near = 0;
-        if (ibox != nullptr) {
-            const int nt = (cl.npad + 127) / 128, itile = (igk - cl.poff) / 128;
-            const float dfar2 = cl.dfar * cl.dfar;
-            for (int t0 = 0; t0 < nt; t0 += NTH) {
-                const int t = t0 + li;
-                const bool nr = t < nt && (t == itile ||
-                                           box_dist2(ibox, bbox + 8 * (size_t)(cl.tile0 + t)) <= dfar2);
-                const unsigned m = __ballot_sync(0xffffffffu, nr);
-                if (lane == 0) wcnt[warp] = __popc(m);
-                __syncthreads();
-                int off = n_near, tot = 0;
-                for (int w = 0; w < NTH / 32; w++) {
-                    if (w < warp) off += wcnt[w];
-                    tot += wcnt[w];
-                }
-                if (nr) {
-                    const int at = off + __popc(m & ((1u << lane) - 1u));
-                    if (at < kNearCap) near_tiles[at] = t;
-                }
-                __syncthreads();
-                n_near += tot;
-            }
-        }
-        const bool listed = ibox != nullptr && n_near <= kNearCap;
-        const int n_scan = listed ? n_near * 128 : cl.npad;
-        for (int qj = li; qj < n_scan; qj += NTH) {
-            const int j = listed ? near_tiles[qj >> 7] * 128 + (qj & 127) : qj;
-            if (j >= cl.npad) continue;
-            const int jg = cl.poff + j;
-            PairF p = pair_f32(c32[jg], c32[NP + jg], c32[2 * NP + jg], c32[4 * NP + jg],
-                               c32[5 * NP + jg], c32[6 * NP + jg], xih, yih, zih, xil, yil,
-                               zil);
-            if (ibox != nullptr && !listed) {
-                // the sorted kernel summed this pair from the high parts if its tiles are far
-                const float* jbox = bbox + 8 * (size_t)(cl.tile0 + j / 128);
-                const bool same = (igk - cl.poff) / 128 == j / 128;
-                if (!same && box_dist2(ibox, jbox) > cl.dfar * cl.dfar) {
-                    const PairH q = pair_hi(c32[jg], c32[NP + jg], c32[2 * NP + jg], xih, yih, zih);
-                    p.dx = q.dx;
-                    p.dy = q.dy;
-                    p.dz = q.dz;
-                    p.y3 = q.y3;
-                }
-            }
-            if (p.y3 > thr3 && p.y3 <= wc && jg != igk) {
-                const float wf = __fmul_rn(c32[3 * NP + jg], p.y3);
-                const double rx = xi - c64[jg], ry = yi - c64[NP + jg], rz = zi - c64[2 * NP + jg];
-                const double inv = rsqrt_fp64(rx * rx + ry * ry + rz * rz);
-                const double wq = c64[3 * NP + jg] * inv * inv * inv;
-                const double wsc = invL2 * (double)cl.qscale * (double)wf;
-                ax += wq * rx + wsc * (double)p.dx;
-                ay += wq * ry + wsc * (double)p.dy;
-                az += wq * rz + wsc * (double)p.dz;
-            }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            ax += __shfl_down_sync(0xffffffffu, ax, o);
-            ay += __shfl_down_sync(0xffffffffu, ay, o);
-            az += __shfl_down_sync(0xffffffffu, az, o);
-        }
-        if (lane == 0) {
-            wsum[warp][0] = ax;
-            wsum[warp][1] = ay;
-            wsum[warp][2] = az;
-        }
-        __syncthreads();
-        if (li == 0) {
-            double sx = 0.0, sy = 0.0, sz = 0.0;
+    const int igk = cl.poff + (i - cl.off);
+    const double invL2 = cl.invL * cl.invL;
+    const float wc = cl.wc;
+    const double tq = 0.1 * pf;
+    const float thr3 = (float)(tq * sqrt(tq));  // (|P|/10)^(3/2): |f_ij| > |P|/10
+    const float xih = c32[igk], yih = c32[NP + igk], zih = c32[2 * NP + igk];
+    const float xil = c32[4 * NP + igk], yil = c32[5 * NP + igk], zil = c32[6 * NP + igk];
+    const double xi = c64[igk], yi = c64[NP + igk], zi = c64[2 * NP + igk];
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    const float* ibox = bbox ? bbox + 8 * (size_t)(cl.tile0 + (igk - cl.poff) / 128) : nullptr;
+    // k-d ordered clouds: scan only the tiles near the ion's own tile, listed in order by
+    // a block-wide ballot (far tiles are the far fix-up's); the whole cloud if the list
+    // would overflow
+    int n_near = 0;
+    if (ibox != nullptr) {
+        const int nt = (cl.npad + 127) / 128, itile = (igk - cl.poff) / 128;
+        const float dfar2 = cl.dfar * cl.dfar;
+        for (int t0 = 0; t0 < nt; t0 += NTH) {
+            const int t = t0 + li;
+            const bool nr = t < nt && (t == itile ||
+                                       box_dist2(ibox, bbox + 8 * (size_t)(cl.tile0 + t)) <= dfar2);
+            const unsigned m = __ballot_sync(0xffffffffu, nr);
+            if (lane == 0) wcnt[warp] = __popc(m);
+            __syncthreads();
+            int off = n_near, tot = 0;
             for (int w = 0; w < NTH / 32; w++) {
-                sx += wsum[w][0];
-                sy += wsum[w][1];
-                sz += wsum[w][2];
+                if (w < warp) off += wcnt[w];
+                tot += wcnt[w];
             }
-            out[i] += sx;
-            out[(size_t)n_total + i] += sy;
-            out[2 * (size_t)n_total + i] += sz;
+            if (nr) {
+                const int at = off + __popc(m & ((1u << lane) - 1u));
+                if (at < kNearCap) near_tiles[at] = t;
+            }
+            __syncthreads();
+            n_near += tot;
         }
-        __syncthreads();
     }
+    const bool listed = ibox != nullptr && n_near <= kNearCap;
+    const int n_scan = listed ? n_near * 128 : cl.npad;
+    for (int qj = li; qj < n_scan; qj += NTH) {
+        const int j = listed ? near_tiles[qj >> 7] * 128 + (qj & 127) : qj;
+        if (j >= cl.npad) continue;
+        const int jg = cl.poff + j;
+        PairF p = pair_f32(c32[jg], c32[NP + jg], c32[2 * NP + jg], c32[4 * NP + jg],
+                           c32[5 * NP + jg], c32[6 * NP + jg], xih, yih, zih, xil, yil, zil);
+        if (ibox != nullptr && !listed) {
+            // the sorted kernel summed this pair from the high parts if its tiles are far
+            const float* jbox = bbox + 8 * (size_t)(cl.tile0 + j / 128);
+            const bool same = (igk - cl.poff) / 128 == j / 128;
+            if (!same && box_dist2(ibox, jbox) > cl.dfar * cl.dfar) {
+                const PairH q = pair_hi(c32[jg], c32[NP + jg], c32[2 * NP + jg], xih, yih, zih);
+                p.dx = q.dx;
+                p.dy = q.dy;
+                p.dz = q.dz;
+                p.y3 = q.y3;
+            }
+        }
+        if (p.y3 > thr3 && p.y3 <= wc && jg != igk) {
+            const float wf = __fmul_rn(c32[3 * NP + jg], p.y3);
+            const double rx = xi - c64[jg], ry = yi - c64[NP + jg], rz = zi - c64[2 * NP + jg];
+            const double inv = rsqrt_fp64(rx * rx + ry * ry + rz * rz);
+            const double wq = c64[3 * NP + jg] * inv * inv * inv;
+            const double wsc = invL2 * (double)cl.qscale * (double)wf;
+            ax += wq * rx + wsc * (double)p.dx;
+            ay += wq * ry + wsc * (double)p.dy;
+            az += wq * rz + wsc * (double)p.dz;
+        }
+    }
+    return block_sum3<NTH>(ax, ay, az, sh);
 }
 
-// Far-tile correction of ion i (see fixup_ion): each warp takes whole 128-ion tiles that
-// the Coulomb kernel treated as far from the ion's own tile, and each pair term
-// f(u) = q u / |u|^3 of the hi-part difference u = fl(hi_j - hi_i) gets
+// Far fix-up of ion i, chunk c of nch: the warps take the 128-ion tiles t = (c + m nch) W
+// + w (W warps per block) that the Coulomb kernel treated as far from the ion's own
+// tile, and each pair term f(u) = q u / |u|^3 of the hi-part difference u = fl(hi_j - hi_i)
+// gets
 //     delta = q y3 (D - 3 y^2 (u.D) u),   D = (lo_j - lo_i) + (hi_j - hi_i - u),
 // the exact first-order change to the float-float difference (|D|/|u| ~ 1e-7, so the
-// second order is far below FP32 rounding).  y and y3 are formed as the kernel formed
-// them.  Summed in FP32 per thread (the terms are small), in FP64 across the block.
+// second order is far below FP32 rounding); y and y3 are formed as the kernel formed
+// them.  Summed in FP32 per thread (the terms are small), in FP64 across the block;
+// returns the correction of P_i (SI, thread 0).
 template <int NTH>
-__device__ void fixup_far(const SgCloud& cl, int i, const float* __restrict__ c32,
-                          int npad_total, double* __restrict__ out, int n_total,
-                          const float* __restrict__ bbox, FixupShared<NTH>& sh) {
+__device__ Corr3 fixup_far(const SgCloud& cl, int i, const float* __restrict__ c32,
+                           int npad_total, const float* __restrict__ bbox, int c, int nch,
+                           FixupShared<NTH>& sh) {
+    constexpr int W = NTH / 32;
     const int li = threadIdx.x;
     const int warp = li >> 5, lane = li & 31;
     const size_t NP = (size_t)npad_total;
@@ -1028,7 +1027,7 @@ __device__ void fixup_far(const SgCloud& cl, int i, const float* __restrict__ c3
     const float* ibox = bbox + 8 * (size_t)(cl.tile0 + itile);
     const float dfar2 = cl.dfar * cl.dfar;
     float fx = 0.f, fy = 0.f, fz = 0.f;
-    for (int t = warp; t < nt; t += NTH / 32) {
+    for (int t = c * W + warp; t < nt; t += nch * W) {
         // the Coulomb kernel's far test for this (leaf, tile) pair, uniform per warp
         if (t == itile || !(box_dist2(ibox, bbox + 8 * (size_t)(cl.tile0 + t)) > dfar2)) continue;
         for (int jj = lane; jj < 128; jj += 32) {
@@ -1054,30 +1053,35 @@ __device__ void fixup_far(const SgCloud& cl, int i, const float* __restrict__ c3
             fz = fmaf(qy3, fmaf(-s3, uz, dz), fz);
         }
     }
-    double ax = fx, ay = fy, az = fz;
-    for (int o = 16; o > 0; o >>= 1) {
-        ax += __shfl_down_sync(0xffffffffu, ax, o);
-        ay += __shfl_down_sync(0xffffffffu, ay, o);
-        az += __shfl_down_sync(0xffffffffu, az, o);
+    Corr3 r = block_sum3<NTH>(fx, fy, fz, sh);
+    // frame sums of q u / r^3 -> P (SI), as the kernel's epilogue scales them
+    const double sc = -(cl.invL * cl.invL) * cl.qscale;
+    r.x *= sc;
+    r.y *= sc;
+    r.z *= sc;
+    return r;
+}
+
+// Whole fix-up of one flagged ion by one block: kFixFar (k-d ordered shapes) and/or
+// kFixNear, added to out by thread 0.  The j-ions are taken in a fixed order, so the
+// result does not depend on which block runs it or when.
+template <int NTH>
+__device__ void fixup_ion(const SgCloud& cl, int i, double pf, int kind,
+                          const float* __restrict__ c32, const double* __restrict__ c64,
+                          int npad_total, double* __restrict__ out, int n_total,
+                          const float* __restrict__ bbox, FixupShared<NTH>& sh) {
+    Corr3 r{0.0, 0.0, 0.0};
+    if ((kind & kFixFar) && bbox != nullptr) r = fixup_far<NTH>(cl, i, c32, npad_total, bbox, 0, 1, sh);
+    if (kind & kFixNear) {
+        const Corr3 q = fixup_near<NTH>(cl, i, pf, c32, c64, npad_total, bbox, sh);
+        r.x += q.x;
+        r.y += q.y;
+        r.z += q.z;
     }
-    if (lane == 0) {
-        sh.wsum[warp][0] = ax;
-        sh.wsum[warp][1] = ay;
-        sh.wsum[warp][2] = az;
-    }
-    __syncthreads();
-    if (li == 0) {
-        double sx = 0.0, sy = 0.0, sz = 0.0;
-        for (int w = 0; w < NTH / 32; w++) {
-            sx += sh.wsum[w][0];
-            sy += sh.wsum[w][1];
-            sz += sh.wsum[w][2];
-        }
-        // frame sums of q u / r^3 -> P (SI), as the kernel's epilogue scales them
-        const double sc = -(cl.invL * cl.invL) * cl.qscale;
-        out[i] += sc * sx;
-        out[(size_t)n_total + i] += sc * sy;
-        out[2 * (size_t)n_total + i] += sc * sz;
+    if (threadIdx.x == 0) {
+        out[i] += r.x;
+        out[(size_t)n_total + i] += r.y;
+        out[2 * (size_t)n_total + i] += r.z;
     }
     __syncthreads();
 }
@@ -1159,21 +1163,70 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
         fixup_ion(cl, flist[k], fpf[k], fkind[k], c32, c64, npad_total, out, n_total, bbox, sh);
 }
 
-// The flagged ions of a whole batch, one block per ion (blocks stride over the list).
-// Larger blocks than the reduction's: a far fix-up scans the whole cloud, and with one
-// block per SM its dependent chains need the warps.
+// The flagged ions of a whole batch.  Each of the first kChunkedCap listed ions is
+// kFarChunks work units (unit 0 also does the near fix-up), so that a far fix-up, which
+// scans the whole cloud, is spread over blocks; each unit leaves its correction in
+// fix_part and the last unit of an ion (counted in fix_done) adds them to out in chunk
+// order -- the result does not depend on the order the units ran in.  Ions past the cap
+// are one unit each.  Blocks are larger than the reduction's: a unit with only a few
+// warps per SM would wait on its own dependent chains.
 constexpr int kFixupThreads = 1024;
 __global__ void __launch_bounds__(kFixupThreads) coulomb_fixup_kernel(
     const SgCloud* __restrict__ clouds, const float* __restrict__ c32,
     const double* __restrict__ c64, int npad_total, double* __restrict__ out, int n_total,
     const int* __restrict__ fix_list, const double* __restrict__ fix_pf,
-    const float* __restrict__ bbox) {
+    const float* __restrict__ bbox, double* __restrict__ fix_part, int* __restrict__ fix_done) {
     __shared__ FixupShared<kFixupThreads> sh;
+    __shared__ int last;
     const int count = fix_list[0];
-    for (int k = blockIdx.x; k < count; k += gridDim.x) {
+    const int nchunked = min(count, kChunkedCap);
+    const int units = nchunked * kFarChunks + (count - nchunked);
+    for (int u = blockIdx.x; u < units; u += gridDim.x) {
+        if (u >= nchunked * kFarChunks) {
+            const int k = nchunked + (u - nchunked * kFarChunks);
+            const int ck = fix_list[2 + 2 * k];
+            fixup_ion<kFixupThreads>(clouds[ck & 0x0FFFFFFF], fix_list[1 + 2 * k], fix_pf[k],
+                                     ck >> 28, c32, c64, npad_total, out, n_total, bbox, sh);
+            continue;
+        }
+        const int k = u / kFarChunks, c = u % kFarChunks;
+        const int i = fix_list[1 + 2 * k];
         const int ck = fix_list[2 + 2 * k];
-        fixup_ion(clouds[ck & 0x0FFFFFFF], fix_list[1 + 2 * k], fix_pf[k], ck >> 28, c32, c64,
-                  npad_total, out, n_total, bbox, sh);
+        const SgCloud& cl = clouds[ck & 0x0FFFFFFF];
+        const int kind = ck >> 28;
+        Corr3 r{0.0, 0.0, 0.0};
+        if ((kind & kFixFar) && bbox != nullptr)
+            r = fixup_far<kFixupThreads>(cl, i, c32, npad_total, bbox, c, kFarChunks, sh);
+        if (c == 0 && (kind & kFixNear)) {
+            const Corr3 q = fixup_near<kFixupThreads>(cl, i, fix_pf[k], c32, c64, npad_total, bbox, sh);
+            r.x += q.x;
+            r.y += q.y;
+            r.z += q.z;
+        }
+        if (threadIdx.x == 0) {
+            double* fp = fix_part + ((size_t)k * kFarChunks + c) * 3;
+            fp[0] = r.x;
+            fp[1] = r.y;
+            fp[2] = r.z;
+            __threadfence();
+            last = atomicAdd(&fix_done[k], 1) == kFarChunks - 1;
+        }
+        __syncthreads();
+        if (last && threadIdx.x == 0) {
+            __threadfence();
+            const volatile double* vp = fix_part + (size_t)k * kFarChunks * 3;
+            double sx = 0.0, sy = 0.0, sz = 0.0;
+            for (int q = 0; q < kFarChunks; q++) {
+                sx += vp[3 * q];
+                sy += vp[3 * q + 1];
+                sz += vp[3 * q + 2];
+            }
+            out[i] += sx;
+            out[(size_t)n_total + i] += sy;
+            out[2 * (size_t)n_total + i] += sz;
+            fix_done[k] = 0;  // ready for the next call
+        }
+        __syncthreads();
     }
 }
 
@@ -1316,7 +1369,8 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
         // (flagged ions are a small fraction: small batches get a small grid)
         const int grid = n_total / 256 < 1 ? 1 : (n_total / 256 > kFixupBlocks ? kFixupBlocks : n_total / 256);
         coulomb_fixup_kernel<<<grid, kFixupThreads, 0, s>>>(
-            a.clouds, a.c32, a.c64, a.npad_total, out, n_total, a.fix_list, a.fix_pf, bbox);
+            a.clouds, a.c32, a.c64, a.npad_total, out, n_total, a.fix_list, a.fix_pf, bbox,
+            a.fix_part, a.fix_done);
     } else {
         coulomb_reduce_kernel<false, false><<<n_rows, SG_ROWS, 0, s>>>(
             rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, nullptr,

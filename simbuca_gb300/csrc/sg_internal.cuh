@@ -31,6 +31,9 @@
 // Arrays of a Coulomb partial-sum slot: x, y, z, and the FP32c conditioning estimates
 // of the near tiles and of the far tiles (sums of squared 32-ion partial sums).
 #define SG_PART_ARRAYS 5
+// FP32c fix-up kernel: work units per listed ion, and the listed ions that get them
+#define SG_FIX_UNITS 16
+#define SG_FIX_CHUNKED_CAP 4096
 
 // Bounded device waits: a wait gives up after this many nanoseconds of
 // %globaltimer and raises SG_TIMEOUT in the context's error word.
@@ -365,6 +368,9 @@ struct SgCoulombArgs {
     // per flagged ion its global index and cloud (ints) and |P| in frame units
     int* fix_list;
     double* fix_pf;
+    // per listed ion and work unit its correction, and the count of finished units
+    double* fix_part;
+    int* fix_done;
     // k-d ordered shapes: accumulate the far tiles' conditioning estimate s2f in this
     // call (it costs the kernel ~4 %); otherwise the slots keep the last call's values
     int far_estimate;
