@@ -69,7 +69,7 @@ struct Problem {
     std::vector<int> hspec0;
     std::vector<double> hmass0;
     double *pmass = nullptr, *pmass0 = nullptr;  // print masses (dissociation), both orders
-    int* fix_list = nullptr;   // FP32c fix-up work list: count, then (ion, cloud) pairs
+    int* fix_list = nullptr;   // FP32c fix-up work lists: counts, then (ion, cloud) pairs
     double* fix_pf = nullptr;
     double* fix_part = nullptr;  // fix-up work units' corrections [listed][units][3]
     int* fix_done = nullptr;     // finished units per listed ion (zero between calls)
@@ -426,9 +426,10 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(cudaMemset(P.spec, 0, N * sizeof(int)));
     CK(dalloc(&P.pmass, N));
     CK(dalloc(&P.pmass0, N));
-    CK(dalloc(&P.fix_list, 1 + 2 * N));
-    CK(dalloc(&P.fix_pf, N));
-    CK(cudaMemset(P.fix_list, 0, sizeof(int)));
+    // two lists (near-only ions; ions with a far fix-up): counts, then N pairs each
+    CK(dalloc(&P.fix_list, 2 + 4 * N));
+    CK(dalloc(&P.fix_pf, 2 * N));
+    CK(cudaMemset(P.fix_list, 0, 2 * sizeof(int)));
     CK(dalloc(&P.fix_part, (size_t)SG_FIX_CHUNKED_CAP * SG_FIX_UNITS * 3));
     CK(dalloc(&P.fix_done, SG_FIX_CHUNKED_CAP));
     CK(cudaMemset(P.fix_done, 0, sizeof(int) * SG_FIX_CHUNKED_CAP));

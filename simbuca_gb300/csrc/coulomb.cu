@@ -869,7 +869,7 @@ constexpr int kFixNear = 1, kFixFar = 2;
 // tiles listed for the fix-up scan of one ion in k-d order
 constexpr int kNearCap = 1024;
 // blocks of the fix-up kernel (each takes every kFixupBlocks-th work unit)
-constexpr int kFixupBlocks = 256;
+constexpr int kFixupBlocks = 512;
 // work units of one listed ion in the fix-up kernel, and the listed ions that get them
 constexpr int kFarChunks = SG_FIX_UNITS;
 constexpr int kChunkedCap = SG_FIX_CHUNKED_CAP;
@@ -1091,7 +1091,8 @@ __device__ void fixup_ion(const SgCloud& cl, int i, double pf, int kind,
 // or whose far terms are large next to |P| (sqrt(s2f) > 0.5 |P|) is fixed up
 // (fixup_ion): INBLOCK, by this block right away (small batches, where a second launch
 // costs more than the work); otherwise it is put on the work list of
-// coulomb_fixup_kernel (ion index; cloud | kind << 28; |P| in frame units).
+// coulomb_fixup_kernel (ion index; cloud | kind << 28; |P| in frame units): the ions
+// with only a near fix-up in one list, those with a far one in the other.
 template <bool F32, bool INBLOCK>
 __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     const SgRowBlock* __restrict__ rows, const SgCloud* __restrict__ clouds,
@@ -1135,10 +1136,13 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     if (!F32) return;
     if (!INBLOCK) {
         if (kind) {
-            const int at = atomicAdd(fix_list, 1);
-            fix_list[1 + 2 * at] = i;
-            fix_list[2 + 2 * at] = rb.cloud | (kind << 28);
-            fix_pf[at] = pf;
+            // two lists: near-only ions from fix_list[2], the others from fix_list[2 + 2N]
+            const bool far = (kind & kFixFar) != 0;
+            const int at = atomicAdd(fix_list + (far ? 1 : 0), 1);
+            const size_t base = far ? 2 + 2 * (size_t)n_total : 2;
+            fix_list[base + 2 * at] = i;
+            fix_list[base + 2 * at + 1] = rb.cloud | (kind << 28);
+            fix_pf[(far ? (size_t)n_total : 0) + at] = pf;
             if (counters != nullptr) atomicAdd(counters, 1);
         }
         return;
@@ -1163,13 +1167,14 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
         fixup_ion(cl, flist[k], fpf[k], fkind[k], c32, c64, npad_total, out, n_total, bbox, sh);
 }
 
-// The flagged ions of a whole batch.  Each of the first kChunkedCap listed ions is
-// kFarChunks work units (unit 0 also does the near fix-up), so that a far fix-up, which
-// scans the whole cloud, is spread over blocks; each unit leaves its correction in
-// fix_part and the last unit of an ion (counted in fix_done) adds them to out in chunk
-// order -- the result does not depend on the order the units ran in.  Ions past the cap
-// are one unit each.  Blocks are larger than the reduction's: a unit with only a few
-// warps per SM would wait on its own dependent chains.
+// The flagged ions of a whole batch.  A near-only ion is one work unit.  Each of the
+// first kChunkedCap ions with a far fix-up is kFarChunks units (unit 0 also does its near
+// fix-up), so that the far scan of the whole cloud is spread over blocks: each unit leaves
+// its correction in fix_part and the last unit of the ion (counted in fix_done) adds them
+// to out in unit order -- the result does not depend on the order the units ran in.
+// Units are numbered so that every ion's first units come first.  Far ions past the cap
+// are one unit each.  Blocks are larger than the reduction's: a unit with only a few warps
+// per SM would wait on its own dependent chains.
 constexpr int kFixupThreads = 1024;
 __global__ void __launch_bounds__(kFixupThreads) coulomb_fixup_kernel(
     const SgCloud* __restrict__ clouds, const float* __restrict__ c32,
@@ -1178,27 +1183,37 @@ __global__ void __launch_bounds__(kFixupThreads) coulomb_fixup_kernel(
     const float* __restrict__ bbox, double* __restrict__ fix_part, int* __restrict__ fix_done) {
     __shared__ FixupShared<kFixupThreads> sh;
     __shared__ int last;
-    const int count = fix_list[0];
-    const int nchunked = min(count, kChunkedCap);
-    const int units = nchunked * kFarChunks + (count - nchunked);
+    const int cn = fix_list[0], cf = fix_list[1];
+    const int* near_list = fix_list + 2;
+    const int* far_list = fix_list + 2 + 2 * (size_t)n_total;
+    const double* far_pf = fix_pf + n_total;
+    const int cfc = min(cf, kChunkedCap);
+    const int units = cn + cfc * kFarChunks + (cf - cfc);
     for (int u = blockIdx.x; u < units; u += gridDim.x) {
-        if (u >= nchunked * kFarChunks) {
-            const int k = nchunked + (u - nchunked * kFarChunks);
-            const int ck = fix_list[2 + 2 * k];
-            fixup_ion<kFixupThreads>(clouds[ck & 0x0FFFFFFF], fix_list[1 + 2 * k], fix_pf[k],
+        if (u < cn) {
+            const int ck = near_list[2 * u + 1];
+            fixup_ion<kFixupThreads>(clouds[ck & 0x0FFFFFFF], near_list[2 * u], fix_pf[u],
                                      ck >> 28, c32, c64, npad_total, out, n_total, bbox, sh);
             continue;
         }
-        const int k = u / kFarChunks, c = u % kFarChunks;
-        const int i = fix_list[1 + 2 * k];
-        const int ck = fix_list[2 + 2 * k];
+        const int v = u - cn;
+        if (v >= cfc * kFarChunks) {
+            const int k = cfc + (v - cfc * kFarChunks);
+            const int ck = far_list[2 * k + 1];
+            fixup_ion<kFixupThreads>(clouds[ck & 0x0FFFFFFF], far_list[2 * k], far_pf[k],
+                                     ck >> 28, c32, c64, npad_total, out, n_total, bbox, sh);
+            continue;
+        }
+        const int k = v % cfc, c = v / cfc;
+        const int i = far_list[2 * k];
+        const int ck = far_list[2 * k + 1];
         const SgCloud& cl = clouds[ck & 0x0FFFFFFF];
         const int kind = ck >> 28;
         Corr3 r{0.0, 0.0, 0.0};
-        if ((kind & kFixFar) && bbox != nullptr)
+        if (bbox != nullptr)
             r = fixup_far<kFixupThreads>(cl, i, c32, npad_total, bbox, c, kFarChunks, sh);
         if (c == 0 && (kind & kFixNear)) {
-            const Corr3 q = fixup_near<kFixupThreads>(cl, i, fix_pf[k], c32, c64, npad_total, bbox, sh);
+            const Corr3 q = fixup_near<kFixupThreads>(cl, i, far_pf[k], c32, c64, npad_total, bbox, sh);
             r.x += q.x;
             r.y += q.y;
             r.z += q.z;
@@ -1360,7 +1375,7 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
                 nullptr, a.c32, a.c64, bbox);
             return cudaGetLastError();
         }
-        cudaError_t e = cudaMemsetAsync(a.fix_list, 0, sizeof(int), s);
+        cudaError_t e = cudaMemsetAsync(a.fix_list, 0, 2 * sizeof(int), s);
         if (e != cudaSuccess) return e;
         coulomb_reduce_kernel<true, false><<<n_rows, SG_ROWS, 0, s>>>(
             rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, a.fix_list,
