@@ -1173,10 +1173,10 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
 // its correction in fix_part and the last unit of the ion (counted in fix_done) adds them
 // to out in unit order -- the result does not depend on the order the units ran in.
 // Units are numbered so that every ion's first units come first.  Far ions past the cap
-// are one unit each.  Blocks are larger than the reduction's: a unit with only a few warps
-// per SM would wait on its own dependent chains.
-constexpr int kFixupThreads = 1024;
-__global__ void __launch_bounds__(kFixupThreads) coulomb_fixup_kernel(
+// are one unit each.  Blocks of 256 threads, three per SM (80 registers, no spills):
+// the units of a 65,536-ion call (about 170) run in one wave.
+constexpr int kFixupThreads = 256;
+__global__ void __launch_bounds__(kFixupThreads, 3) coulomb_fixup_kernel(
     const SgCloud* __restrict__ clouds, const float* __restrict__ c32,
     const double* __restrict__ c64, int npad_total, double* __restrict__ out, int n_total,
     const int* __restrict__ fix_list, const double* __restrict__ fix_pf,
