@@ -358,6 +358,12 @@ void set_frame(SgCloud& cl, const double* pos_aos, int off) {
     // far tiles (sorted kernel): beyond every capped pair, and far enough that the
     // high parts alone give the pair distance to ~1e-6
     cl.dfar = (float)std::max(0.25, 1.01 * rc);
+    // Far fix-up threshold.  The error of the hi-only far terms is ~c sqrt(s2f) with c
+    // growing as the square root of the ion density in frame units, i.e. of n (numpy
+    // model of the kernel's arithmetic: c ~ 1.2e-6 for the 1M-ion spheroid, ~2.5e-7 for
+    // the 65,536-ion Gaussian cloud); fixing ions with c sqrt(s2f) > 5e-7 |P| keeps them
+    // at half the 1e-6 bound: sqrt(s2f) > 0.5 |P| from ~1M ions up, 2 |P| at 65,536.
+    cl.kfar2 = (float)(0.25 * std::max(1.0, 1048576.0 / std::max(n, 1)));
 }
 
 // k-d tree order of one cloud: recursive median splits along the widest axis, the

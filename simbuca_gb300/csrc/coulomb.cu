@@ -857,12 +857,11 @@ __global__ void __launch_bounds__(NT) coulomb_fp64_kernel(const double* __restri
 // its far terms (the centre of a uniform cloud).  Its size tracks sqrt(s2f), the far
 // tiles' conditioning estimate: on the 1M-ion spheroid and the 65,536-ion Gaussian cloud
 // (numpy model of the kernel's arithmetic) the relative error of P_i stayed below
-// 1.3e-6 sqrt(s2f)/|P_i|.  An ion with sqrt(s2f) > 0.5 |P_i| gets the exact first-order
-// correction of every far pair term (fixup_ion), which leaves it at the near tiles'
-// FP32 accuracy.
+// 1.3e-6 sqrt(s2f)/|P_i|, the constant growing with the ion density.  An ion with
+// s2f > SgCloud::kfar2 |P_i|^2 gets the exact first-order correction of every far pair
+// term (fixup_ion), which leaves it at the near tiles' FP32 accuracy.
 // ---------------------------------------------------------------------------
 constexpr double kKappa2 = 2.25;
-constexpr double kKappaFar2 = 0.25;
 // kinds of fix-up of a flagged ion
 constexpr int kFixNear = 1, kFixFar = 2;
 
@@ -1088,7 +1087,7 @@ __device__ void fixup_ion(const SgCloud& cl, int i, double pf, int kind,
 
 // Sums the j-chunk partials of each ion (x, y, z and the FP32c conditioning estimates
 // s2, s2f) into out.  FP32c: an ion whose near terms cancel strongly (sqrt(s2) > 1.5 |P|)
-// or whose far terms are large next to |P| (sqrt(s2f) > 0.5 |P|) is fixed up
+// or whose far terms are large next to |P| (s2f > SgCloud::kfar2 |P|^2) is fixed up
 // (fixup_ion): INBLOCK, by this block right away (small batches, where a second launch
 // costs more than the work); otherwise it is put on the work list of
 // coulomb_fixup_kernel (ion index; cloud | kind << 28; |P| in frame units): the ions
@@ -1130,7 +1129,7 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
         if (F32) {
             pf = sqrt(px * px + py * py + pz * pz) * (cl.L * cl.L);  // frame units
             kind = (s2 > kKappa2 * pf * pf ? kFixNear : 0) |
-                   (s2f > kKappaFar2 * pf * pf ? kFixFar : 0);
+                   (s2f > (double)cl.kfar2 * pf * pf ? kFixFar : 0);
         }
     }
     if (!F32) return;

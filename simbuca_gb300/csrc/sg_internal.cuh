@@ -72,7 +72,7 @@ struct SgCloud {
     int32_t tile0;       // first entry of this cloud in the 128-ion tile bounding boxes
     float dfar;          // FP32c: tiles farther apart than this (frame units) use hi parts only
     float wc;            // FP32c close-pair threshold on 1/r^3 (frame units)
-    float pad2;
+    float kfar2;         // FP32c: far fix-up when s2f > kfar2 |P|^2 (k-d ordered shapes)
     sg_field_params fp;
     long long rec_off;   // recorder: first double of this cloud's record ring
     int32_t nsel;        // recorder: ions kept per record (every stride-th in caller order)
