@@ -197,7 +197,11 @@ def stage_roofline(args, w, st, attempts):
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "bytes_per_ion_attempt": STAGE_BYTES_PER_ION,
             "launches": st["stage_launches"], "ms": st["stage_ms"], "peak_source": src,
-            "note": "per-attempt working set below the 129 MB L2 reads partly from L2"}
+            "note": ("per-attempt working set below the 129 MB L2: reads partly from L2"
+                     if STAGE_BYTES_PER_ION * w.n_total < 129e6 else
+                     "per-attempt working set above the 129 MB L2")
+            + "; these kernels are bound by the FP64 pipe first (~80 FP64 operations "
+              "per ion and stage)"}
 
 
 def apply_step_control(args, batch) -> str:
