@@ -57,6 +57,14 @@ def init_weights(seed: int = 0) -> np.ndarray:
     return np.concatenate(parts).astype(np.float32)
 
 
+def drop_features(w: np.ndarray, feats) -> np.ndarray:
+    """Weights that ignore the given inputs: their first-layer columns set to zero
+    (trained with those inputs zeroed, they then stay zero)."""
+    w = np.array(w, np.float32, copy=True)
+    w[:64 * 16].reshape(64, 16)[:, list(feats)] = 0.0
+    return w
+
+
 def targets(h_prev, h, err):
     err = np.maximum(err, 1e-12)
     y = np.log(h * err ** -0.2 / np.where(h_prev > 0, h_prev, h))
@@ -122,6 +130,9 @@ def main():
     ap.add_argument("--safety", default="0.75,0.8,0.85,0.9")
     ap.add_argument("--eval", default="learned_4k", choices=sorted(configs.WORKLOADS))
     ap.add_argument("--no-fp64-eval", action="store_true")
+    ap.add_argument("--drop-features", default="",
+                    help="comma-separated input indices the network ignores (e.g. 9, the "
+                         "absolute log step size)")
     ap.add_argument("--max-attempts", type=int, default=100000,
                     help="attempt cap of each evaluation run")
     a = ap.parse_args()
@@ -140,10 +151,13 @@ def main():
         print(f"collected {len(yi)} steps from {w.name}", flush=True)
     X = np.concatenate(X)
     y = np.concatenate(y)
+    dropped = [int(v) for v in a.drop_features.split(",") if v.strip()]
+    if dropped:
+        X[:, dropped] = 0.0
     # hold out every fifth sample to compare the MLP with the reference controller's rule
     rng = np.random.default_rng(0)
     test = rng.random(len(y)) < 0.2
-    w0 = init_weights(0)
+    w0 = drop_features(init_weights(0), dropped)
     wts, hist = ctx.mlp_train(X[~test], y[~test], w0, iters=300 if a.quick else 4000,
                               batch=256, lr=2e-3)
     pred = ctx.mlp_forward(X[test], wts)
@@ -158,7 +172,7 @@ def main():
     np.save(os.path.join(a.out, "proposer_weights.npy"), wts)
     ev = (configs.learned_4k(sim_time=a.horizon) if a.eval == "learned_4k"
           else configs.WORKLOADS[a.eval]())
-    res = {"eval_workload": a.eval, "train_samples": int(len(y)),
+    res = {"eval_workload": a.eval, "dropped_features": dropped, "train_samples": int(len(y)),
            "train_loss_first": float(hist[0]),
            "train_loss_last": float(hist[-1]), "heldout_mse_mlp": mse_mlp,
            "heldout_mse_controller_rule": mse_ctrl, "horizon_s": a.horizon,
