@@ -54,6 +54,16 @@ def test_null_context_is_rejected(lib):
     assert lib.sg_sync(None) == abi.SG_BAD_ARG
     assert lib.sg_batch_attempts(None, 1) == abi.SG_BAD_ARG
     assert lib.sg_create(0, None) == abi.SG_BAD_ARG
+    assert lib.sg_stage_timing(None, None, None) == abi.SG_BAD_ARG
+    assert lib.sg_kernel_timing(None, None, None, None) == abi.SG_BAD_ARG
+    assert lib.sg_batch_set_controller_safety(None, 0.9) == abi.SG_BAD_ARG
+    assert lib.sg_batch_set_proposer(None, None, 0.9) == abi.SG_BAD_ARG
+    assert lib.sg_dp45_step(None, None) == abi.SG_BAD_ARG
+    assert lib.sg_batch_run(None, 1, None) == abi.SG_BAD_ARG
+
+
+def test_status_string_io(lib):
+    assert lib.sg_status_string(abi.SG_IO_ERR) == b"file could not be read or written"
 
 
 STRUCTS = {
