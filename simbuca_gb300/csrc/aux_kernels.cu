@@ -22,6 +22,7 @@ __global__ void __launch_bounds__(128) cunbody_kernel(const double* __restrict__
                                                       const double* __restrict__ mj,
                                                       const double* __restrict__ xi, double eps2,
                                                       double* __restrict__ ai, int ni, int nj) {
+    sg_griddep_wait();
     __shared__ double t[4][128];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool act = i < ni;
@@ -65,6 +66,7 @@ __global__ void __launch_bounds__(128) cunbody_kernel(const double* __restrict__
 constexpr int kProbeIters = 4096;
 
 __global__ void probe_ffma(float* sink, float a, float b) {
+    sg_griddep_wait();
     float v[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) v[q] = threadIdx.x * 1e-3f + q;
@@ -79,6 +81,7 @@ __global__ void probe_ffma(float* sink, float a, float b) {
 }
 
 __global__ void probe_ffma2(float* sink, float a, float b) {
+    sg_griddep_wait();
     unsigned long long v[4], A, B;
     asm("mov.b64 %0, {%1, %1};" : "=l"(A) : "f"(a));
     asm("mov.b64 %0, {%1, %1};" : "=l"(B) : "f"(b));
@@ -103,6 +106,7 @@ __global__ void probe_ffma2(float* sink, float a, float b) {
 }
 
 __global__ void probe_dfma(float* sink, double a, double b) {
+    sg_griddep_wait();
     double v[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) v[q] = threadIdx.x * 1e-3 + q;
@@ -122,7 +126,7 @@ __global__ void probe_dfma(float* sink, double a, double b) {
 cudaError_t sg_cunbody_launch(const double* xj, const double* mj, const double* xi, double eps2,
                               double* ai, int ni, int nj, cudaStream_t st) {
     if (ni <= 0) return cudaSuccess;
-    cunbody_kernel<<<(ni + 127) / 128, 128, 0, st>>>(xj, mj, xi, eps2, ai, ni, nj);
+    sg_launch(cunbody_kernel, (ni + 127) / 128, 128, 0, st, xj, mj, xi, eps2, ai, ni, nj);
     return cudaGetLastError();
 }
 
@@ -130,9 +134,9 @@ cudaError_t sg_cunbody_launch(const double* xj, const double* mj, const double* 
 // 2 * 8 * iters * blocks * threads (FP32 / FP32x2), iters/16 for FP64.
 cudaError_t sg_probe_launch(int which, int blocks, int threads, float* sink, cudaStream_t st) {
     switch (which) {
-        case 0: probe_ffma<<<blocks, threads, 0, st>>>(sink, 0.999f, 1e-4f); break;
-        case 1: probe_ffma2<<<blocks, threads, 0, st>>>(sink, 0.999f, 1e-4f); break;
-        case 2: probe_dfma<<<blocks, threads, 0, st>>>(sink, 0.999, 1e-4); break;
+        case 0: sg_launch(probe_ffma, blocks, threads, 0, st, sink, 0.999f, 1e-4f); break;
+        case 1: sg_launch(probe_ffma2, blocks, threads, 0, st, sink, 0.999f, 1e-4f); break;
+        case 2: sg_launch(probe_dfma, blocks, threads, 0, st, sink, 0.999, 1e-4); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

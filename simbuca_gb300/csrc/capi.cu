@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <ctime>
 #include <mutex>
@@ -91,6 +92,10 @@ struct TimedLaunch {
 
 // O(N) kernels of one attempt timed by the kernel-timing graph (at most)
 constexpr int kStageMarks = 12;
+
+// Launches may use programmatic dependent launch (sg_launch): set while the untimed
+// attempt graph is captured, unless SIMGB_PDL=0 in the environment.
+int g_sg_pdl = 0;
 
 struct sg_ctx {
     int device = 0;
@@ -768,7 +773,11 @@ int capture_attempt(sg_ctx* ctx, Problem& P, bool timed, cudaGraphExec_t* out) {
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     ctx->capture_events = timed ? 0 : -1;
     ctx->capture_stage = timed ? 0 : -1;
+    // the timed graph has event nodes between its kernels: plain launches there
+    const char* pdl_env = getenv("SIMGB_PDL");
+    g_sg_pdl = (!timed && !(pdl_env && pdl_env[0] == '0')) ? 1 : 0;
     int st = enqueue_attempt(ctx, P);
+    g_sg_pdl = 0;
     ctx->capture_events = -1;
     if (timed) ctx->stage_pairs = ctx->capture_stage;
     ctx->capture_stage = -1;

@@ -326,6 +326,7 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
                                                             const SgCtrl* __restrict__ ctrl,
                                                             double* __restrict__ part,
                                                             int npad_total, int* errword) {
+    sg_griddep_wait();
     constexpr int T = SG_TILE;
     __shared__ __align__(128) float tile[SG_STAGES][7][T];
     __shared__ __align__(8) uint64_t full[SG_STAGES];
@@ -560,6 +561,7 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
                                                             double* __restrict__ part,
                                                             int npad_total, int* errword,
                                                             const float* __restrict__ bbox) {
+    sg_griddep_wait();
     constexpr int T = TJ;  // j-tile: a multiple of the 128-ion leaves
     __shared__ __align__(128) float tile[STAGES][7][T];
     __shared__ __align__(8) uint64_t full[STAGES];
@@ -782,6 +784,7 @@ __global__ void __launch_bounds__(NT) coulomb_fp64_kernel(const double* __restri
                                                            const SgCtrl* __restrict__ ctrl,
                                                            double* __restrict__ part,
                                                            int npad_total) {
+    sg_griddep_wait();
     constexpr int T = NT;
     __shared__ double tile[4][T];
     const SgWorkItem it = items[blockIdx.x];
@@ -1099,6 +1102,7 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     double* __restrict__ out, int n_total, int* __restrict__ counters,
     int* __restrict__ fix_list, double* __restrict__ fix_pf, const float* __restrict__ c32,
     const double* __restrict__ c64, const float* __restrict__ bbox) {
+    sg_griddep_wait();
     const SgRowBlock rb = rows[blockIdx.x];
     if (ctrl != nullptr &&
         (ctrl[rb.cloud].done || ctrl[rb.cloud].hold || ctrl[rb.cloud].status != SG_OK))
@@ -1180,6 +1184,7 @@ __global__ void __launch_bounds__(kFixupThreads, 3) coulomb_fixup_kernel(
     const double* __restrict__ c64, int npad_total, double* __restrict__ out, int n_total,
     const int* __restrict__ fix_list, const double* __restrict__ fix_pf,
     const float* __restrict__ bbox, double* __restrict__ fix_part, int* __restrict__ fix_done) {
+    sg_griddep_wait();
     __shared__ FixupShared<kFixupThreads> sh;
     __shared__ int last;
     const int cn = fix_list[0], cf = fix_list[1];
@@ -1263,93 +1268,93 @@ cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s) {
     if (a.n_items <= 0) return cudaSuccess;
     switch (a.variant) {
         case 1:
-            coulomb_fp32c_kernel<128, 2><<<a.n_items, 128, 0, s>>>(
+            sg_launch(coulomb_fp32c_kernel<128, 2>, a.n_items, 128, 0, s, 
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
             break;
         case 2:
-            coulomb_fp32c_kernel<256, 2><<<a.n_items, 256, 0, s>>>(
+            sg_launch(coulomb_fp32c_kernel<256, 2>, a.n_items, 256, 0, s, 
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
             break;
         case 3:
-            coulomb_fp32c_kernel<64, 4><<<a.n_items, 64, 0, s>>>(
+            sg_launch(coulomb_fp32c_kernel<64, 4>, a.n_items, 64, 0, s, 
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
             break;
         case 5:
-            coulomb_fp32c_kernel<64, 2><<<a.n_items, 64, 0, s>>>(
+            sg_launch(coulomb_fp32c_kernel<64, 2>, a.n_items, 64, 0, s, 
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
             break;
         case 6:
-            coulomb_fp32c_kernel<32, 4><<<a.n_items, 32, 0, s>>>(
+            sg_launch(coulomb_fp32c_kernel<32, 4>, a.n_items, 32, 0, s, 
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
             break;
         case SG_C32_SORTED:
-            coulomb_fp32c_sorted_kernel<128, 4, 4, SG_STAGES><<<a.n_items, 128, 0, s>>>(
+            sg_launch(coulomb_fp32c_sorted_kernel<128, 4, 4, SG_STAGES>, a.n_items, 128, 0, s, 
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case SG_C32_SORTED_LEAF:
             // one k-d leaf per block: warps never wait for a slower (near) neighbour
-            coulomb_fp32c_sorted_kernel<32, 4, 16, 3><<<a.n_items, 32, 0, s>>>(
+            sg_launch(coulomb_fp32c_sorted_kernel<32, 4, 16, 3>, a.n_items, 32, 0, s, 
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 8:
             // one leaf per block split over two warps (same far/near decisions)
-            coulomb_fp32c_sorted_kernel<64, 2, 12, 3><<<a.n_items, 64, 0, s>>>(
+            sg_launch(coulomb_fp32c_sorted_kernel<64, 2, 12, 3>, a.n_items, 64, 0, s, 
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 9:
             if (a.far_estimate)
-                coulomb_fp32c_sorted_kernel<128, 1, 8, 3><<<a.n_items, 128, 0, s>>>(
+                sg_launch(coulomb_fp32c_sorted_kernel<128, 1, 8, 3>, a.n_items, 128, 0, s, 
                     a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             else
-                coulomb_fp32c_sorted_kernel<128, 1, 8, 3, SG_TILE, 0, false><<<a.n_items, 128, 0, s>>>(
+                sg_launch(coulomb_fp32c_sorted_kernel<128, 1, 8, 3, SG_TILE, 0, false>, a.n_items, 128, 0, s, 
                     a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 12:
             // as 9 with 256-ion j-tiles: half the ring waits and barriers per pair
             if (a.far_estimate)
-                coulomb_fp32c_sorted_kernel<128, 1, 8, 3, 256><<<a.n_items, 128, 0, s>>>(
+                sg_launch(coulomb_fp32c_sorted_kernel<128, 1, 8, 3, 256>, a.n_items, 128, 0, s, 
                     a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             else
-                coulomb_fp32c_sorted_kernel<128, 1, 8, 3, 256, 0, false><<<a.n_items, 128, 0, s>>>(
+                sg_launch(coulomb_fp32c_sorted_kernel<128, 1, 8, 3, 256, 0, false>, a.n_items, 128, 0, s, 
                     a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 13:
             if (a.far_estimate)
-                coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256><<<a.n_items, 64, 0, s>>>(
+                sg_launch(coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256>, a.n_items, 64, 0, s, 
                     a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             else
-                coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256, 0, false><<<a.n_items, 64, 0, s>>>(
+                sg_launch(coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256, 0, false>, a.n_items, 64, 0, s, 
                     a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 14:
             // as 13 with four j pairs in flight per ion on far tiles
             if (a.far_estimate)
-                coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256, 4><<<a.n_items, 64, 0, s>>>(
+                sg_launch(coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256, 4>, a.n_items, 64, 0, s, 
                     a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             else
-                coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256, 4, false><<<a.n_items, 64, 0, s>>>(
+                sg_launch(coulomb_fp32c_sorted_kernel<64, 2, 9, 3, 256, 4, false>, a.n_items, 64, 0, s, 
                     a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 15:
             // the leaf in one warp (4 ions per thread), 256-ion j-tiles
-            coulomb_fp32c_sorted_kernel<32, 4, 16, 3, 256><<<a.n_items, 32, 0, s>>>(
+            sg_launch(coulomb_fp32c_sorted_kernel<32, 4, 16, 3, 256>, a.n_items, 32, 0, s, 
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 16:
             // as 13 with a 4-stage ring
-            coulomb_fp32c_sorted_kernel<64, 2, 8, 4, 256><<<a.n_items, 64, 0, s>>>(
+            sg_launch(coulomb_fp32c_sorted_kernel<64, 2, 8, 4, 256>, a.n_items, 64, 0, s, 
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword, a.bbox);
             break;
         case 10:
-            coulomb_fp32c_kernel<32, 2><<<a.n_items, 32, 0, s>>>(
+            sg_launch(coulomb_fp32c_kernel<32, 2>, a.n_items, 32, 0, s, 
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
             break;
         case 11:
-            coulomb_fp32c_kernel<32, 1><<<a.n_items, 32, 0, s>>>(
+            sg_launch(coulomb_fp32c_kernel<32, 1>, a.n_items, 32, 0, s, 
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
             break;
         default:
-            coulomb_fp32c_kernel<128, 4><<<a.n_items, 128, 0, s>>>(
+            sg_launch(coulomb_fp32c_kernel<128, 4>, a.n_items, 128, 0, s, 
                 a.c32, a.c64, a.items, a.clouds, a.ctrl, a.part, a.npad_total, a.errword);
     }
     return cudaGetLastError();
@@ -1357,7 +1362,7 @@ cudaError_t sg_launch_coulomb_fp32c(const SgCoulombArgs& a, cudaStream_t s) {
 
 cudaError_t sg_launch_coulomb_fp64(const SgCoulombArgs& a, cudaStream_t s) {
     if (a.n_items <= 0) return cudaSuccess;
-    coulomb_fp64_kernel<SG_C64_THREADS, SG_C64_IPT><<<a.n_items, SG_C64_THREADS, 0, s>>>(
+    sg_launch(coulomb_fp64_kernel<SG_C64_THREADS, SG_C64_IPT>, a.n_items, SG_C64_THREADS, 0, s, 
         a.c64, a.items, a.ctrl, a.part, a.npad_total);
     return cudaGetLastError();
 }
@@ -1369,7 +1374,7 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
     if (fp32c) {
         const float* bbox = sg_variant_sorted(a.variant) ? a.bbox : nullptr;
         if (n_total <= kInBlockFixupMax) {
-            coulomb_reduce_kernel<true, true><<<n_rows, SG_ROWS, 0, s>>>(
+            sg_launch(coulomb_reduce_kernel<true, true>, n_rows, SG_ROWS, 0, s, 
                 rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, nullptr,
                 nullptr, a.c32, a.c64, bbox);
             return cudaGetLastError();
@@ -1382,11 +1387,11 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
         // a block per flagged ion: a fixed grid that strides over however many there are
         // (flagged ions are a small fraction: small batches get a small grid)
         const int grid = n_total / 256 < 1 ? 1 : (n_total / 256 > kFixupBlocks ? kFixupBlocks : n_total / 256);
-        coulomb_fixup_kernel<<<grid, kFixupThreads, 0, s>>>(
+        sg_launch(coulomb_fixup_kernel, grid, kFixupThreads, 0, s, 
             a.clouds, a.c32, a.c64, a.npad_total, out, n_total, a.fix_list, a.fix_pf, bbox,
             a.fix_part, a.fix_done);
     } else {
-        coulomb_reduce_kernel<false, false><<<n_rows, SG_ROWS, 0, s>>>(
+        sg_launch(coulomb_reduce_kernel<false, false>, n_rows, SG_ROWS, 0, s, 
             rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, nullptr,
             nullptr, nullptr, nullptr, nullptr);
     }

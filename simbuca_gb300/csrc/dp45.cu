@@ -103,6 +103,7 @@ __device__ __forceinline__ void tile_bounds(const DpArgs& a, const SgCloud& cl,
 // S = 7, the embedded error of the attempt).
 template <int S>
 __global__ void __launch_bounds__(SG_ROWS) dp_stage_kernel(DpArgs a) {
+    sg_griddep_wait();
     __shared__ double red[SG_ROWS / 32];
     const SgRowBlock rb = a.rows[blockIdx.x];
     const SgCtrl& cs = a.ctrl[rb.cloud];
@@ -222,6 +223,7 @@ __constant__ double c_ck_e[7] = {0,
 // S+1, or for S = 6 the 5th-order solution (into ys) and the embedded error.
 template <int S>
 __global__ void __launch_bounds__(SG_ROWS) ck_stage_kernel(DpArgs a) {
+    sg_griddep_wait();
     __shared__ double red[SG_ROWS / 32];
     const SgRowBlock rb = a.rows[blockIdx.x];
     const SgCtrl& cs = a.ctrl[rb.cloud];
@@ -319,6 +321,7 @@ __global__ void __launch_bounds__(SG_ROWS) ck_stage_kernel(DpArgs a) {
 // InitAcceleraction (bin/ode.cpp:36-59): constant seeds for every ion of a cloud but the
 // last in the caller's order (left as allocated there, zero here); b = c = d = 0.
 __global__ void __launch_bounds__(SG_ROWS) gear_init_kernel(DpArgs a, const int* __restrict__ perm) {
+    sg_griddep_wait();
     const SgRowBlock rb = a.rows[blockIdx.x];
     const SgCloud& cl = a.clouds[rb.cloud];
     const int li = threadIdx.x;
@@ -336,6 +339,7 @@ __global__ void __launch_bounds__(SG_ROWS) gear_init_kernel(DpArgs a, const int*
 
 template <int PHASE>
 __global__ void __launch_bounds__(SG_ROWS) gear_kernel(DpArgs a) {
+    sg_griddep_wait();
     const SgRowBlock rb = a.rows[blockIdx.x];
     const SgCtrl& cs = a.ctrl[rb.cloud];
     if (cs.done || cs.hold || cs.status != SG_OK) return;
@@ -414,6 +418,7 @@ __global__ void dp_control_kernel(SgCloud* __restrict__ clouds, SgCtrl* __restri
                                   const double* __restrict__ err_part, const double* __restrict__ y,
                                   int n_clouds, const int* __restrict__ hold_on_accept,
                                   const SgOp* __restrict__ ops) {
+    sg_griddep_wait();
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n_clouds) return;
     SgCtrl cs = ctrl[c];
@@ -513,6 +518,7 @@ __global__ void dp_control_kernel(SgCloud* __restrict__ clouds, SgCtrl* __restri
 }
 
 __global__ void clear_hold_kernel(SgCtrl* ctrl, int n_clouds) {
+    sg_griddep_wait();
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c < n_clouds) ctrl[c].hold &= ~1;
 }
@@ -520,6 +526,7 @@ __global__ void clear_hold_kernel(SgCtrl* ctrl, int n_clouds) {
 // Commit an accepted attempt: pos <- pos2, vel <- vel2 (bin/ode.cpp:488-489) and the
 // stage-7 Coulomb sum becomes the next stage-1 sum.
 __global__ void __launch_bounds__(SG_ROWS) dp_commit_kernel(DpArgs a) {
+    sg_griddep_wait();
     const SgRowBlock rb = a.rows[blockIdx.x];
     if (!a.ctrl[rb.cloud].accepted) return;
     const int li = threadIdx.x;
@@ -535,6 +542,7 @@ __global__ void __launch_bounds__(SG_ROWS) dp_commit_kernel(DpArgs a) {
 // Coulomb inputs of the state y (set-up and stand-alone calls); ghosts get q = 0.
 __global__ void __launch_bounds__(SG_ROWS) coords_from_state_kernel(DpArgs a,
                                                                     const double* __restrict__ q) {
+    sg_griddep_wait();
     const SgRowBlock rb = a.rows[blockIdx.x];
     const SgCloud& cl = a.clouds[rb.cloud];
     const int li = threadIdx.x;
@@ -578,6 +586,7 @@ __global__ void __launch_bounds__(SG_ROWS) force_finish_kernel(DpArgs a, double 
                                                                int with_field,
                                                                const int* __restrict__ perm,
                                                                double* __restrict__ out) {
+    sg_griddep_wait();
     const SgRowBlock rb = a.rows[blockIdx.x];
     const SgCloud& cl = a.clouds[rb.cloud];
     const int li = threadIdx.x;
@@ -605,6 +614,7 @@ __global__ void __launch_bounds__(SG_ROWS) force_finish_kernel(DpArgs a, double 
 // y[c][k] = pos[perm[k]][c]: the caller's order into the device (sorted) order.
 __global__ void aos_to_soa_kernel(const double* __restrict__ pos, const double* __restrict__ vel,
                                   const int* __restrict__ perm, double* __restrict__ y, int n) {
+    sg_griddep_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const size_t N = (size_t)n;
@@ -618,6 +628,7 @@ __global__ void aos_to_soa_kernel(const double* __restrict__ pos, const double* 
 // pos[perm[k]][c] = y[c][k]: back to the caller's order.
 __global__ void soa_to_aos_kernel(const double* __restrict__ y, const int* __restrict__ perm,
                                   double* __restrict__ pos, double* __restrict__ vel, int n) {
+    sg_griddep_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const size_t N = (size_t)n;
@@ -630,6 +641,7 @@ __global__ void soa_to_aos_kernel(const double* __restrict__ y, const int* __res
 
 __global__ void gather_kernel(const double* __restrict__ src, const int* __restrict__ perm,
                               double* __restrict__ dst, int n) {
+    sg_griddep_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) dst[i] = src[perm ? perm[i] : i];
 }
@@ -637,6 +649,7 @@ __global__ void gather_kernel(const double* __restrict__ src, const int* __restr
 // Per-row-block moment partials: sum x, x^2 per axis, v^2 per axis, m(vx^2+vy^2), m vz^2.
 __global__ void __launch_bounds__(SG_ROWS) moments_kernel(DpArgs a, const double* __restrict__ mass,
                                                           double* __restrict__ out) {
+    sg_griddep_wait();
     __shared__ double red[11][SG_ROWS / 32];
     const SgRowBlock rb = a.rows[blockIdx.x];
     const int li = threadIdx.x;
@@ -674,13 +687,13 @@ __global__ void __launch_bounds__(SG_ROWS) moments_kernel(DpArgs a, const double
 cudaError_t sg_dp_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t st) {
     if (n_rows <= 0) return cudaSuccess;
     switch (stage) {
-        case 1: dp_stage_kernel<1><<<n_rows, SG_ROWS, 0, st>>>(a); break;
-        case 2: dp_stage_kernel<2><<<n_rows, SG_ROWS, 0, st>>>(a); break;
-        case 3: dp_stage_kernel<3><<<n_rows, SG_ROWS, 0, st>>>(a); break;
-        case 4: dp_stage_kernel<4><<<n_rows, SG_ROWS, 0, st>>>(a); break;
-        case 5: dp_stage_kernel<5><<<n_rows, SG_ROWS, 0, st>>>(a); break;
-        case 6: dp_stage_kernel<6><<<n_rows, SG_ROWS, 0, st>>>(a); break;
-        case 7: dp_stage_kernel<7><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        case 1: sg_launch(dp_stage_kernel<1>, n_rows, SG_ROWS, 0, st, a); break;
+        case 2: sg_launch(dp_stage_kernel<2>, n_rows, SG_ROWS, 0, st, a); break;
+        case 3: sg_launch(dp_stage_kernel<3>, n_rows, SG_ROWS, 0, st, a); break;
+        case 4: sg_launch(dp_stage_kernel<4>, n_rows, SG_ROWS, 0, st, a); break;
+        case 5: sg_launch(dp_stage_kernel<5>, n_rows, SG_ROWS, 0, st, a); break;
+        case 6: sg_launch(dp_stage_kernel<6>, n_rows, SG_ROWS, 0, st, a); break;
+        case 7: sg_launch(dp_stage_kernel<7>, n_rows, SG_ROWS, 0, st, a); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -689,12 +702,12 @@ cudaError_t sg_dp_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t s
 cudaError_t sg_ck_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t st) {
     if (n_rows <= 0) return cudaSuccess;
     switch (stage) {
-        case 1: ck_stage_kernel<1><<<n_rows, SG_ROWS, 0, st>>>(a); break;
-        case 2: ck_stage_kernel<2><<<n_rows, SG_ROWS, 0, st>>>(a); break;
-        case 3: ck_stage_kernel<3><<<n_rows, SG_ROWS, 0, st>>>(a); break;
-        case 4: ck_stage_kernel<4><<<n_rows, SG_ROWS, 0, st>>>(a); break;
-        case 5: ck_stage_kernel<5><<<n_rows, SG_ROWS, 0, st>>>(a); break;
-        case 6: ck_stage_kernel<6><<<n_rows, SG_ROWS, 0, st>>>(a); break;
+        case 1: sg_launch(ck_stage_kernel<1>, n_rows, SG_ROWS, 0, st, a); break;
+        case 2: sg_launch(ck_stage_kernel<2>, n_rows, SG_ROWS, 0, st, a); break;
+        case 3: sg_launch(ck_stage_kernel<3>, n_rows, SG_ROWS, 0, st, a); break;
+        case 4: sg_launch(ck_stage_kernel<4>, n_rows, SG_ROWS, 0, st, a); break;
+        case 5: sg_launch(ck_stage_kernel<5>, n_rows, SG_ROWS, 0, st, a); break;
+        case 6: sg_launch(ck_stage_kernel<6>, n_rows, SG_ROWS, 0, st, a); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -703,70 +716,70 @@ cudaError_t sg_ck_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t s
 cudaError_t sg_gear_stage(const SgDpArgs& a, int phase, int n_rows, cudaStream_t st) {
     if (n_rows <= 0) return cudaSuccess;
     if (phase == 0)
-        gear_kernel<0><<<n_rows, SG_ROWS, 0, st>>>(a);
+        sg_launch(gear_kernel<0>, n_rows, SG_ROWS, 0, st, a);
     else
-        gear_kernel<1><<<n_rows, SG_ROWS, 0, st>>>(a);
+        sg_launch(gear_kernel<1>, n_rows, SG_ROWS, 0, st, a);
     return cudaGetLastError();
 }
 
 cudaError_t sg_gear_init(const SgDpArgs& a, const int* perm, int n_rows, cudaStream_t st) {
     if (n_rows <= 0) return cudaSuccess;
-    gear_init_kernel<<<n_rows, SG_ROWS, 0, st>>>(a, perm);
+    sg_launch(gear_init_kernel, n_rows, SG_ROWS, 0, st, a, perm);
     return cudaGetLastError();
 }
 
 cudaError_t sg_dp_control(SgCloud* clouds, SgCtrl* ctrl, const double* err_part,
                           const double* y, int n_clouds, const int* hold_on_accept,
                           const SgOp* ops, cudaStream_t st) {
-    dp_control_kernel<<<(n_clouds + 127) / 128, 128, 0, st>>>(clouds, ctrl, err_part, y, n_clouds,
+    sg_launch(dp_control_kernel, (n_clouds + 127) / 128, 128, 0, st, clouds, ctrl, err_part, y, n_clouds,
                                                               hold_on_accept, ops);
     return cudaGetLastError();
 }
 
 cudaError_t sg_clear_hold(SgCtrl* ctrl, int n_clouds, cudaStream_t st) {
-    clear_hold_kernel<<<(n_clouds + 127) / 128, 128, 0, st>>>(ctrl, n_clouds);
+    sg_launch(clear_hold_kernel, (n_clouds + 127) / 128, 128, 0, st, ctrl, n_clouds);
     return cudaGetLastError();
 }
 
 cudaError_t sg_dp_commit(const SgDpArgs& a, int n_rows, cudaStream_t st) {
-    dp_commit_kernel<<<n_rows, SG_ROWS, 0, st>>>(a);
+    sg_launch(dp_commit_kernel, n_rows, SG_ROWS, 0, st, a);
     return cudaGetLastError();
 }
 
 cudaError_t sg_coords_from_state(const SgDpArgs& a, const double* q, int n_rows, cudaStream_t st) {
-    coords_from_state_kernel<<<n_rows, SG_ROWS, 0, st>>>(a, q);
+    sg_launch(coords_from_state_kernel, n_rows, SG_ROWS, 0, st, a, q);
     return cudaGetLastError();
 }
 
 cudaError_t sg_force_finish(const SgDpArgs& a, double t, int with_field, const int* perm,
                             double* out, int n_rows, cudaStream_t st) {
-    force_finish_kernel<<<n_rows, SG_ROWS, 0, st>>>(a, t, with_field, perm, out);
+    sg_launch(force_finish_kernel, n_rows, SG_ROWS, 0, st, a, t, with_field, perm, out);
     return cudaGetLastError();
 }
 
 cudaError_t sg_aos_to_soa(const double* pos, const double* vel, const int* perm, double* y, int n,
                           cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    aos_to_soa_kernel<<<(n + 255) / 256, 256, 0, st>>>(pos, vel, perm, y, n);
+    sg_launch(aos_to_soa_kernel, (n + 255) / 256, 256, 0, st, pos, vel, perm, y, n);
     return cudaGetLastError();
 }
 
 cudaError_t sg_soa_to_aos(const double* y, const int* perm, double* pos, double* vel, int n,
                           cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    soa_to_aos_kernel<<<(n + 255) / 256, 256, 0, st>>>(y, perm, pos, vel, n);
+    sg_launch(soa_to_aos_kernel, (n + 255) / 256, 256, 0, st, y, perm, pos, vel, n);
     return cudaGetLastError();
 }
 
 cudaError_t sg_gather(const double* src, const int* perm, double* dst, int n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    gather_kernel<<<(n + 255) / 256, 256, 0, st>>>(src, perm, dst, n);
+    sg_launch(gather_kernel, (n + 255) / 256, 256, 0, st, src, perm, dst, n);
     return cudaGetLastError();
 }
 
 cudaError_t sg_moments(const SgDpArgs& a, const double* mass, double* out, int n_rows,
                        cudaStream_t st) {
-    moments_kernel<<<n_rows, SG_ROWS, 0, st>>>(a, mass, out);
+    sg_launch(moments_kernel, n_rows, SG_ROWS, 0, st, a, mass, out);
     return cudaGetLastError();
 }
 

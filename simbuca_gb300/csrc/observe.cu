@@ -18,6 +18,7 @@ __device__ __forceinline__ double* record_of(const SgRecArgs& r, const SgCloud& 
 // The kept ions: device position i holds caller index perm[i]; every stride-th caller
 // index of the cloud goes to slot (index - first) / stride.
 __global__ void __launch_bounds__(SG_ROWS) record_ions_kernel(SgRecArgs r) {
+    sg_griddep_wait();
     const SgRowBlock rb = r.rows[blockIdx.x];
     const SgCtrl& cs = r.ctrl[rb.cloud];
     if (!cs.print_due) return;
@@ -40,6 +41,7 @@ __global__ void __launch_bounds__(SG_ROWS) record_ions_kernel(SgRecArgs r) {
 __global__ void __launch_bounds__(SG_ROWS) dissociate_kernel(SgRecArgs r, double* __restrict__ mass,
                                                              int* __restrict__ spec0,
                                                              double* __restrict__ mass0) {
+    sg_griddep_wait();
     const SgRowBlock rb = r.rows[blockIdx.x];
     const SgCtrl& cs = r.ctrl[rb.cloud];
     if (!cs.dis_due) return;
@@ -78,6 +80,7 @@ __device__ void block_sum(double (&v)[K], double* red) {
 // then spread about it).  As in the reference, both divide by the cloud's ion count and
 // the energy sums m (vx^2 + vy^2 + vz vy) / 2.
 __global__ void __launch_bounds__(256) record_stats_kernel(SgRecArgs r) {
+    sg_griddep_wait();
     __shared__ double red[8 * 5 * SG_MAX_SPECIES];
     __shared__ double cen[3 * SG_MAX_SPECIES];
     const SgCtrl& cs = r.ctrl[blockIdx.x];
@@ -150,6 +153,7 @@ __global__ void __launch_bounds__(256) record_stats_kernel(SgRecArgs r) {
 // A record of every cloud now (the reference's print after an operation): takes the
 // next ring slot, or holds the cloud when its ring is full.
 __global__ void record_now_kernel(SgCtrl* ctrl, int n_clouds) {
+    sg_griddep_wait();
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n_clouds) return;
     SgCtrl& cs = ctrl[c];
@@ -166,6 +170,7 @@ __global__ void record_now_kernel(SgCtrl* ctrl, int n_clouds) {
 
 __global__ void gather_int_kernel(const int* __restrict__ src, const int* __restrict__ perm,
                                   int* __restrict__ dst, int n) {
+    sg_griddep_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) dst[i] = src[perm[i]];
 }
@@ -174,23 +179,23 @@ __global__ void gather_int_kernel(const int* __restrict__ src, const int* __rest
 
 cudaError_t sg_gather_int(const int* src, const int* perm, int* dst, int n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    gather_int_kernel<<<(n + 255) / 256, 256, 0, st>>>(src, perm, dst, n);
+    sg_launch(gather_int_kernel, (n + 255) / 256, 256, 0, st, src, perm, dst, n);
     return cudaGetLastError();
 }
 
 cudaError_t sg_record(const SgRecArgs& r, int n_rows, int n_clouds, cudaStream_t st) {
-    if (n_rows > 0) record_ions_kernel<<<n_rows, SG_ROWS, 0, st>>>(r);
-    if (n_clouds > 0) record_stats_kernel<<<n_clouds, 256, 0, st>>>(r);
+    if (n_rows > 0) sg_launch(record_ions_kernel, n_rows, SG_ROWS, 0, st, r);
+    if (n_clouds > 0) sg_launch(record_stats_kernel, n_clouds, 256, 0, st, r);
     return cudaGetLastError();
 }
 
 cudaError_t sg_dissociate(const SgRecArgs& r, double* mass, int* spec0, double* mass0, int n_rows,
                           cudaStream_t st) {
-    if (n_rows > 0) dissociate_kernel<<<n_rows, SG_ROWS, 0, st>>>(r, mass, spec0, mass0);
+    if (n_rows > 0) sg_launch(dissociate_kernel, n_rows, SG_ROWS, 0, st, r, mass, spec0, mass0);
     return cudaGetLastError();
 }
 
 cudaError_t sg_record_now(SgCtrl* ctrl, int n_clouds, cudaStream_t st) {
-    record_now_kernel<<<(n_clouds + 127) / 128, 128, 0, st>>>(ctrl, n_clouds);
+    sg_launch(record_now_kernel, (n_clouds + 127) / 128, 128, 0, st, ctrl, n_clouds);
     return cudaGetLastError();
 }

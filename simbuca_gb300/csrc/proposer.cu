@@ -105,6 +105,7 @@ __global__ void proposer_kernel(const SgCloud* __restrict__ clouds, SgCtrl* __re
                                 const __nv_bfloat16* __restrict__ w, float* __restrict__ log_feat,
                                 double* __restrict__ log_num, int log_cap, int use_mlp,
                                 double safety, int n_clouds) {
+    sg_griddep_wait();
     const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (c >= n_clouds) return;
@@ -169,6 +170,7 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_grad_kernel(
     const __nv_bfloat16* __restrict__ w, const float* __restrict__ X, const float* __restrict__ Y,
     const int* __restrict__ idx, int B, int per, float* __restrict__ gpart,
     float* __restrict__ lpart) {
+    sg_griddep_wait();
     __shared__ float g[SG_MLP_NP];
     __shared__ float lsum[kTrainThreads / 32];
     for (int k = threadIdx.x; k < SG_MLP_NP; k += blockDim.x) g[k] = 0.f;
@@ -236,6 +238,7 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_grad_kernel(
 // grad[k] = sum_b gpart[b][k] (fixed order); loss = sum_b lpart[b] / B.
 __global__ void mlp_reduce_kernel(const float* __restrict__ gpart, const float* __restrict__ lpart,
                                   int nb, int B, float* __restrict__ grad, float* __restrict__ loss) {
+    sg_griddep_wait();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < SG_MLP_NP) {
         float s = 0.f;
@@ -254,6 +257,7 @@ __global__ void mlp_adam_kernel(float* __restrict__ wm, __nv_bfloat16* __restric
                                 float* __restrict__ m1, float* __restrict__ m2,
                                 const float* __restrict__ grad, float lr, float b1, float b2,
                                 float eps, int step) {
+    sg_griddep_wait();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= SG_MLP_NP) return;
     const float g = grad[k];
@@ -269,6 +273,7 @@ __global__ void mlp_adam_kernel(float* __restrict__ wm, __nv_bfloat16* __restric
 }
 
 __global__ void mlp_to_bf16_kernel(const float* __restrict__ wm, __nv_bfloat16* __restrict__ wb) {
+    sg_griddep_wait();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < SG_MLP_NP) wb[k] = __float2bfloat16_rn(wm[k]);
 }
@@ -276,6 +281,7 @@ __global__ void mlp_to_bf16_kernel(const float* __restrict__ wm, __nv_bfloat16* 
 // Inference of a batch: one warp per sample.
 __global__ void mlp_forward_kernel(const __nv_bfloat16* __restrict__ w, const float* __restrict__ X,
                                    int n, float* __restrict__ out) {
+    sg_griddep_wait();
     const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (s >= n) return;
     float x[SG_MLP_IN];
@@ -292,7 +298,7 @@ cudaError_t sg_proposer_launch(const SgCloud* clouds, SgCtrl* ctrl, const double
                                double* log_num, int log_cap, int use_mlp, double safety,
                                int n_clouds, cudaStream_t st) {
     const int warps = 4;
-    proposer_kernel<<<(n_clouds + warps - 1) / warps, 32 * warps, 0, st>>>(
+    sg_launch(proposer_kernel, (n_clouds + warps - 1) / warps, 32 * warps, 0, st, 
         clouds, ctrl, mom, pst, static_cast<const __nv_bfloat16*>(wbf), log_feat, log_num, log_cap,
         use_mlp, safety, n_clouds);
     return cudaGetLastError();
@@ -302,27 +308,27 @@ cudaError_t sg_mlp_grad_launch(const void* wbf, const float* X, const float* Y, 
                                int B, float* gpart, float* lpart, int nb, float* grad, float* loss,
                                cudaStream_t st) {
     const int per = (B + nb - 1) / nb;
-    mlp_grad_kernel<<<nb, kTrainThreads, 0, st>>>(static_cast<const __nv_bfloat16*>(wbf), X, Y, idx,
+    sg_launch(mlp_grad_kernel, nb, kTrainThreads, 0, st, static_cast<const __nv_bfloat16*>(wbf), X, Y, idx,
                                                   B, per, gpart, lpart);
-    mlp_reduce_kernel<<<(SG_MLP_NP + 255) / 256, 256, 0, st>>>(gpart, lpart, nb, B, grad, loss);
+    sg_launch(mlp_reduce_kernel, (SG_MLP_NP + 255) / 256, 256, 0, st, gpart, lpart, nb, B, grad, loss);
     return cudaGetLastError();
 }
 
 cudaError_t sg_mlp_adam_launch(float* wm, void* wbf, float* m1, float* m2, const float* grad,
                                float lr, int step, cudaStream_t st) {
-    mlp_adam_kernel<<<(SG_MLP_NP + 255) / 256, 256, 0, st>>>(
+    sg_launch(mlp_adam_kernel, (SG_MLP_NP + 255) / 256, 256, 0, st, 
         wm, static_cast<__nv_bfloat16*>(wbf), m1, m2, grad, lr, 0.9f, 0.999f, 1e-8f, step);
     return cudaGetLastError();
 }
 
 cudaError_t sg_mlp_to_bf16_launch(const float* wm, void* wbf, cudaStream_t st) {
-    mlp_to_bf16_kernel<<<(SG_MLP_NP + 255) / 256, 256, 0, st>>>(wm, static_cast<__nv_bfloat16*>(wbf));
+    sg_launch(mlp_to_bf16_kernel, (SG_MLP_NP + 255) / 256, 256, 0, st, wm, static_cast<__nv_bfloat16*>(wbf));
     return cudaGetLastError();
 }
 
 cudaError_t sg_mlp_forward_launch(const void* wbf, const float* X, int n, float* out,
                                   cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    mlp_forward_kernel<<<(n + 3) / 4, 128, 0, st>>>(static_cast<const __nv_bfloat16*>(wbf), X, n, out);
+    sg_launch(mlp_forward_kernel, (n + 3) / 4, 128, 0, st, static_cast<const __nv_bfloat16*>(wbf), X, n, out);
     return cudaGetLastError();
 }

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #include "../../include/simgb.h"
 
 // ---- constants of the reference (bin/globals.h:4-16) -------------------------
@@ -11,6 +13,35 @@
 #define SG_EL_CHARGE 1.60217733e-19
 #define SG_KE 8.987551787E9
 #define SG_KB 1.3806504E-23
+
+// ---- programmatic dependent launch -----------------------------------------------
+// Kernels of the graph-captured attempt are launched with programmatic stream
+// serialization: the next kernel's grid is set up while the previous one drains, and
+// every kernel waits (griddepcontrol.wait) for its predecessor's completion and memory
+// before its first global access -- a no-op when it was launched without the attribute.
+// g_sg_pdl (capi.cu) is set only while the untimed attempt graph is captured, whose only
+// non-kernel node (the fix-up list reset) is followed by a plain launch.
+extern int g_sg_pdl;
+
+__device__ __forceinline__ void sg_griddep_wait() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t sg_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                             cudaStream_t st, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = g_sg_pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // ---- launch geometry ---------------------------------------------------------
 // FP32c Coulomb: 128 threads x 4 ions per thread = 512 i-ions per block; j-tiles of
