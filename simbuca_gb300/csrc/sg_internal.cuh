@@ -25,6 +25,9 @@ extern int g_sg_pdl;
 
 __device__ __forceinline__ void sg_griddep_wait() {
     asm volatile("griddepcontrol.wait;" ::: "memory");
+    // the next kernel may be scheduled once every block of this one has started; its
+    // blocks then wait above for this grid's completion
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 template <typename... KArgs, typename... Args>
