@@ -202,7 +202,7 @@ __device__ __forceinline__ void close_pairs_warp(const float (*tl)[TL], int len,
 // Main loop over one shared-memory j-tile for the IPT ions of a thread: packed FP32x2
 // over consecutive j pairs.  DIAG: the tile contains the thread's own ions, whose self
 // pair must not raise the close-pair flag.
-template <int IPT, bool DIAG, bool NOQ = false>
+template <int IPT, bool DIAG, bool NOQ = false, int NU = 2>
 __device__ __forceinline__ void tile_pairs(const float* tx, const float* ty, const float* tz,
                                            const float* tq, const float* txl, const float* tyl,
                                            const float* tzl, int jb, int je, int j0,
@@ -210,7 +210,7 @@ __device__ __forceinline__ void tile_pairs(const float* tx, const float* ty, con
                                            const f2* xh, const f2* yh, const f2* zh,
                                            const f2* xl, const f2* yl, const f2* zl, f2 tiny2,
                                            float wc, f2* ax, f2* ay, f2* az, float* y3max) {
-#pragma unroll 2
+#pragma unroll NU
     for (int jj = jb; jj < je; jj += 2) {
         const f2 Xj = *reinterpret_cast<const f2*>(tx + jj);
         const f2 Yj = *reinterpret_cast<const f2*>(ty + jj);
@@ -396,6 +396,8 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
     }
 
     const f2 tiny2 = pk(kTiny, kTiny);
+    // one ion per thread (the small-cloud shapes): four j pairs in flight per thread
+    constexpr int kNU = IPT == 1 ? 4 : 2;
     // Small clouds fold partial sums every 16 j-ions so that the squared partial sums
     // still estimate sum_j |f_ij|^2 when the whole cloud is one or two tiles.
     const int flush_len = (cl.npad <= 2048) ? 16 : SG_TILE;
@@ -438,13 +440,13 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
 #pragma unroll
             for (int k = 0; k < IPT; k++) ax[k] = ay[k] = az[k] = 0ull;
             if (!diag && noq)
-                tile_pairs<IPT, false, true>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh,
+                tile_pairs<IPT, false, true, kNU>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh,
                                              yh, zh, xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
             else if (!diag)
-                tile_pairs<IPT, false>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh, zh,
+                tile_pairs<IPT, false, false, kNU>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh, zh,
                                        xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
             else
-                tile_pairs<IPT, true>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh, zh,
+                tile_pairs<IPT, true, false, kNU>(tx, ty, tz, tq, txl, tyl, tzl, jb, je, j0, ipad, xh, yh, zh,
                                       xl, yl, zl, tiny2, wc, ax, ay, az, y3max);
             // fold the partial sums into the compensated accumulators
 #pragma unroll
