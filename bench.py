@@ -427,6 +427,7 @@ def run_ours(args, dist: Dist):
             cx = Context(dist.local)
             bb = Batch(cx, w.counts, w.fields, odes, pr)
             bb.upload(snap_pos, snap_vel, allc.mass, allc.charge)
+            bb.step()  # untimed: captures and instantiates the attempt graph
             i0 = bb.info()
             cx.timer_start()
             for _ in range(n64):
