@@ -19,8 +19,9 @@
 // serialization: the next kernel's grid is set up while the previous one drains, and
 // every kernel waits (griddepcontrol.wait) for its predecessor's completion and memory
 // before its first global access -- a no-op when it was launched without the attribute.
-// g_sg_pdl (capi.cu) is set only while the untimed attempt graph is captured, whose only
-// non-kernel node (the fix-up list reset) is followed by a plain launch.
+// g_sg_pdl (capi.cu) is set only while the untimed attempt graph is captured (opt-in,
+// SIMGB_PDL=1), whose only non-kernel node (the fix-up list reset) is followed by a
+// plain launch.
 extern int g_sg_pdl;
 
 __device__ __forceinline__ void sg_griddep_wait() {
