@@ -353,3 +353,40 @@ def test_kernel_timing_counts(ctx, method, coul, stages):
     assert kt["interactions"] == pytest.approx(5 * coul * 600 * 599)
     assert st["stage_launches"] == 5 * stages and st["stage_ms"] > 0
     assert b.info()[0]["status"] == 0
+
+
+@pytest.mark.parametrize("variant", [9, 14])
+@pytest.mark.parametrize("method", [4, 1])
+def test_integrators_in_kd_order(ctx, variant, method):
+    """Cash-Karp and Gear with the ions in k-d order (the launch shapes large clouds take;
+    the far tiles' conditioning estimate comes from the first Coulomb sum of each
+    attempt): the end state matches the oracle -- Cash-Karp replaying the accepted
+    schedule, Gear over the same fixed steps."""
+    w = configs.penning_1k(n=3000, seed=41)
+    c = w.clouds[0]
+    fp = configs.penning_field(quad=(0.5, configs.nu_c(configs.M_CS), 0.0, 0.0, 1.0), delta=1e3)
+    ctx.set_coulomb_variant(variant)
+    try:
+        if method == 4:
+            b = one_cloud(ctx, c.pos, c.vel, c.mass, c.charge, fp, 1e-9, 1e-15, 1e-9, 0.15e-6,
+                          SG_PREC_FP32C, method=4)
+            ts, hs, last = run_recording(b)
+            assert last[0]["status"] == 0 and last[0]["done"] == 1
+        else:
+            b = one_cloud(ctx, c.pos, c.vel, c.mass, c.charge, fp, 1e-9, 1e-15, 2e-9, 1.0,
+                          SG_PREC_FP32C, adaptive=False, method=1)
+            info, _ = b.run(max_attempts=60)
+            assert info[0]["steps"] == 60 and info[0]["status"] == 0
+        p, v = b.download()
+    finally:
+        ctx.set_coulomb_variant(-1)
+    if method == 4:
+        ep, ev = replay_error(c, fp, ts[0], hs[0], p, v, method=4)
+        assert ep <= 1e-9 and ev <= 1e-9, (ep, ev)
+    else:
+        pr, vr, _, _, _ = oracle.dp45_run(c.pos, c.vel, c.mass, c.charge, fp, rtol=1e-9,
+                                          atol=1e-15, h0=2e-9, t0=0.0, t_end=1.0,
+                                          adaptive=False, max_steps=60, method=1)
+        ep = np.abs(p - pr).max() / np.abs(pr).max()
+        ev = np.abs(v - vr).max() / np.abs(vr).max()
+        assert ep <= 1e-7 and ev <= 1e-7, (ep, ev)
