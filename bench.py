@@ -12,8 +12,11 @@ Metric: simulated microseconds per wall second (higher is better).
 Our arm (FP32-compensated Coulomb, device-resident state, CUDA-graph attempts):
 value = device-timed rate with the state resident in HBM; e2e = the same through the
 public C ABI with the state uploaded from pinned host memory and read back every
-step.  The plain FP64 GPU form is timed on the same cloud for comparison.  Rank 0
-also times the CPU oracle on a bounded row sample (cpu_baseline).
+step.  Kernel times (roofline: the Coulomb kernel; stage_roofline: the O(N) kernels)
+come from a second pass of as many steps with CUDA events around those launches.  The
+plain FP64 GPU form is timed on the same cloud for comparison.  Rank 0 also times the
+CPU oracle on a bounded row sample (cpu_baseline).  Step control is the reference's
+I-controller; --proposer on runs the learned step-size proposer instead.
 
 Reference arm (--impl reference): the CPU oracle (the reference's FP64 direct sum and
 Dormand-Prince loop restated in C, oracle/) on all host cores, full attempts of the
