@@ -284,16 +284,18 @@ void plan(Problem& P, int n_sm) {
         S[c] = std::max(1, (int)std::ceil(cl.npad / jmax));
         items += (long long)((cl.n + ib - 1) / ib) * S[c];
     }
-    // j-chunks are whole 128-ion tiles, or 64-ion ones (plain shapes only: the k-d
+    // j-chunks are whole 128-ion tiles, or smaller ones (plain shapes only: the k-d
     // ordered kernels test whole tiles) when 128-ion chunks would leave fewer than two
-    // blocks per SM -- a 1,000-ion cloud then runs 512 one-warp blocks instead of 256
-    // (measured: 64-ion chunks 7 % faster per step than 32-ion ones, whose 32 partial-sum
-    // slots made the reduction dearer than the extra parallelism paid)
+    // blocks per SM.  FP32c: 64-ion chunks -- a 1,000-ion cloud runs 512 one-warp blocks
+    // instead of 256 (7 % faster per step than 32-ion chunks, whose 32 partial-sum slots
+    // made the reduction dearer than the extra parallelism paid).  FP64: 32-ion chunks,
+    // its pair kernel being bound by the FP64 pipe of every SM it can reach (1,000 ions:
+    // 23 sim-us/s with 32-ion chunks, 14.5 with 64).
     long long full_split = 0;
     for (int c = 0; c < C; c++)
         if (S[c] > 0)
             full_split += (long long)((P.hc[c].n + ib - 1) / ib) * std::max(1, P.hc[c].npad / 128);
-    const int jgran = (!P.sorted && full_split < 2LL * n_sm) ? 64 : 128;
+    const int jgran = (!P.sorted && full_split < 2LL * n_sm) ? (f32 ? 64 : 32) : 128;
     const double target = conc * 4.0;
     if (items > 0 && items < target) {
         const int f = (int)std::ceil(target / (double)items);
