@@ -3,8 +3,9 @@ CPU path itself, compiled from its own sources (oracle/Makefile `make ref`).
 
     python tests/golden/make_golden.py
 
-Needs the reference checkout (the `ref` make target reads its sources); the
-committed .npz files are what the tests use everywhere else.  Inputs are seeded
+Needs the reference checkout, its root directory named by the environment variable
+SIMBUCA_REF_DIR (the `ref` make targets read its sources); the committed .npz files
+are what the tests use everywhere else.  Inputs are seeded
 synthetic clouds (numpy Philox), stored next to the outputs.
 """
 from __future__ import annotations
@@ -24,7 +25,7 @@ import oracle  # noqa: E402
 from simbuca_gb300 import configs  # noqa: E402
 
 AMU = oracle.AMU
-REF_BIN = "/root/reference/bin"  # the reference checkout (read only)
+REF_BIN = os.path.join(os.environ.get("SIMBUCA_REF_DIR", ""), "bin")  # read only
 # Paul trap of the reference (_trap_param defaults, bin/trapparameters.cpp:2-10) with a
 # TOF kick: Vrf, Vdc, kappa, r0, z0, freq_rf, E_kick
 TRAPP = np.array([50.0, 5.0, 0.001, 0.04, 0.04, 50e5, 100.0])
@@ -45,7 +46,7 @@ def init_library():
     initialization.cpp reads ../libraries/ mass tables when loaded, so it is loaded
     from the reference's bin/ directory."""
     odir = os.path.join(ROOT, "oracle")
-    subprocess.run(["make", "-C", odir, "-s", "ref-init"], check=True)
+    subprocess.run(["make", "-C", odir, "-s", "ref-init", f"REF_SRC={REF_BIN}"], check=True)
     cwd = os.getcwd()
     os.chdir(REF_BIN)
     try:
