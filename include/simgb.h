@@ -110,6 +110,10 @@ typedef struct sg_ode_params {
                             adaptive ignored, history restarted by upload and set_state.
                             All clouds of a batch use one method.                      */
     int32_t pad;
+    double beta;         /* PI term of error_succes (bin/ode.cpp:431-439): on an accepted
+                            step scale = 0.9 err^-(0.2 - 0.75 beta) errold^beta; the
+                            reference's build has beta = 0 (the I-controller) and names
+                            0.04-0.08 for PI control.  0 reproduces the reference.       */
 } sg_ode_params;
 
 /* State of one cloud after a call. */
@@ -161,9 +165,11 @@ int sg_force(sg_ctx* ctx, int precision, int n, const double* pos, const double*
  * buffers owned by the caller; the result is the FP64 form of sg_coulomb_accel.  Work
  * is queued on `stream` (a cudaStream_t, NULL = legacy default stream) of the current
  * device and the call returns without waiting.  Scratch lives in a fixed 1.8 MB device
- * array of the library: n <= 8192, else SG_TOO_LARGE.  The first call on a device looks
- * up that array's device address (make it before capturing any stream).  Calls share
- * the array: calls that overlap on the GPU race. */
+ * array of the library: n <= 8192, else SG_TOO_LARGE.  The array has one address per
+ * CUDA context: the first call made in a context looks it up and keeps it under that
+ * context's unique id (make that first call before capturing any stream).  n = 0
+ * returns SG_OK and queues nothing; a null pointer gives SG_BAD_ARG.  Calls share the
+ * array: calls that overlap on the GPU race. */
 int sg_coulomb_accel_noalloc(int n, const double* pos, const double* q, const double* kq,
                              double* acc, void* stream);
 
@@ -249,6 +255,16 @@ int sg_mlp_train(sg_ctx* ctx, int n, const float* X, const float* Y, int iters, 
 /* Use the MLP (w != NULL) with step-size safety factor `safety` in (0, 1] for the
  * clouds of the batch, or the reference's controller (w == NULL). */
 int sg_batch_set_proposer(sg_ctx* ctx, const float* w, double safety);
+/* Test of the bounded device waits (no counterpart in the reference).  With tile >= 0,
+ * every block of the FP32c Coulomb kernels of the current batch, once its j-tile
+ * `tile` has arrived, also waits on a barrier that nothing arrives at until limit_us
+ * microseconds (1 .. 1e6) have passed, and then takes its timeout path: it raises
+ * SG_TIMEOUT, waits (bounded) for the copies it has issued, and returns without writing
+ * sums.  The attempt is then neither accepted nor used for step control: every cloud
+ * stops with status SG_TIMEOUT and the call returns it.  tile < 0 turns the test off;
+ * sg_batch_upload clears the error word.  No copy is left in flight and no device
+ * state is lost: the context stays usable. */
+int sg_set_wait_test(sg_ctx* ctx, int tile, int limit_us);
 /* The reference's controller with the safety factor of its accepted-step rule
  * (0.9, bin/ode.cpp:431,439) replaced by `safety` in (0, 1]: the ablation that separates
  * the proposer's learning from a plain change of safety.  Replaces the proposer; the

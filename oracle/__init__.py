@@ -48,7 +48,8 @@ class OrcCtrl(ctypes.Structure):
                 ("reject", ctypes.c_int32), ("adaptive", ctypes.c_int32),
                 ("max_rejects", ctypes.c_int32), ("status", ctypes.c_int32),
                 ("steps", ctypes.c_int64), ("rejects", ctypes.c_int64),
-                ("force_evals", ctypes.c_int64), ("attempts", ctypes.c_int64)]
+                ("force_evals", ctypes.c_int64), ("attempts", ctypes.c_int64),
+                ("beta", ctypes.c_double)]
 
 
 def _d(a):
@@ -138,7 +139,7 @@ def field(pos, vel, mass, charge, t, fp):
 
 
 def dp45_run(pos, vel, mass, charge, fp, *, rtol, atol, h0, t0, t_end, adaptive=True,
-             max_steps=1 << 62, hist_cap=0, max_rejects=0, method=5):
+             max_steps=1 << 62, hist_cap=0, max_rejects=0, method=5, beta=0.0):
     """Run the restated step loop (method 5 Dormand-Prince, 4 Cash-Karp); returns
     (pos, vel, ctrl, hist[attempts, 4], n_attempts)."""
     pos = np.array(pos, np.float64, order="C")
@@ -148,6 +149,7 @@ def dp45_run(pos, vel, mass, charge, fp, *, rtol, atol, h0, t0, t_end, adaptive=
     c = OrcCtrl()
     c.rtol, c.atol, c.h, c.hnext, c.errold = rtol, atol, h0, h0, 1e-4
     c.t, c.t_end, c.adaptive, c.max_rejects = t0, t_end, int(adaptive), int(max_rejects)
+    c.beta = float(beta)
     hist = np.zeros((max(hist_cap, 1), 4))
     nh = lib().orc_rk_run(int(method), len(mass), _d(pos), _d(vel), _d(mass), _i(charge),
                           ctypes.byref(fp), ctypes.byref(c), int(max_steps), _d(hist),

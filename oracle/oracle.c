@@ -553,10 +553,12 @@ void orc_gear_step(int n, const double* pos, const double* vel, const double* ma
 }
 #undef GS
 
-/* error_succes, bin/ode.cpp:426-457 (beta = 0, alpha = 0.2, safe = 0.9,
- * minscale = 0.2, maxscale = 10). */
+/* error_succes, bin/ode.cpp:426-457 (alpha = 0.2 - 0.75 beta, safe = 0.9,
+ * minscale = 0.2, maxscale = 10).  The reference compiles beta = 0 (the I-controller,
+ * :431) and recommends 0.04-0.08 for PI control (:428, :433); beta comes from the
+ * controller state here. */
 int orc_error_succes(double err, orc_ctrl* c) {
-    const double beta = 0.0, alpha = 0.2 - beta * 0.75, safe = 0.9, minscale = 0.2,
+    const double beta = c->beta, alpha = 0.2 - beta * 0.75, safe = 0.9, minscale = 0.2,
                  maxscale = 10.0;
     double scale;
     if (err <= 1.0) {

@@ -46,6 +46,7 @@ typedef struct orc_ctrl {
     double t, t_end;
     int32_t reject, adaptive, max_rejects, status;
     int64_t steps, rejects, force_evals, attempts;
+    double beta; /* PI term of error_succes; the reference's build has 0 */
 } orc_ctrl;
 
 void orc_set_threads(int n);

@@ -55,7 +55,8 @@ class OdeParams(ctypes.Structure):
     _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double), ("h0", ctypes.c_double),
                 ("t0", ctypes.c_double), ("t_end", ctypes.c_double),
                 ("adaptive", ctypes.c_int32), ("max_rejects", ctypes.c_int32),
-                ("method", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("method", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("beta", ctypes.c_double)]
 
 
 class StepInfo(ctypes.Structure):
@@ -91,7 +92,7 @@ _vp = ctypes.c_void_p
 # every extern "C" symbol declared in include/simgb.h
 EXPORTED = [
     "sg_create", "sg_destroy", "sg_status_string", "sg_last_cuda_error", "sg_sync",
-    "sg_version", "sg_coulomb_accel", "sg_force", "sg_coulomb_accel_noalloc",
+    "sg_version", "sg_coulomb_accel", "sg_force", "sg_coulomb_accel_noalloc", "sg_set_wait_test",
     "sg_batch_create", "sg_batch_upload",
     "sg_batch_set_state", "sg_batch_download", "sg_batch_attempts", "sg_dp45_step",
     "sg_batch_run", "sg_batch_info", "sg_batch_set_field", "sg_batch_set_t_end",
@@ -131,6 +132,7 @@ def _declare(L):
     L.sg_force.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _ip,
                            ctypes.c_double, ctypes.POINTER(FieldParams), _dp]
     L.sg_coulomb_accel_noalloc.argtypes = [ctypes.c_int, _vp, _vp, _vp, _vp, _vp]
+    L.sg_set_wait_test.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
     L.sg_batch_create.argtypes = [_vp, ctypes.c_int, _ip, ctypes.POINTER(FieldParams),
                                   ctypes.POINTER(OdeParams), ctypes.c_int]
     L.sg_batch_upload.argtypes = [_vp, _dp, _dp, _dp, _ip]

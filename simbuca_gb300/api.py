@@ -148,6 +148,11 @@ class Context:
     def set_use_graph(self, on: bool):
         check(self._L.sg_set_use_graph(self._h, int(bool(on))), "sg_set_use_graph")
 
+    def set_wait_test(self, tile: int, limit_us: int = 1000):
+        """Make the FP32c Coulomb kernels of the current batch give up a bounded wait at
+        j-tile `tile` after limit_us (tile < 0: off); see sg_set_wait_test."""
+        check(self._L.sg_set_wait_test(self._h, int(tile), int(limit_us)), "sg_set_wait_test")
+
 
 class Batch:
     """Resident clouds advanced on the device by the Dormand-Prince loop.

@@ -140,11 +140,14 @@ def penning_field(coulomb=True, quad=None, dipole=None, delta=0.0) -> FieldParam
     return fp
 
 
-def ode(rtol, atol, h0, t_end, t0=0.0, adaptive=True, max_rejects=0, method=5) -> OdeParams:
-    """Controller settings; method 5 = Dormand-Prince, 4 = Cash-Karp, 1 = Gear."""
+def ode(rtol, atol, h0, t_end, t0=0.0, adaptive=True, max_rejects=0, method=5,
+        beta=0.0) -> OdeParams:
+    """Controller settings; method 5 = Dormand-Prince, 4 = Cash-Karp, 1 = Gear; beta
+    is the PI term of the step-size controller (0: the reference's I-controller)."""
     o = OdeParams()
     o.rtol, o.atol, o.h0, o.t0, o.t_end = rtol, atol, h0, t0, t_end
     o.adaptive, o.max_rejects, o.method = int(adaptive), int(max_rejects), int(method)
+    o.beta = float(beta)
     return o
 
 

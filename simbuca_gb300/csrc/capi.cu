@@ -430,8 +430,8 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(dalloc(&P.err_part, (size_t)std::max(P.n_rows, 1)));
     CK(dalloc(&P.mom, (size_t)std::max(P.n_rows, 1) * 11));
     CK(dalloc(&P.stage, 6 * N));
-    CK(dalloc(&P.flags, 4));
-    CK(cudaMemset(P.flags, 0, 4 * sizeof(int)));
+    CK(dalloc(&P.flags, SG_NFLAGS));
+    CK(cudaMemset(P.flags, 0, SG_NFLAGS * sizeof(int)));
     CK(dalloc(&P.pst, (size_t)std::max(P.n_clouds, 1)));
     CK(cudaMemset(P.pst, 0, sizeof(SgProposerState) * (size_t)std::max(P.n_clouds, 1)));
     CK(cudaMalloc(&P.wbf, SG_MLP_NP * 2));
@@ -730,7 +730,7 @@ int enqueue_attempt(sg_ctx* ctx, Problem& P) {
             STAGE_TIMED(sg_dp_stage(a, s, P.n_rows, ctx->stream));
         }
     }
-    STAGE_TIMED(sg_dp_control(P.dc, P.dctrl, P.err_part, P.y, P.n_clouds, P.flags + 1, P.dops,
+    STAGE_TIMED(sg_dp_control(P.dc, P.dctrl, P.err_part, P.y, P.n_clouds, P.flags, P.dops,
                               ctx->stream));
     STAGE_TIMED(sg_dp_commit(a, P.n_rows, ctx->stream));
     if (P.rec_cap > 0) CK(sg_record(rec_args(P), P.n_rows, P.n_clouds, ctx->stream));
@@ -938,6 +938,15 @@ int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel,
         CK(sg_gather(P.mass0, P.dperm, P.mass, P.n, ctx->stream));
         CK(sg_gather_int(P.spec0, P.dperm, P.spec, P.n, ctx->stream));
         CK(sg_gather(P.pmass0, P.dperm, P.pmass, P.n, ctx->stream));
+    }
+    for (int c = 0; c < P.n_clouds; c++) {
+        SgCloud& cl = P.hc[c];
+        cl.ion0 = cl.off;
+        for (int i = cl.off; i < cl.off + cl.n; i++)
+            if (P.perm[i] == cl.off) {
+                cl.ion0 = i;
+                break;
+            }
     }
     for (int c = 0; c < P.n_clouds; c++) {
         set_frame(P.hc[c], pos, P.hc[c].off);
@@ -1186,6 +1195,7 @@ int sg_batch_create(sg_ctx* ctx, int n_clouds, const int* counts, const sg_field
         s.atol = op[c].atol;
         s.adaptive = op[c].adaptive;
         s.max_rejects = op[c].max_rejects;
+        s.beta = op[c].beta;
         s.method = P.method;
         {
             // Init_ode's step powers (bin/ode.cpp:548-552); the reference is C++98, where
@@ -1975,6 +1985,18 @@ int sg_batch_set_proposer(sg_ctx* ctx, const float* w, double safety) {
         int st = proposer_reset(ctx, P);
         if (st != SG_OK) return st;
     }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
+int sg_set_wait_test(sg_ctx* ctx, int tile, int limit_us) {
+    if (!ctx || limit_us < 1 || limit_us > 1000000) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    const int w[2] = {tile >= 0 ? tile + 1 : 0, limit_us};
+    CK(cudaMemcpyAsync(P.flags + SG_FLAG_WAIT_TILE, w, sizeof w, cudaMemcpyHostToDevice,
+                       ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return SG_OK;
 }

@@ -56,14 +56,24 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait on an mbarrier phase: false once SG_WAIT_NS have passed.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait on an mbarrier phase: false once limit_ns have passed.
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
     if (mbar_try(bar, parity)) return true;
     const uint64_t t0 = globaltimer();
     for (;;) {
         if (mbar_try(bar, parity)) return true;
-        if (globaltimer() - t0 > SG_WAIT_NS) return false;
+        if (globaltimer() - t0 > limit_ns) return false;
     }
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    return mbar_wait_for(bar, parity, SG_WAIT_NS);
+}
+// The wait test (flags[SG_FLAG_WAIT_TILE] = t + 1): after tile t has arrived, the block
+// also waits on `never`, a barrier that nothing arrives at, until the test's limit runs
+// out; the kernel then takes its timeout path, whose drain finds every issued copy landed.
+__device__ __forceinline__ bool wait_test(uint64_t* never, const int* flags) {
+    const uint64_t limit = 1000ull * (uint64_t)max(flags[SG_FLAG_WAIT_US], 1);
+    return mbar_wait_for(never, 0, limit);
 }
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
                                          uint64_t* bar) {
@@ -330,9 +340,11 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
     constexpr int T = SG_TILE;
     __shared__ __align__(128) float tile[SG_STAGES][7][T];
     __shared__ __align__(8) uint64_t full[SG_STAGES];
+    __shared__ __align__(8) uint64_t never;  // the wait test's barrier
     __shared__ double corr[3][NT * IPT];
 
     const SgWorkItem it = items[blockIdx.x];
+    const int wtest = errword ? errword[SG_FLAG_WAIT_TILE] : 0;
     if (ctrl != nullptr && (ctrl[it.cloud].done || ctrl[it.cloud].hold || ctrl[it.cloud].status != SG_OK)) return;
     const SgCloud& cl = clouds[it.cloud];
     const float wc = cl.wc;
@@ -380,6 +392,7 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
     bool ok = true;
     if (tid == 0) {
         for (int s = 0; s < SG_STAGES; s++) mbar_init(&full[s], 1);
+        mbar_init(&never, 1);
         fence_mbar_init();
     }
     __syncthreads();
@@ -406,7 +419,8 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
         const uint32_t parity = (uint32_t)((t / SG_STAGES) & 1);
         const int j0 = it.j0 + t * T;
         const int len = min(T, it.j0 + it.nj - j0);
-        const bool arrived = mbar_wait(&full[s], parity);
+        bool arrived = mbar_wait(&full[s], parity);
+        if (t + 1 == wtest) arrived = wait_test(&never, errword) && arrived;
         if (!__syncthreads_and(arrived)) {  // block-uniform decision
             ok = false;
             if (tid == 0) {
@@ -567,9 +581,11 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
     constexpr int T = TJ;  // j-tile: a multiple of the 128-ion leaves
     __shared__ __align__(128) float tile[STAGES][7][T];
     __shared__ __align__(8) uint64_t full[STAGES];
+    __shared__ __align__(8) uint64_t never;  // the wait test's barrier
     __shared__ double corr[3][NT * IPT];
 
     const SgWorkItem it = items[blockIdx.x];
+    const int wtest = errword ? errword[SG_FLAG_WAIT_TILE] : 0;
     if (ctrl != nullptr && (ctrl[it.cloud].done || ctrl[it.cloud].hold || ctrl[it.cloud].status != SG_OK)) return;
     const SgCloud& cl = clouds[it.cloud];
     const float wc = cl.wc;
@@ -618,6 +634,7 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
     bool ok = true;
     if (tid == 0) {
         for (int s = 0; s < STAGES; s++) mbar_init(&full[s], 1);
+        mbar_init(&never, 1);
         fence_mbar_init();
     }
     __syncthreads();
@@ -652,7 +669,8 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         const uint32_t parity = (uint32_t)((t / STAGES) & 1);
         const int j0 = it.j0 + t * T;
         const int len = min(T, it.j0 + it.nj - j0);
-        const bool arrived = mbar_wait(&full[s], parity);
+        bool arrived = mbar_wait(&full[s], parity);
+        if (t + 1 == wtest) arrived = wait_test(&never, errword) && arrived;
         if (!__syncthreads_and(arrived)) {  // block-uniform decision
             ok = false;
             if (tid == 0) {

@@ -412,11 +412,11 @@ __global__ void __launch_bounds__(SG_ROWS) gear_kernel(DpArgs a) {
 }
 
 // error_succes + step bookkeeping (bin/ode.cpp:426-494), one thread per cloud.
-// With *hold_on_accept set, a cloud that accepts holds (skips further attempts) until
+// With flags[SG_FLAG_HOLD] set, a cloud that accepts holds (skips further attempts) until
 // the host clears the hold: used to take exactly one step per cloud.
 __global__ void dp_control_kernel(SgCloud* __restrict__ clouds, SgCtrl* __restrict__ ctrl,
                                   const double* __restrict__ err_part, const double* __restrict__ y,
-                                  int n_clouds, const int* __restrict__ hold_on_accept,
+                                  int n_clouds, const int* __restrict__ flags,
                                   const SgOp* __restrict__ ops) {
     sg_griddep_wait();
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -438,18 +438,26 @@ __global__ void dp_control_kernel(SgCloud* __restrict__ clouds, SgCtrl* __restri
     cs.force_evals += (cs.method == 4) ? 6 : (cs.method == 1 ? 1 : 7);
     cs.coulomb_evals += (cl.fp.flags & SG_F_COULOMB) ? (cs.method == 1 ? 1 : 6) : 0;
     int accepted = 1;
-    if (!isfinite(err)) {
+    if (flags[SG_FLAG_ERR] != 0) {
+        // a kernel of this attempt gave up a bounded wait: its sums are incomplete, so
+        // the attempt is neither accepted nor used for step control
+        cs.status = flags[SG_FLAG_ERR];
+        cs.done = 1;
+        accepted = 0;
+    } else if (!isfinite(err)) {
         cs.status = SG_NONFINITE;
         cs.done = 1;
         accepted = 0;
     } else if (cs.adaptive && cs.method != 1) {  // step() turns control off for Gear
-        const double alpha = 0.2, safe = 0.9, minscale = 0.2, maxscale = 10.0;
+        // beta = 0: the reference's I-controller, pow(errold, 0) = 1 exactly
+        const double beta = cs.beta, alpha = 0.2 - beta * 0.75, safe = 0.9, minscale = 0.2,
+                     maxscale = 10.0;
         if (err <= 1.0) {
             double scale;
             if (err == 0.0)
                 scale = maxscale;
             else {
-                scale = safe * pow(err, -alpha);
+                scale = safe * pow(err, -alpha) * pow(cs.errold, beta);
                 if (scale < minscale) scale = minscale;
                 if (scale > maxscale) scale = maxscale;
             }
@@ -464,7 +472,8 @@ __global__ void dp_control_kernel(SgCloud* __restrict__ clouds, SgCtrl* __restri
             accepted = 0;
             cs.rejects++;
             cs.rejects_here++;
-            const double x0 = fabs(y[cl.off]);  // IonCloud::pos[0][0] (bin/ode.cpp:482)
+            // IonCloud::pos[0][0] (bin/ode.cpp:482): x of the caller's first ion
+            const double x0 = fabs(y[cl.ion0]);
             if (fabs(cs.h) <= x0 * 2.220446049250313e-16) {
                 cs.status = SG_H_UNDERFLOW;
                 cs.done = 1;
@@ -497,7 +506,7 @@ __global__ void dp_control_kernel(SgCloud* __restrict__ clouds, SgCtrl* __restri
         } else if (cs.t >= cs.t_end) {
             cs.done = 1;
         }
-        if (*hold_on_accept) cs.hold |= 1;
+        if (flags[SG_FLAG_HOLD]) cs.hold |= 1;
         // the reference prints after a step once (t - start) > interval * prints so far
         // (bin/ion_fly.cpp:103-108); the record goes to the next ring slot, and a full
         // ring holds the cloud until the host has drained it
@@ -729,10 +738,10 @@ cudaError_t sg_gear_init(const SgDpArgs& a, const int* perm, int n_rows, cudaStr
 }
 
 cudaError_t sg_dp_control(SgCloud* clouds, SgCtrl* ctrl, const double* err_part,
-                          const double* y, int n_clouds, const int* hold_on_accept,
+                          const double* y, int n_clouds, const int* flags,
                           const SgOp* ops, cudaStream_t st) {
     sg_launch(dp_control_kernel, (n_clouds + 127) / 128, 128, 0, st, clouds, ctrl, err_part, y, n_clouds,
-                                                              hold_on_accept, ops);
+                                                              flags, ops);
     return cudaGetLastError();
 }
 

@@ -74,6 +74,17 @@ inline cudaError_t sg_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, si
 // %globaltimer and raises SG_TIMEOUT in the context's error word.
 #define SG_WAIT_NS 1000000000ull
 
+// The context's device flag words (Problem::flags): the error word the kernels raise,
+// the hold-on-accept word, the fix-up list count, and the wait test: with
+// flags[SG_FLAG_WAIT_TILE] = t + 1, every block of the FP32c Coulomb kernels waits, at
+// j-tile t, on a barrier that nothing arrives at until flags[SG_FLAG_WAIT_US]
+// microseconds have passed, and takes the timeout path (sg_set_wait_test).
+#define SG_FLAG_ERR 0
+#define SG_FLAG_HOLD 1
+#define SG_FLAG_WAIT_TILE 4
+#define SG_FLAG_WAIT_US 5
+#define SG_NFLAGS 8
+
 // One unit of Coulomb work: i-ions [i0, i0+ni) (padded indices) of cloud `cloud`
 // against j-ions [j0, j0+nj) of the same cloud; the partial sums go to slot `slot`.
 struct SgWorkItem {
@@ -100,7 +111,8 @@ struct SgCloud {
     int32_t npad;    // padded ions (multiple of SG_PAD)
     int32_t nslots;  // Coulomb partial-sum slots (j-chunks) of this cloud
     int32_t rb0, nrb;  // row blocks [rb0, rb0+nrb)
-    int32_t pad;
+    int32_t ion0;      // device index of the caller's first ion of the cloud (k-d order
+                       // moves it; the step-size underflow test reads its x)
     double cx, cy, cz;   // centre of the FP32 frame (m)
     double L, invL;      // scale of the FP32 frame (m)
     double vref;         // RMS velocity per axis at upload (m/s), proposer features
@@ -136,6 +148,7 @@ struct SgCtrl {
     // ramp's starting Vrf/Vdc, the cloud's trap terms, dissociation to apply (index+1)
     int32_t op_index, n_ops, trap_bits, dis_due;
     double t_op_start, old_vrf, old_vdc;
+    double beta;  // PI term of error_succes (0: the reference's I-controller)
 };
 
 // One operation of the sequence (sg_operation plus the row of its dissociation table).
@@ -355,7 +368,7 @@ cudaError_t sg_ck_stage(const SgDpArgs& a, int stage, int n_rows, cudaStream_t s
 cudaError_t sg_gear_stage(const SgDpArgs& a, int phase, int n_rows, cudaStream_t st);
 cudaError_t sg_gear_init(const SgDpArgs& a, const int* perm, int n_rows, cudaStream_t st);
 cudaError_t sg_dp_control(SgCloud* clouds, SgCtrl* ctrl, const double* err_part,
-                          const double* y, int n_clouds, const int* hold_on_accept,
+                          const double* y, int n_clouds, const int* flags,
                           const SgOp* ops, cudaStream_t st);
 cudaError_t sg_clear_hold(SgCtrl* ctrl, int n_clouds, cudaStream_t st);
 int sg_probe_iters(int which);

@@ -120,6 +120,7 @@ class OdeVars:
         self.rk_atol = 1e-7      # bin/ode.cpp:515-516
         self.rk_rtol = 1e-7
         self.errold = 1.0e-4
+        self.beta = 0.0          # PI term of error_succes (bin/ode.cpp:431); 0 as built
         self.reject = False
         self.EPS = float(np.finfo(np.float64).eps)
         self.change_stepsize = True
@@ -163,13 +164,14 @@ def step(cloud: IonCloud, odev: OdeVars) -> None:
     """step(), bin/ode.cpp:459-494: one accepted step of the whole cloud on the device."""
     fp = odev.forcev.field_params()
     key = (cloud.nrparticles, odev.precision, bytes(fp), odev.rk_rtol, odev.rk_atol,
-           odev.change_stepsize, odev.method)
+           odev.change_stepsize, odev.method, odev.beta)
     if odev._batch is None or odev._batch_key != key:
         op = OdeParams()
         op.rtol, op.atol, op.h0 = odev.rk_rtol, odev.rk_atol, odev.h
         op.t0, op.t_end = cloud.lifetime, float("inf")
         op.adaptive, op.max_rejects = int(odev.change_stepsize), 0
         op.method = odev.method
+        op.beta = odev.beta
         odev._batch = Batch(odev.context(), [cloud.nrparticles], [fp], [op], odev.precision)
         odev._batch.upload(cloud.pos, cloud.vel, cloud.mass, cloud.charge)
         odev._batch_key = key
@@ -250,6 +252,7 @@ class Operations:
         op.rtol, op.atol, op.h0 = odev.rk_rtol, odev.rk_atol, odev.h
         op.t0, op.t_end = cloud.lifetime, float("inf")
         op.adaptive, op.max_rejects, op.method = int(odev.change_stepsize), 0, odev.method
+        op.beta = odev.beta
         b = Batch(odev.context(), [cloud.nrparticles], [fp], [op], odev.precision)
         b.upload(cloud.pos, cloud.vel, cloud.mass, cloud.charge)
         if recorder is not None:

@@ -30,9 +30,9 @@ def _oracle():
 
 
 def one_cloud(ctx, pos, vel, mass, charge, fp, rtol, atol, h0, t_end, prec, adaptive=True,
-              max_rejects=0, method=5):
+              max_rejects=0, method=5, beta=0.0):
     op = configs.ode(rtol, atol, h0, t_end, adaptive=adaptive, max_rejects=max_rejects,
-                     method=method)
+                     method=method, beta=beta)
     b = Batch(ctx, [len(mass)], [fp], [op], prec)
     b.upload(pos, vel, mass, charge)
     return b
@@ -95,6 +95,50 @@ def test_golden_adaptive_fp32c(ctx):
     assert ep <= 1e-9 and ev <= 1e-9, (ep, ev)
     # accepted/rejected counts of the FP64 reference run
     assert abs(last[0]["steps"] - int(g[f"{tag}_ctrl"][5])) <= 1
+
+
+@pytest.mark.parametrize("beta", [0.04, 0.08])
+def test_pi_controller_vs_oracle(ctx, beta):
+    """The PI controller (beta of bin/ode.cpp:431-439) on the device against the oracle's
+    restatement, FP64: the golden's Paul-trap cloud at its tight tolerances (the whole
+    attempt history), and a Penning cloud with drive and friction (the accepted step
+    sizes, which follow the last bits of the first steps' error norms: see the test of
+    the reference controller below)."""
+    g = np.load(os.path.join(GOLD, "dp45_adaptive.npz"))
+    tag = "tight"
+    rtol, atol, t_end, h0 = g[f"{tag}_cfg"]
+    fp = paul_fp(TRAPP)
+    args = (g[f"{tag}_pos0"], g[f"{tag}_vel0"], g[f"{tag}_mass"], g[f"{tag}_charge"], fp)
+    _, _, cr, oh, nh = oracle.dp45_run(*args, rtol=rtol, atol=atol, h0=h0, t0=0.0,
+                                       t_end=t_end, hist_cap=100000, beta=beta)
+    assert cr.status == 0
+    b = one_cloud(ctx, *args, rtol, atol, h0, t_end, SG_PREC_FP64, beta=beta)
+    hist, last = attempt_history(b)
+    assert hist.shape == oh.shape
+    assert np.array_equal(hist[:, 3], oh[:, 3])          # same accept/reject sequence
+    # The first step's error norm sits on the rounding floor (~1e-6 relative between
+    # the device's and the oracle's summation orders).  The I-controller clamps the
+    # growth after it at 10x, so its step sizes never see that noise; the PI factor
+    # errold^beta lowers the scale below the clamp, and the noise, times alpha, stays
+    # in every later step size.
+    np.testing.assert_allclose(hist[:, :2], oh[:, :2], rtol=1e-5)
+    np.testing.assert_allclose(hist[:, 2], oh[:, 2], rtol=1e-5, atol=1e-9)
+    assert last["steps"] == cr.steps and last["rejects"] == cr.rejects
+
+    c = configs.penning_1k(n=300, seed=11).clouds[0]
+    fpn = configs.penning_field(quad=(0.5, configs.nu_c(132.905), 0.0, 0.0, 1.0), delta=1e3)
+    te = 0.3e-6
+    _, _, cr, oh, nh = oracle.dp45_run(c.pos, c.vel, c.mass, c.charge, fpn, rtol=1e-9,
+                                       atol=1e-15, h0=1e-9, t0=0.0, t_end=te,
+                                       hist_cap=100000, beta=beta)
+    assert cr.status == 0
+    b = one_cloud(ctx, c.pos, c.vel, c.mass, c.charge, fpn, 1e-9, 1e-15, 1e-9, te,
+                  SG_PREC_FP64, beta=beta)
+    ts, hs, last = run_recording(b)
+    ho = oh[oh[:, 3] == 1][:, 1]
+    assert last[0]["steps"] == cr.steps
+    np.testing.assert_allclose(hs[0][:2], ho[:2], rtol=1e-5)
+    np.testing.assert_allclose(hs[0][2:20], ho[2:20], rtol=1e-6)
 
 
 @pytest.mark.parametrize("prec", [SG_PREC_FP64, SG_PREC_FP32C])
@@ -266,6 +310,37 @@ def test_underflow_status(ctx):
     with pytest.raises(RuntimeError, match="stepsize underflow created"):
         for _ in range(100000):
             ode.step(cl, od)
+
+
+def test_underflow_reads_callers_first_ion_in_kd_order(ctx):
+    """The underflow test |h| <= |pos[0][0]| eps (bin/ode.cpp:482) reads the caller's
+    first ion also when the device holds the cloud in k-d order.  That ion sits at
+    x = 0.1 m, so the k-d order puts it in the last leaf and the first leaf's first ion
+    is ~1 mm out.  A nearly coincident pair keeps every attempt rejected at the 0.2
+    floor, so h = 1e-9 0.2^k: the caller's ion gives underflow at k = 11, the first
+    sorted ion would give it ~3 rejects later.  Both runs are bounded."""
+    c = configs.penning_1k(n=512, seed=21).clouds[0]
+    pos = c.pos.copy()
+    pos[0] = [0.1, 2e-4, -1e-4]           # the caller's first ion: |x| = 0.1 m
+    pos[2] = pos[1] + 1e-13               # a nearly coincident pair: err explodes
+    fp = paul_fp(TRAPP)
+    _, _, cr, oh, nh = oracle.dp45_run(pos, c.vel, c.mass, c.charge, fp, rtol=1e-15,
+                                       atol=1e-30, h0=1e-9, t0=0.0, t_end=1e-6,
+                                       max_steps=2, hist_cap=1000)
+    assert cr.status == abi.SG_H_UNDERFLOW and cr.steps == 0
+    k = int(np.ceil(np.log(1e-9 / (0.1 * np.finfo(float).eps)) / np.log(5.0)))
+    assert cr.rejects == k == 11
+    ctx.set_coulomb_variant(9)            # a k-d ordered launch shape
+    try:
+        b = one_cloud(ctx, pos, c.vel, c.mass, c.charge, fp, 1e-15, 1e-30, 1e-9, 1e-6,
+                      SG_PREC_FP32C)
+        info, st = b.run(max_attempts=100, raise_on_error=False)
+    finally:
+        ctx.set_coulomb_variant(-1)
+    s = info[0]
+    assert s["status"] == abi.SG_H_UNDERFLOW and s["done"] == 1
+    assert s["rejects"] == cr.rejects and s["steps"] == 0, (s, cr.rejects)
+    assert s["h"] == pytest.approx(cr.h, rel=1e-12)
 
 
 def test_nonfinite_status(ctx):

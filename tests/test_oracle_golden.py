@@ -142,6 +142,46 @@ def test_controller_table():
     assert oracle.lib().orc_error_succes(1e9, c) == 0 and c.h == pytest.approx(0.2)
 
 
+@pytest.mark.parametrize("beta", [0.04, 0.08])
+def test_pi_controller_table(beta):
+    """The PI form of error_succes (bin/ode.cpp:431-439): alpha = 0.2 - 0.75 beta and the
+    factor errold^beta on accepted steps; rejects use err^-alpha alone."""
+    alpha = 0.2 - 0.75 * beta
+    c = oracle.OrcCtrl()
+    c.beta = beta
+    c.h, c.errold, c.reject = 1.0, 0.3, 0
+    assert oracle.lib().orc_error_succes(0.5, c) == 1
+    assert c.hnext == pytest.approx(0.9 * 0.5 ** -alpha * 0.3 ** beta, rel=1e-15)
+    assert c.errold == 0.5
+    assert oracle.lib().orc_error_succes(2.0, c) == 0
+    assert c.h == pytest.approx(0.9 * 2.0 ** -alpha, rel=1e-15) and c.reject == 1
+    c.h, c.reject, c.errold = 1.0, 0, 1e-4
+    assert oracle.lib().orc_error_succes(1e-3, c) == 1
+    # 0.9 * 1e-3^-alpha * 1e-4^beta, clamped to [0.2, 10]
+    assert c.hnext == pytest.approx(min(10.0, 0.9 * 1e-3 ** -alpha * 1e-4 ** beta), rel=1e-15)
+
+
+def test_beta_zero_is_the_reference_controller():
+    """beta = 0 multiplies by errold^0 = 1 exactly: the history against the reference's
+    golden is the one of the test above."""
+    g = np.load(os.path.join(GOLD, "dp45_adaptive.npz"))
+    tag = "default"
+    rtol, atol, t_end, h0 = g[f"{tag}_cfg"]
+    fp = paul_fp(np.array([50.0, 5.0, 0.001, 0.04, 0.04, 50e5, 100.0]))
+    fp.flags &= ~SG_F_TOF
+    _, _, c, hist, _ = oracle.dp45_run(g[f"{tag}_pos0"], g[f"{tag}_vel0"], g[f"{tag}_mass"],
+                                       g[f"{tag}_charge"], fp, rtol=rtol, atol=atol, h0=h0,
+                                       t0=0.0, t_end=t_end, hist_cap=100000, beta=0.0)
+    gh = g[f"{tag}_hist"]
+    assert np.array_equal(hist[:, 3], gh[:, 3])
+    np.testing.assert_allclose(hist, gh, rtol=1e-13, atol=0)
+    # PI control changes the sequence (and needs no more attempts here)
+    _, _, c8, hist8, _ = oracle.dp45_run(g[f"{tag}_pos0"], g[f"{tag}_vel0"], g[f"{tag}_mass"],
+                                         g[f"{tag}_charge"], fp, rtol=rtol, atol=atol, h0=h0,
+                                         t0=0.0, t_end=t_end, hist_cap=100000, beta=0.08)
+    assert c8.status == SG_OK and not np.array_equal(hist8[:, 1], gh[: len(hist8), 1])
+
+
 def test_underflow_status():
     """A step size driven to zero gives the reference's underflow (ode.cpp:482-483)."""
     g = np.load(os.path.join(GOLD, "force_edges.npz"))
