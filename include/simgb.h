@@ -255,6 +255,32 @@ int sg_mlp_train(sg_ctx* ctx, int n, const float* X, const float* Y, int iters, 
 /* Use the MLP (w != NULL) with step-size safety factor `safety` in (0, 1] for the
  * clouds of the batch, or the reference's controller (w == NULL). */
 int sg_batch_set_proposer(sg_ctx* ctx, const float* w, double safety);
+/* In-run check of the FP32c Coulomb sums (no counterpart in the reference).  Every
+ * `every_attempts` attempts (default 16; 0 = off) the last Coulomb sum of the attempt
+ * is checked, per cloud, at eight probe ions -- the two ions without fix-up whose far
+ * terms are largest next to their net force (sqrt(s2f)/|P|), the two whose near terms
+ * are, and four drawn at random -- against their rows evaluated exactly in FP64.  From
+ * the far-ranked probes the check measures c = err / (sqrt(s2f)/|P|) and lowers the
+ * cloud's far fix-up threshold kfar (an ion with sqrt(s2f) > kfar |P| is corrected) to
+ * 5e-7 / c when that is below the prior set from the cloud's density.  FP32c batches
+ * only. */
+typedef struct sg_check_info {
+    double max_err;      /* largest per-ion relative error over every check               */
+    double last_err;     /* largest of the last check                                     */
+    double c_far;        /* largest measured err / (sqrt(s2f)/|P|), 0 before any          */
+    double kfar;         /* far fix-up threshold in use                                   */
+    double kfar_prior;   /* the prior from the cloud's density (or sg_batch_set_far_threshold) */
+    int64_t checks;      /* checks made                                                   */
+    int64_t probes;      /* probe ions evaluated                                          */
+    int64_t breaches;    /* probes above 1e-6                                             */
+} sg_check_info;
+int sg_batch_set_force_check(sg_ctx* ctx, int every_attempts);
+int sg_batch_force_check(sg_ctx* ctx, sg_check_info* out);  /* out[n_clouds] */
+/* Prior of the far fix-up threshold for every cloud of the batch (kfar > 0), or the
+ * automatic prior from each cloud's density (kfar = 0); clears the measured record.
+ * Takes effect at the next sg_batch_upload / sg_batch_set_state. */
+int sg_batch_set_far_threshold(sg_ctx* ctx, double kfar);
+
 /* Test of the bounded device waits (no counterpart in the reference).  With tile >= 0,
  * every block of the FP32c Coulomb kernels of the current batch, once its j-tile
  * `tile` has arrived, also waits on a barrier that nothing arrives at until limit_us

@@ -72,6 +72,17 @@ class StepInfo(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
 
 
+class CheckInfo(ctypes.Structure):
+    """sg_check_info (include/simgb.h)."""
+    _fields_ = [("max_err", ctypes.c_double), ("last_err", ctypes.c_double),
+                ("c_far", ctypes.c_double), ("kfar", ctypes.c_double),
+                ("kfar_prior", ctypes.c_double), ("checks", ctypes.c_int64),
+                ("probes", ctypes.c_int64), ("breaches", ctypes.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 SG_OP_NORMAL, SG_OP_TOF, SG_OP_TRAP_RAMP, SG_OP_FREE, SG_OP_DISSOCIATION = 0, 1, 2, 3, 4
 
 
@@ -93,6 +104,7 @@ _vp = ctypes.c_void_p
 EXPORTED = [
     "sg_create", "sg_destroy", "sg_status_string", "sg_last_cuda_error", "sg_sync",
     "sg_version", "sg_coulomb_accel", "sg_force", "sg_coulomb_accel_noalloc", "sg_set_wait_test",
+    "sg_batch_set_force_check", "sg_batch_force_check", "sg_batch_set_far_threshold",
     "sg_batch_create", "sg_batch_upload",
     "sg_batch_set_state", "sg_batch_download", "sg_batch_attempts", "sg_dp45_step",
     "sg_batch_run", "sg_batch_info", "sg_batch_set_field", "sg_batch_set_t_end",
@@ -133,6 +145,9 @@ def _declare(L):
                            ctypes.c_double, ctypes.POINTER(FieldParams), _dp]
     L.sg_coulomb_accel_noalloc.argtypes = [ctypes.c_int, _vp, _vp, _vp, _vp, _vp]
     L.sg_set_wait_test.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
+    L.sg_batch_set_force_check.argtypes = [_vp, ctypes.c_int]
+    L.sg_batch_force_check.argtypes = [_vp, ctypes.POINTER(CheckInfo)]
+    L.sg_batch_set_far_threshold.argtypes = [_vp, ctypes.c_double]
     L.sg_batch_create.argtypes = [_vp, ctypes.c_int, _ip, ctypes.POINTER(FieldParams),
                                   ctypes.POINTER(OdeParams), ctypes.c_int]
     L.sg_batch_upload.argtypes = [_vp, _dp, _dp, _dp, _ip]

@@ -207,6 +207,26 @@ class Batch:
         self._live()
         check(self._L.sg_batch_attempts(self.ctx.handle, int(n)), "sg_batch_attempts")
 
+    def set_force_check(self, every_attempts: int):
+        """In-run check of the FP32c sums every `every_attempts` attempts (0: off)."""
+        self._live()
+        check(self._L.sg_batch_set_force_check(self.ctx.handle, int(every_attempts)),
+              "sg_batch_set_force_check")
+
+    def force_check(self):
+        """Per cloud: the in-run check's record (sg_check_info as a dict)."""
+        self._live()
+        out = (abi.CheckInfo * self.n_clouds)()
+        check(self._L.sg_batch_force_check(self.ctx.handle, out), "sg_batch_force_check")
+        return [o.as_dict() for o in out]
+
+    def set_far_threshold(self, kfar: float):
+        """Prior of the far fix-up threshold of every cloud (0: from each cloud's density);
+        applies from the next upload or set_state."""
+        self._live()
+        check(self._L.sg_batch_set_far_threshold(self.ctx.handle, float(kfar)),
+              "sg_batch_set_far_threshold")
+
     def step(self, raise_on_error=True):
         self._live()
         st = self._L.sg_dp45_step(self.ctx.handle, self._info)

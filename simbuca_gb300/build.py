@@ -16,7 +16,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 OUT = os.path.join(PKG, "libsimgb.so")
-UNITS = ["coulomb.cu", "dp45.cu", "capi.cu", "aux_kernels.cu", "noalloc.cu",
+UNITS = ["coulomb.cu", "dp45.cu", "capi.cu", "aux_kernels.cu", "noalloc.cu", "check.cu",
          "proposer.cu", "cloud_io.cu", "observe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]

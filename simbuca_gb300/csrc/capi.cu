@@ -81,6 +81,13 @@ struct Problem {
     int* dis_spec = nullptr;     // [dissociations][N] caller order
     double* dis_mass = nullptr;
     int n_dis = 0;
+    // in-run force check of the FP32c sums (check.cu): every check_every attempts
+    float* risk = nullptr;   // [2][N] far and near ratios of the last in-attempt sum
+    int* ran = nullptr;      // [clouds] an in-attempt sum ran since the last check
+    SgCheck* dchk = nullptr; // [clouds] check records and measured thresholds
+    int check_every = 16;
+    long long attempt_count = 0;
+    double kfar_prior = 0.0;  // > 0: the far fix-up threshold's prior of every cloud
 };
 
 struct TimedLaunch {
@@ -190,6 +197,9 @@ void free_problem(Problem& P) {
     cudaFree(P.mass0);
     cudaFree(P.log_feat);
     cudaFree(P.log_num);
+    cudaFree(P.risk);
+    cudaFree(P.ran);
+    cudaFree(P.dchk);
     if (P.hctrl) cudaFreeHost(P.hctrl);
     P = Problem();
 }
@@ -369,12 +379,18 @@ void set_frame(SgCloud& cl, const double* pos_aos, int off) {
     // far tiles (sorted kernel): beyond every capped pair, and far enough that the
     // high parts alone give the pair distance to ~1e-6
     cl.dfar = (float)std::max(0.25, 1.01 * rc);
-    // Far fix-up threshold.  The error of the hi-only far terms is ~c sqrt(s2f) with c
-    // growing as the square root of the ion density in frame units, i.e. of n (numpy
-    // model of the kernel's arithmetic: c ~ 1.2e-6 for the 1M-ion spheroid, ~2.5e-7 for
-    // the 65,536-ion Gaussian cloud); fixing ions with c sqrt(s2f) > 5e-7 |P| keeps them
-    // at half the 1e-6 bound: sqrt(s2f) > 0.5 |P| from ~1M ions up, 2 |P| at 65,536.
-    cl.kfar2 = (float)(0.25 * std::max(1.0, 1048576.0 / std::max(n, 1)));
+    // Prior of the far fix-up threshold.  The error of the hi-only far terms is
+    // ~c sqrt(s2f)/|P| with c growing with the ion density in frame units, n / vol.
+    // Measured (numpy model of the kernel's arithmetic, and the GPU): c = 2.5e-7 for the
+    // 65,536-ion Gaussian cloud (density 4.2e3), 1.2e-6 for the 1M-ion uniform spheroid
+    // (density 2.7e5): c = 1.08e-8 density^0.377 through both.  Ions with
+    // c sqrt(s2f) > 5e-7 |P| are fixed up, which keeps the others at half the 1e-6 bound.
+    // The in-run check (check.cu) measures c on the cloud itself and lowers the
+    // threshold when it finds a larger c.
+    const double density = std::max(n, 1) / vol;
+    const double c_far = 1.08e-8 * std::pow(density, 0.377);
+    const double kfar = 5e-7 / c_far;
+    cl.kfar2 = (float)(kfar * kfar);
 }
 
 // k-d tree order of one cloud: recursive median splits along the widest axis, the
@@ -432,6 +448,18 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(dalloc(&P.stage, 6 * N));
     CK(dalloc(&P.flags, SG_NFLAGS));
     CK(cudaMemset(P.flags, 0, SG_NFLAGS * sizeof(int)));
+    if (P.precision == SG_PREC_FP32C) {
+        CK(dalloc(&P.risk, 2 * N));
+        CK(dalloc(&P.ran, (size_t)std::max(P.n_clouds, 1)));
+        CK(cudaMemset(P.ran, 0, sizeof(int) * (size_t)std::max(P.n_clouds, 1)));
+        std::vector<SgCheck> h0((size_t)std::max(P.n_clouds, 1));
+        for (SgCheck& h : h0) {
+            memset(&h, 0, sizeof h);
+            h.kfar2 = INFINITY;
+        }
+        CK(dalloc(&P.dchk, h0.size()));
+        CK(cudaMemcpy(P.dchk, h0.data(), sizeof(SgCheck) * h0.size(), cudaMemcpyHostToDevice));
+    }
     CK(dalloc(&P.pst, (size_t)std::max(P.n_clouds, 1)));
     CK(cudaMemset(P.pst, 0, sizeof(SgProposerState) * (size_t)std::max(P.n_clouds, 1)));
     CK(cudaMalloc(&P.wbf, SG_MLP_NP * 2));
@@ -649,6 +677,13 @@ int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter, double
     ca.fix_part = P.fix_part;
     ca.fix_done = P.fix_done;
     ca.far_estimate = far_estimate ? 1 : 0;
+    if (P.precision == SG_PREC_FP32C) {
+        ca.chk = P.dchk;
+        if (out == P.coulS) {
+            ca.risk = P.risk;
+            ca.ran = P.ran;
+        }
+    }
     TimedLaunch tl{nullptr, nullptr, inter};
     const int cap = ctx->capture_events;
     if (cap >= 0) {
@@ -799,6 +834,16 @@ int capture_attempt(sg_ctx* ctx, Problem& P, bool timed, cudaGraphExec_t* out) {
     return SG_OK;
 }
 
+// The in-run force check (check.cu) after an attempt, every check_every attempts of an
+// FP32c batch; its launches are not part of the attempt graph.
+int maybe_check(sg_ctx* ctx, Problem& P) {
+    if (!P.dchk || P.check_every <= 0 || !P.any_coulomb) return SG_OK;
+    if (++P.attempt_count % P.check_every != 0) return SG_OK;
+    CK(sg_force_check(P.dc, P.n_clouds, P.ran, P.risk, P.c64, P.npad, P.coulS, P.n, P.dchk,
+                      ctx->stream));
+    return SG_OK;
+}
+
 int run_attempts(sg_ctx* ctx, Problem& P, int n) {
     if (ctx->use_graph && ctx->timing) {
         // graph replays one at a time, reading the Coulomb event pairs after each
@@ -811,6 +856,10 @@ int run_attempts(sg_ctx* ctx, Problem& P, int n) {
         for (int i = 0; i < n; i++) {
             const double inter = active_interactions(P);
             CK(cudaGraphLaunch(ctx->graph_timed, ctx->stream));
+            {
+                int st = maybe_check(ctx, P);
+                if (st != SG_OK) return st;
+            }
             if (pairs) {
                 CK(cudaEventSynchronize(ctx->gev[2 * pairs - 1]));
                 for (int k = 0; k < pairs; k++) {
@@ -838,11 +887,17 @@ int run_attempts(sg_ctx* ctx, Problem& P, int n) {
             int st = capture_attempt(ctx, P, false, &ctx->graph);
             if (st != SG_OK) return st;
         }
-        for (int i = 0; i < n; i++) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+        for (int i = 0; i < n; i++) {
+            CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+            int st = maybe_check(ctx, P);
+            if (st != SG_OK) return st;
+        }
         return SG_OK;
     }
     for (int i = 0; i < n; i++) {
         int st = enqueue_attempt(ctx, P);
+        if (st != SG_OK) return st;
+        st = maybe_check(ctx, P);
         if (st != SG_OK) return st;
     }
     return SG_OK;
@@ -920,6 +975,9 @@ void ion_constants(const Problem& P, const double* mass, const int* charge,
 int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel,
                  bool resort = true, bool sync = true) {
     const size_t N = (size_t)P.n;
+    // the last in-attempt Coulomb sums no longer match the Coulomb inputs
+    if (P.ran)
+        CK(cudaMemsetAsync(P.ran, 0, sizeof(int) * (size_t)std::max(P.n_clouds, 1), ctx->stream));
     if (P.sorted && resort) {
         for (int c = 0; c < P.n_clouds; c++)
             kd_order(pos, P.hc[c].off, P.hc[c].n, P.perm.data() + P.hc[c].off);
@@ -950,6 +1008,7 @@ int upload_state(sg_ctx* ctx, Problem& P, const double* pos, const double* vel,
     }
     for (int c = 0; c < P.n_clouds; c++) {
         set_frame(P.hc[c], pos, P.hc[c].off);
+        if (P.kfar_prior > 0.0) P.hc[c].kfar2 = (float)(P.kfar_prior * P.kfar_prior);
         double v2 = 0.0;
         if (vel)
             for (int i = P.hc[c].off; i < P.hc[c].off + P.hc[c].n; i++)
@@ -1986,6 +2045,63 @@ int sg_batch_set_proposer(sg_ctx* ctx, const float* w, double safety) {
         if (st != SG_OK) return st;
     }
     CK(cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
+int sg_batch_set_force_check(sg_ctx* ctx, int every_attempts) {
+    if (!ctx || every_attempts < 0) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    P.check_every = every_attempts;
+    P.attempt_count = 0;
+    return SG_OK;
+}
+
+int sg_batch_force_check(sg_ctx* ctx, sg_check_info* out) {
+    if (!ctx || !out) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    if (!P.dchk) {
+        for (int c = 0; c < P.n_clouds; c++) memset(&out[c], 0, sizeof(sg_check_info));
+        return SG_OK;
+    }
+    std::vector<SgCheck> h(P.n_clouds);
+    std::vector<SgCloud> cl(P.n_clouds);
+    CK(cudaMemcpyAsync(h.data(), P.dchk, sizeof(SgCheck) * P.n_clouds, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(cl.data(), P.dc, sizeof(SgCloud) * P.n_clouds, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int c = 0; c < P.n_clouds; c++) {
+        sg_check_info& o = out[c];
+        memset(&o, 0, sizeof o);
+        o.max_err = h[c].max_err;
+        o.last_err = h[c].last_err;
+        o.c_far = h[c].c_far;
+        o.kfar = std::sqrt((double)std::min(cl[c].kfar2, h[c].kfar2));
+        o.kfar_prior = std::sqrt((double)cl[c].kfar2);
+        o.checks = h[c].checks;
+        o.probes = h[c].probes;
+        o.breaches = h[c].breaches;
+    }
+    return SG_OK;
+}
+
+int sg_batch_set_far_threshold(sg_ctx* ctx, double kfar) {
+    if (!ctx || !(kfar >= 0.0) || !std::isfinite(kfar)) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    P.kfar_prior = kfar;
+    if (P.dchk) {
+        std::vector<SgCheck> h0(P.n_clouds);
+        for (SgCheck& h : h0) {
+            memset(&h, 0, sizeof h);
+            h.kfar2 = INFINITY;
+        }
+        CK(cudaMemcpy(P.dchk, h0.data(), sizeof(SgCheck) * h0.size(), cudaMemcpyHostToDevice));
+    }
     return SG_OK;
 }
 

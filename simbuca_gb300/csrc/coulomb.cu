@@ -1121,7 +1121,8 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     const SgCtrl* __restrict__ ctrl, const double* __restrict__ part, int npad_total,
     double* __restrict__ out, int n_total, int* __restrict__ counters,
     int* __restrict__ fix_list, double* __restrict__ fix_pf, const float* __restrict__ c32,
-    const double* __restrict__ c64, const float* __restrict__ bbox) {
+    const double* __restrict__ c64, const float* __restrict__ bbox, float* __restrict__ risk,
+    int* __restrict__ ran, const SgCheck* __restrict__ chk) {
     sg_griddep_wait();
     const SgRowBlock rb = rows[blockIdx.x];
     if (ctrl != nullptr &&
@@ -1152,10 +1153,17 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
         out[2 * (size_t)n_total + i] = pz;
         if (F32) {
             pf = sqrt(px * px + py * py + pz * pz) * (cl.L * cl.L);  // frame units
-            kind = (s2 > kKappa2 * pf * pf ? kFixNear : 0) |
-                   (s2f > (double)cl.kfar2 * pf * pf ? kFixFar : 0);
+            // the far threshold: the prior of the frame set-up, or the measured one
+            const double kf2 = chk ? fmin((double)cl.kfar2, (double)chk[rb.cloud].kfar2)
+                                   : (double)cl.kfar2;
+            kind = (s2 > kKappa2 * pf * pf ? kFixNear : 0) | (s2f > kf2 * pf * pf ? kFixFar : 0);
+            if (risk != nullptr) {
+                risk[i] = kind ? -1.f : (float)(sqrt(s2f) / pf);
+                risk[(size_t)n_total + i] = kind ? -1.f : (float)(sqrt(s2) / pf);
+            }
         }
     }
+    if (F32 && ran != nullptr && li == 0) ran[rb.cloud] = 1;
     if (!F32) return;
     if (!INBLOCK) {
         if (kind) {
@@ -1396,14 +1404,14 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
         if (n_total <= kInBlockFixupMax) {
             sg_launch(coulomb_reduce_kernel<true, true>, n_rows, SG_ROWS, 0, s, 
                 rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, nullptr,
-                nullptr, a.c32, a.c64, bbox);
+                nullptr, a.c32, a.c64, bbox, a.risk, a.ran, a.chk);
             return cudaGetLastError();
         }
         cudaError_t e = cudaMemsetAsync(a.fix_list, 0, 2 * sizeof(int), s);
         if (e != cudaSuccess) return e;
         coulomb_reduce_kernel<true, false><<<n_rows, SG_ROWS, 0, s>>>(
             rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, a.fix_list,
-            a.fix_pf, nullptr, nullptr, nullptr);
+            a.fix_pf, nullptr, nullptr, nullptr, a.risk, a.ran, a.chk);
         // a block per flagged ion: a fixed grid that strides over however many there are
         // (flagged ions are a small fraction: small batches get a small grid)
         const int grid = n_total / 256 < 1 ? 1 : (n_total / 256 > kFixupBlocks ? kFixupBlocks : n_total / 256);
@@ -1413,7 +1421,7 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
     } else {
         sg_launch(coulomb_reduce_kernel<false, false>, n_rows, SG_ROWS, 0, s, 
             rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, nullptr,
-            nullptr, nullptr, nullptr, nullptr);
+            nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
     }
     return cudaGetLastError();
 }

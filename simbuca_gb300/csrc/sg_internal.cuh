@@ -422,7 +422,31 @@ struct SgCoulombArgs {
     // k-d ordered shapes: accumulate the far tiles' conditioning estimate s2f in this
     // call (it costs the kernel ~4 %); otherwise the slots keep the last call's values
     int far_estimate;
+    // in-run force check (check.cu), FP32c sums of an attempt only: the reduction writes
+    // each ion's far and near ratios sqrt(s2f)/|P|, sqrt(s2)/|P| (-1 when the ion is
+    // fixed up) to risk[2][N] and marks its cloud in ran[]; chk holds each cloud's
+    // measured far fix-up threshold
+    float* risk = nullptr;
+    int* ran = nullptr;
+    const struct SgCheck* chk = nullptr;
 };
+
+// ---- in-run force check (check.cu) ---------------------------------------------
+#define SG_CHECK_PROBES 8
+struct SgCheck {
+    double max_err;    // largest per-ion relative error over every check
+    double last_err;   // largest of the last check
+    double c_far;      // largest err / (sqrt(s2f)/|P|) of the far-ranked probes
+    long long checks, probes, breaches;  // breaches: probes above 1e-6
+    float kfar2;       // measured far fix-up threshold (kfar^2); +inf until measured
+    int32_t pad;
+    int32_t ion[SG_CHECK_PROBES];
+    float rf[SG_CHECK_PROBES], rn[SG_CHECK_PROBES];
+    double err[SG_CHECK_PROBES];
+};
+cudaError_t sg_force_check(const SgCloud* clouds, int n_clouds, int* ran, const float* risk,
+                           const double* c64, int npad_total, const double* out, int n_total,
+                           SgCheck* chk, cudaStream_t st);
 
 #define SG_C32_VARIANTS 17
 // variant 4: ions in k-d tree order, far tile pairs from the high parts only

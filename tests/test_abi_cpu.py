@@ -70,6 +70,7 @@ STRUCTS = {
     "sg_field_params": abi.FieldParams,
     "sg_ode_params": abi.OdeParams,
     "sg_step_info": abi.StepInfo,
+    "sg_check_info": abi.CheckInfo,
 }
 
 
