@@ -207,6 +207,33 @@ def stage_roofline(args, w, st, attempts):
               "per ion and stage)"}
 
 
+def settled(hist_h) -> bool:
+    """The step size has settled once three successive accepted steps changed it by
+    less than 10 % each (the controller starts at h0 = 1 ns and grows h by up to 10x)."""
+    return len(hist_h) >= 4 and all(abs(hist_h[-k] / hist_h[-k - 1] - 1) < 0.1
+                                    for k in (1, 2, 3))
+
+
+def check_summary(records, every):
+    """The in-run FP32c force check (sg_batch_force_check) over every cloud."""
+    if not records or not any(r["checks"] for r in records):
+        return None
+    return {"every_attempts": every,
+            "checks": int(sum(r["checks"] for r in records)),
+            "probes": int(sum(r["probes"] for r in records)),
+            "breaches_above_1e-6": int(sum(r["breaches"] for r in records)),
+            "max_err": max(r["max_err"] for r in records),
+            "c_far_max": max(r["c_far"] for r in records),
+            "kfar_min": min(r["kfar"] for r in records),
+            "kfar_prior_min": min(r["kfar_prior"] for r in records),
+            "what": "per-ion relative Coulomb error of 8 probe ions per cloud (largest far and "
+                    "near conditioning ratios without fix-up, and 4 random) against their FP64 "
+                    "rows, every few attempts of the whole run"}
+
+
+CHECK_EVERY = 16  # the library's default interval of the in-run force check
+
+
 def apply_step_control(args, batch) -> str:
     """The learned proposer with the shipped weights (every attempt still accepted or
     rejected by the Dormand-Prince error estimate), or the reference's I-controller."""
@@ -246,7 +273,7 @@ def run_ours(args, dist: Dist):
     for _ in range(args.settle):
         info, _ = batch.step()
         hist_h.append(info[0]["h_last"])
-        if len(hist_h) >= 4 and all(abs(hist_h[-k] / hist_h[-k - 1] - 1) < 0.1 for k in (1, 2, 3)):
+        if settled(hist_h):
             break
     snap_pos, snap_vel = batch.download()
     snap = info0()
@@ -278,6 +305,7 @@ def run_ours(args, dist: Dist):
     s_after = info0()
     fixups = ctx.fixup_count()
     total_ms = sum(step_ms)
+    checks = check_summary(batch.force_check(), CHECK_EVERY) if prec == abi.SG_PREC_FP32C else None
 
     # ---- Coulomb kernel timing: a second pass of as many steps with CUDA events
     # around every Coulomb launch (the events and their host reads stay out of the
@@ -384,8 +412,10 @@ def run_ours(args, dist: Dist):
         # (+2 per attempt with the proposer: cloud moments and the MLP)
         "gpu_launches": int(attempts * ((27 if prec == abi.SG_PREC_FP32C and w.n_total > 8192
                                          else 21) + (2 if args.proposer == "on" else 0))
-                            + args.steps),
+                            + args.steps
+                            + (3 * (attempts // CHECK_EVERY) if prec == abi.SG_PREC_FP32C else 0)),
         "fixup_ions_per_coulomb_call": fixups / max(1, 6 * attempts),
+        "force_check": checks,
         "attempts": int(attempts),
         "interactions_per_s": kt["interactions"] / (kt["coulomb_ms"] * 1e-3) if kt["coulomb_ms"] else None,
         "roofline": {"bound": "fp32" if prec == abi.SG_PREC_FP32C else "fp64",
@@ -505,6 +535,7 @@ def run_batched(args, dist: Dist):
     clk = clocks.stop()
     s_after = batch.info()
     total_ms = sum(step_ms)
+    checks = check_summary(batch.force_check(), CHECK_EVERY) if prec == abi.SG_PREC_FP32C else None
     sim_us = (tsum(s_after) - tsum(s_before)) * 1e6
     attempts = sum((a["steps"] + a["rejects"]) - (b["steps"] + b["rejects"])
                    for a, b in zip(s_after, s_before))
@@ -542,8 +573,11 @@ def run_batched(args, dist: Dist):
                    "parallelism": f"replicas x{dist.world}",
                    "l2": "flushed (256 MB write) between timed steps"},
         "gpu_launches": int(((27 if args.precision == "fp32c" else 21)
-                             + (2 if args.proposer == "on" else 0)) * per_step * args.steps),
+                             + (2 if args.proposer == "on" else 0)) * per_step * args.steps
+                            + (3 * (per_step * args.steps // CHECK_EVERY)
+                               if args.precision == "fp32c" else 0)),
         "attempts": int(attempts),
+        "force_check": checks,
         "coulomb_interactions_per_s": sum(
             6.0 * n * (n - 1) * ((a["steps"] + a["rejects"]) - (b["steps"] + b["rejects"]))
             for n, a, b in zip(w.counts, s_after, s_before)) / (total_ms * 1e-3),
@@ -593,7 +627,15 @@ def cpu_baseline_sample(w, allc, s_before, s_after, target_s=15.0):
 # ---------------------------------------------------------------------------
 # reference arm: the CPU oracle on all host cores
 # ---------------------------------------------------------------------------
+REF_TIME_CAP_S = 60.0  # the reference arm's timed steps stop once this much time has passed
+
+
 def run_reference(args, dist: Dist):
+    """The CPU oracle's full Dormand-Prince steps of the workload's (first) cloud on all
+    host threads.  Like our arm it first lets the step size settle by the same rule and
+    takes the same warm-up steps, so both arms time the same stretch of trajectory;
+    it times the first of its `steps` steps, stopping early once REF_TIME_CAP_S have
+    passed (at least one step; ~8 s each at 65,536 ions on 16 Arm threads)."""
     if dist.rank != 0:
         return None
     import oracle
@@ -602,54 +644,71 @@ def run_reference(args, dist: Dist):
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
     w = configs.WORKLOADS[args.workload]()
-    c = w.concat()
     # one cloud at a time, as the reference runs them
     cl0 = w.clouds[0]
     fp, op = w.fields[0], w.odes[0]
     pos, vel = cl0.pos.copy(), cl0.vel.copy()
-    ctrl = None
     h = op.h0
     t = op.t0
-    errold, reject = 1e-4, 0
 
-    def one_attempt():
-        nonlocal pos, vel, t, h, errold, reject
-        # one Dormand-Prince attempt (plus its acceptance) with the state carried over
+    def one_step():
+        """One accepted step (all its attempts) with the state carried over; returns
+        (accepted step size, attempts)."""
+        nonlocal pos, vel, t, h
         p2, v2, cc, hist, nh = oracle.dp45_run(pos, vel, cl0.mass, cl0.charge, fp,
                                                rtol=op.rtol, atol=op.atol, h0=h, t0=t,
                                                t_end=float("inf"), max_steps=1, hist_cap=64)
-        # dp45_run retries until one step is accepted: count its attempts
         dsim = cc.t - t
         pos, vel, t, h = p2, v2, cc.t, cc.h
         return dsim, max(nh, 1)
 
-    # the reference arm caps its timed sample so the run stays within a few minutes
-    warm = min(args.warmup, 1)
-    steps = max(1, min(args.steps, 3))
-    for _ in range(warm):
-        one_attempt()
+    t_start = time.perf_counter()
+    hist_h = []
+    for _ in range(args.settle):
+        hist_h.append(one_step()[0])
+        if settled(hist_h):
+            break
+    h_settled = h
+    for _ in range(args.warmup):
+        one_step()
+    prep_s = time.perf_counter() - t_start
     t0 = time.perf_counter()
     sim = 0.0
     att = 0
-    for _ in range(steps):
-        d, a = one_attempt()
+    steps = 0
+    while steps < max(1, args.steps):
+        d, a = one_step()
         sim += d
         att += a
+        steps += 1
+        if time.perf_counter() - t0 >= REF_TIME_CAP_S:
+            break
     dt = time.perf_counter() - t0
     value = sim * 1e6 / dt
     return {
         "impl": "reference",
         "metric": "sim-us/wall-s (Coulomb + Penning field + Dormand-Prince, one cloud per GPU)",
         "value": value, "unit": "sim-us/wall-s", "n_gpus": dist.world, "steps": steps,
-        "warmup": warm, "ms_per_step": dt * 1e3 / steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": dt * 1e3 / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
         "data": "synthetic (seeded Gaussian cloud, Maxwell-Boltzmann velocities)",
-        "config": {"workload": args.workload, "ions": w.n_total, "clouds": len(w.counts),
-                   "precision": "fp64", "rtol": 1e-9, "atol": 1e-15,
-                   "parallelism": "CPU threads"},
+        "config": {"workload": args.workload, "ions": len(cl0.mass), "clouds": 1,
+                   "precision": "fp64", "rtol": op.rtol, "atol": op.atol,
+                   "parallelism": f"CPU threads x{cores}",
+                   "l2": "not applicable (CPU)",
+                   "settle_steps": len(hist_h), "h_settled": h_settled,
+                   "method": "dormand-prince",
+                   "step_control": "reference I-controller (bin/ode.cpp:426-457)",
+                   "coulomb_variant": "CPU FP64 direct sum",
+                   "timed_steps": f"{steps} of {args.steps} (timing stops after "
+                                  f"{REF_TIME_CAP_S:.0f} s)",
+                   "settle_and_warmup_s": prep_s},
+        "mean_h": sim / steps,
+        "attempts": att,
         "cpu_baseline": {"value": value, "unit": "sim-us/wall-s", "cores": cores, "kind": "port",
                          "sample": f"{steps} accepted Dormand-Prince steps ({att} attempts) of "
-                                   f"the full cloud, FP64 oracle on {cores} threads"},
+                                   f"the full cloud after {len(hist_h)} settle and "
+                                   f"{args.warmup} warm-up steps, FP64 oracle on {cores} threads"},
         "e2e": {"value": value, "unit": "sim-us/wall-s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
