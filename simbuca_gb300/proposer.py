@@ -93,11 +93,14 @@ def collect(ctx: Context, w: configs.Workload, n_steps: int, precision=abi.SG_PR
 
 def run_controller(ctx: Context, w: configs.Workload, horizon: float, weights=None,
                    safety=0.9, precision=abi.SG_PREC_FP32C, state=None,
-                   max_attempts: int = 100000, controller_safety=None):
+                   max_attempts: int = 100000, controller_safety=None, beta: float = 0.0,
+                   log_cap: int = 0):
     """Advance one workload by `horizon` seconds (at most max_attempts attempts; `done`
-    tells whether the horizon was reached); returns the controller's counters."""
+    tells whether the horizon was reached); returns the controller's counters (and,
+    with log_cap > 0, the step log of cloud 0 under "log")."""
     allc = w.concat()
-    odes = [configs.ode(o.rtol, o.atol, o.h0, o.t0 + horizon, t0=o.t0) for o in w.odes]
+    odes = [configs.ode(o.rtol, o.atol, o.h0, o.t0 + horizon, t0=o.t0, beta=beta)
+            for o in w.odes]
     b = Batch(ctx, w.counts, w.fields, odes, precision)
     if state is None:
         b.upload(allc.pos, allc.vel, allc.mass, allc.charge)
@@ -107,19 +110,40 @@ def run_controller(ctx: Context, w: configs.Workload, horizon: float, weights=No
         b.set_proposer(weights, safety)
     elif controller_safety is not None:
         b.set_controller_safety(controller_safety)
+    if log_cap > 0:
+        b.set_log(log_cap)
     t0 = time.perf_counter()
     info, st = b.run(max_attempts=max_attempts, raise_on_error=False)
     wall = time.perf_counter() - t0
     s = info[0]
     sim_us = (s["t"] - w.odes[0].t0) * 1e6
     attempts = s["steps"] + s["rejects"]
-    return {"steps": s["steps"], "rejects": s["rejects"], "attempts": attempts,
-            "reject_fraction": s["rejects"] / max(attempts, 1),
-            "force_evals": s["force_evals"], "coulomb_evals": s["coulomb_evals"],
-            "force_evals_per_sim_us": s["force_evals"] / sim_us, "sim_us": sim_us,
-            "wall_s": wall, "sim_us_per_wall_s": sim_us / wall, "status": s["status"],
-            "done": s["done"],
-            "mean_h": sim_us * 1e-6 / max(s["steps"], 1)}
+    out = {"steps": s["steps"], "rejects": s["rejects"], "attempts": attempts,
+           "reject_fraction": s["rejects"] / max(attempts, 1),
+           "force_evals": s["force_evals"], "coulomb_evals": s["coulomb_evals"],
+           "force_evals_per_sim_us": s["force_evals"] / sim_us, "sim_us": sim_us,
+           "wall_s": wall, "sim_us_per_wall_s": sim_us / wall, "status": s["status"],
+           "done": s["done"],
+           "mean_h": sim_us * 1e-6 / max(s["steps"], 1)}
+    if log_cap > 0:
+        out["log"] = b.read_log(0)
+    return out
+
+
+def compare(ctx: Context, w: configs.Workload, horizon: float, betas, weights=None,
+            safety=DEFAULT_SAFETY, log_cap: int = 0, max_attempts: int = 1 << 40):
+    """The same workload and horizon under the reference's I-controller and PI
+    controllers (beta > 0), and with the learned proposer when weights are given."""
+    res = {}
+    for beta in betas:
+        tag = "i_controller" if beta == 0 else f"pi_beta_{beta}"
+        res[tag] = run_controller(ctx, w, horizon, beta=beta, log_cap=log_cap,
+                                  max_attempts=max_attempts)
+    if weights is not None:
+        res[f"mlp_safety_{safety}"] = run_controller(ctx, w, horizon, weights=weights,
+                                                     safety=safety, log_cap=log_cap,
+                                                     max_attempts=max_attempts)
+    return res
 
 
 def main():
@@ -135,9 +159,41 @@ def main():
                          "absolute log step size)")
     ap.add_argument("--max-attempts", type=int, default=100000,
                     help="attempt cap of each evaluation run")
+    ap.add_argument("--compare", action="store_true",
+                    help="no training: run the evaluation workload under the controllers "
+                         "of --betas (and the shipped proposer with --with-mlp), write "
+                         "compare.json and the step logs (compare_logs.npz) to --out")
+    ap.add_argument("--betas", default="0,0.04,0.08")
+    ap.add_argument("--with-mlp", action="store_true")
+    ap.add_argument("--seed", type=int, default=None,
+                    help="seed of the evaluation cloud (learned_4k only; default its own)")
+    ap.add_argument("--log-cap", type=int, default=0)
     a = ap.parse_args()
     ctx = Context(0)
     t0 = time.perf_counter()
+    if a.compare:
+        kw = {} if a.seed is None else {"seed": a.seed}
+        ev = (configs.learned_4k(sim_time=a.horizon, **kw) if a.eval == "learned_4k"
+              else configs.WORKLOADS[a.eval]())
+        res = compare(ctx, ev, a.horizon, [float(b) for b in a.betas.split(",")],
+                      weights=default_weights() if a.with_mlp else None,
+                      log_cap=a.log_cap, max_attempts=a.max_attempts)
+        logs = {}
+        for k, r in res.items():
+            lg = r.pop("log", None)
+            if lg is not None:
+                for name, arr in zip(("feat", "h_prev", "h", "err", "t"), lg):
+                    logs[f"{k}__{name}"] = arr
+        res["workload"] = a.eval
+        res["horizon_s"] = a.horizon
+        res["seed"] = a.seed
+        print(json.dumps(res, indent=1), flush=True)
+        with open(os.path.join(a.out, "compare.json"), "w") as f:
+            json.dump(res, f, indent=1)
+        if logs:
+            np.savez_compressed(os.path.join(a.out, "compare_logs.npz"), **logs)
+        ctx.close()
+        return
     X, y = [], []
     plan = [(configs.penning_1k(), 600 if a.quick else 2000),
             (configs.penning_65k(), 60 if a.quick else 300),
