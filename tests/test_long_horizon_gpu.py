@@ -1,0 +1,179 @@
+"""Cloud observables over the workloads' own horizons, FP32-compensated against FP64.
+
+Individual trajectories of an N-body cloud separate over thousands of steps whatever
+the arithmetic; what the FP32c form must keep is the cloud's statistics: the radial and
+axial temperatures (IonCloud::Temperature, bin/ioncloud.cpp:316-335) and the RMS size
+per axis (PrintCloud's spread, bin/ioncloud.cpp:148-183), computed on the device by
+the moments kernel (itself checked against the oracle in test_observables_gpu.py).
+
+* The 512-cloud frequency scan (clouds of 64 to 8,192 ions, quadrupole drive at
+  nu_c + Delta, Delta over +-5 Hz, 0.2 V, buffer gas 5e2 /s) over its full 100 us in one
+  FP32c batch, and 16 evenly spaced clouds of it in one FP64 batch: per cloud the
+  temperatures and RMS sizes agree, and the final radial temperature against Delta is
+  the scan's readout.
+* The 65,536-ion cloud (quadrupole drive at the mass-weighted nu_c, buffer gas 1e3 /s)
+  over 0.3 us from the same state in both forms; the FP32c sums on the FP64 run's end
+  state stay within the 1e-6 per-ion bound.
+
+These runs take about half an hour of a GB300 together (the FP64 runs dominate) and run
+only with SIMGB_LONG=1; SIMGB_LONG_OUT names a directory for a JSON record of every run:
+
+    SIMGB_LONG=1 SIMGB_LONG_OUT=out python -m pytest tests/test_long_horizon_gpu.py -m gpu -s
+"""
+import json
+import os
+import time
+
+import numpy as np
+import pytest
+
+from simbuca_gb300 import configs
+from simbuca_gb300.abi import SG_PREC_FP32C, SG_PREC_FP64
+from simbuca_gb300.api import Batch, Context
+from helpers import kq_of, rel_err_per_ion, summary
+
+pytestmark = [pytest.mark.gpu, pytest.mark.slow,
+              pytest.mark.skipif(os.environ.get("SIMGB_LONG") != "1",
+                                 reason="long-horizon runs: set SIMGB_LONG=1")]
+
+SCAN_SUBSET = np.linspace(0, 511, 16).round().astype(int)
+C2_T = 0.3e-6
+
+
+def record(name, data):
+    """Write a run's numbers to SIMGB_LONG_OUT/<name>.json as soon as they exist."""
+    out = os.environ.get("SIMGB_LONG_OUT")
+    print(name, json.dumps(data), flush=True)
+    if out:
+        os.makedirs(out, exist_ok=True)
+        with open(os.path.join(out, name + ".json"), "w") as f:
+            json.dump(data, f, indent=1)
+
+
+def run_batch(clouds, fields, odes, prec):
+    cx = Context(0)
+    try:
+        b = Batch(cx, [len(c.mass) for c in clouds], fields, odes, prec)
+        cat = configs.Workload("batch", clouds, fields, odes, 0.0).concat()
+        b.upload(cat.pos, cat.vel, cat.mass, cat.charge)
+        t0 = time.time()
+        info, st = b.run()
+        wall = time.time() - t0
+        assert st == 0
+        out = dict(info=info, moments=b.moments(), wall=wall,
+                   check=b.force_check() if prec == SG_PREC_FP32C else None)
+        out["pos"], out["vel"] = b.download()
+        return out
+    finally:
+        cx.close()
+
+
+def observables(m):
+    """T_r, T_z, RMS size x, y, z from the device moments."""
+    return np.stack([m[:, 9], m[:, 10], m[:, 3], m[:, 4], m[:, 5]], axis=1)
+
+
+def summarize(tag, r, counts):
+    return {"tag": tag, "wall_s": r["wall"], "counts": [int(n) for n in counts],
+            "t": [i["t"] for i in r["info"]], "steps": [i["steps"] for i in r["info"]],
+            "rejects": [i["rejects"] for i in r["info"]],
+            "observables_Tr_Tz_rmsxyz": observables(r["moments"]).tolist(),
+            "check": r["check"]}
+
+
+@pytest.fixture(scope="module")
+def scan32():
+    w = configs.scan_512()
+    f32 = run_batch(w.clouds, w.fields, w.odes, SG_PREC_FP32C)
+    sim_us = sum(i["t"] for i in f32["info"]) * 1e6
+    rec = summarize("scan_fp32c", f32, [len(c.mass) for c in w.clouds])
+    rec["summed_sim_us_per_wall_s"] = sim_us / f32["wall"]
+    record("scan_fp32c", rec)
+    return w, f32
+
+
+@pytest.fixture(scope="module")
+def scan64():
+    w = configs.scan_512()
+    sub = [int(k) for k in SCAN_SUBSET]
+    f64 = run_batch([w.clouds[k] for k in sub], [w.fields[k] for k in sub],
+                    [w.odes[k] for k in sub], SG_PREC_FP64)
+    rec = summarize("scan_fp64_subset", f64, [len(w.clouds[k].mass) for k in sub])
+    rec["clouds"] = sub
+    record("scan_fp64_subset", rec)
+    return f64
+
+
+def test_scan_runs_its_horizon(scan32):
+    w, f32 = scan32
+    for i in f32["info"]:
+        assert i["done"] == 1 and i["status"] == 0 and i["t"] >= 100e-6
+    chk = f32["check"]
+    worst = max(c["max_err"] for c in chk)
+    print("scan in-run check: checks", sum(c["checks"] for c in chk), "probes",
+          sum(c["probes"] for c in chk), "max err", worst, "breaches",
+          sum(c["breaches"] for c in chk))
+    assert worst <= 1e-6 and sum(c["breaches"] for c in chk) == 0
+
+
+def test_scan_readout_against_detuning(scan32):
+    """Final radial temperature against Delta: the scan's response.  A 100 us drive has
+    a Fourier width of ~10 kHz, so across +-5 Hz the response is expected flat up to the
+    clouds' own size-to-size spread; it is reported, and checked for that."""
+    w, f32 = scan32
+    tr = f32["moments"][:, 9]
+    counts = np.array([len(c.mass) for c in w.clouds])
+    delta = -5.0 + 10.0 * np.arange(len(w.clouds)) / (len(w.clouds) - 1)
+    bins = []
+    for lo, hi in ((-5, -2.5), (-2.5, 0), (0, 2.5), (2.5, 5.01)):
+        s = (delta >= lo) & (delta < hi)
+        bins.append({"delta_hz": [lo, hi], "mean_Tr_K": float(tr[s].mean()),
+                     "clouds": int(s.sum()), "mean_ions": float(counts[s].mean())})
+    slope = float(np.polyfit(delta, tr, 1)[0])
+    record("scan_readout", {"bins": bins, "slope_K_per_Hz": slope, "Tr_std_K": float(tr.std())})
+    assert np.isfinite(tr).all() and abs(slope) * 10.0 <= 3 * tr.std()
+
+
+def test_scan_fp32c_matches_fp64_subset(scan32, scan64):
+    w, f32 = scan32
+    a = observables(f32["moments"])[SCAN_SUBSET]
+    b = observables(scan64["moments"])
+    r = np.abs(a - b) / np.abs(b)
+    record("scan_compare", {"clouds": SCAN_SUBSET.tolist(), "rel_diff": r.tolist(),
+                            "max_rel_diff_Tr_Tz_rmsxyz": r.max(0).tolist()})
+    assert r[:, :2].max() <= 2e-3, r[:, :2].max(0)
+    assert r[:, 2:].max() <= 2e-3, r[:, 2:].max(0)
+
+
+@pytest.fixture(scope="module")
+def c2():
+    w = configs.penning_65k()
+    c = w.clouds[0]
+    op = w.odes[0]
+    odes = [configs.ode(op.rtol, op.atol, op.h0, C2_T)]
+    f32 = run_batch([c], w.fields, odes, SG_PREC_FP32C)
+    f64 = run_batch([c], w.fields, odes, SG_PREC_FP64)
+    record("c2_fp32c", summarize("c2_fp32c", f32, [len(c.mass)]))
+    record("c2_fp64", summarize("c2_fp64", f64, [len(c.mass)]))
+    return c, f32, f64
+
+
+def test_c2_observables_fp32c_vs_fp64(c2):
+    c, f32, f64 = c2
+    a, b = observables(f32["moments"])[0], observables(f64["moments"])[0]
+    r = np.abs(a - b) / np.abs(b)
+    record("c2_compare", {"fp32c": a.tolist(), "fp64": b.tolist(), "rel_diff": r.tolist()})
+    assert f32["info"][0]["t"] >= C2_T and f64["info"][0]["t"] >= C2_T
+    assert abs(f32["info"][0]["steps"] - f64["info"][0]["steps"]) <= f64["info"][0]["steps"] // 10
+    assert r.max() <= 1e-5, r
+
+
+def test_c2_bound_on_the_evolved_state(c2, ctx):
+    c, _, f64 = c2
+    q = c.charge.astype(np.float64)
+    kq = kq_of(c.mass, q)
+    a32 = ctx.coulomb_accel(f64["pos"], q, kq, SG_PREC_FP32C)
+    a64 = ctx.coulomb_accel(f64["pos"], q, kq, SG_PREC_FP64)
+    e = rel_err_per_ion(a32, a64)
+    record("c2_bound", summary(e))
+    assert e.max() <= 1e-6
