@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sequential", action="store_true",
+                    help="batched workloads: skip the one-cloud-at-a-time comparison pass")
     ap.add_argument("--variant", type=int, default=-1,
                     help="FP32c Coulomb launch shape (-1 automatic, 0..16 fixed: sg_set_coulomb_variant)")
     ap.add_argument("--method", type=int, default=5, choices=[4, 5],
@@ -223,6 +225,9 @@ def check_summary(records, every):
             "probes": int(sum(r["probes"] for r in records)),
             "breaches_above_1e-6": int(sum(r["breaches"] for r in records)),
             "max_err": max(r["max_err"] for r in records),
+            "max_err_far_near_random": [max(r["max_err_far"] for r in records),
+                                        max(r["max_err_near"] for r in records),
+                                        max(r["max_err_random"] for r in records)],
             "c_far_max": max(r["c_far"] for r in records),
             "kfar_min": min(r["kfar"] for r in records),
             "kfar_prior_min": min(r["kfar_prior"] for r in records),
@@ -322,7 +327,9 @@ def run_ours(args, dist: Dist):
     ctx.sync()
     kt = ctx.kernel_timing()
     st = ctx.stage_timing()
+    ft = ctx.fused_timing()
     ctx.set_kernel_timing(False)
+    fused_cluster = batch.fused()
     kt_total_ms = sum(kt_ms)
     kt_attempts = sum((a["steps"] + a["rejects"]) - (b["steps"] + b["rejects"])
                       for a, b in zip(info0(), k_before))
@@ -359,6 +366,12 @@ def run_ours(args, dist: Dist):
     bytes_state = 2 * w.n_total * 3 * 8
 
     # ---- roofline of the Coulomb kernel -----------------------------------
+    if fused_cluster:
+        # the fused small-cloud kernel: whole attempts (Coulomb sums and stages) per
+        # launch; achieved counts the Coulomb flops of the timing pass's attempts only
+        inter_pass = 6.0 * kt_attempts * sum(float(n) * (n - 1) for n in w.counts)
+        kt = {"coulomb_ms": ft["ms"], "coulomb_launches": ft["launches"],
+              "interactions": inter_pass}
     per_launch_inter = kt["interactions"] / max(kt["coulomb_launches"], 1)
     avg_launch_s = kt["coulomb_ms"] * 1e-3 / max(kt["coulomb_launches"], 1)
     achieved = FLOPS_PER_INTERACTION * per_launch_inter / avg_launch_s / 1e12
@@ -399,7 +412,8 @@ def run_ours(args, dist: Dist):
                    "settle_steps": settle_steps, "h_settled": snap[0]["h"],
                    "method": "dormand-prince" if args.method == 5 else "cash-karp",
                    "step_control": step_control,
-                   "coulomb_variant": batch.variant()},
+                   "coulomb_variant": batch.variant(),
+                   "fused_cluster": fused_cluster},
         "e2e": {"value": e2e_val, "unit": "sim-us/wall-s", "h2d_bytes_per_step": bytes_state,
                 "d2h_bytes_per_step": bytes_state, "ms_per_step": sum(e2e_ms) / args.steps,
                 "ms_upload_step_download": (parts / args.steps).tolist(),
@@ -410,8 +424,10 @@ def run_ours(args, dist: Dist):
         # FP32c on batches over 8,192 ions the 6 fix-up launches of the conditioning work
         # list (smaller batches fix up inside the reduction); per step one hold reset
         # (+2 per attempt with the proposer: cloud moments and the MLP)
-        "gpu_launches": int(attempts * ((27 if prec == abi.SG_PREC_FP32C and w.n_total > 8192
-                                         else 21) + (2 if args.proposer == "on" else 0))
+        # fused small-cloud path: one launch per step (its attempts inside it)
+        "gpu_launches": int((args.steps if fused_cluster else
+                             attempts * ((27 if prec == abi.SG_PREC_FP32C and w.n_total > 8192
+                                          else 21) + (2 if args.proposer == "on" else 0)))
                             + args.steps
                             + (3 * (attempts // CHECK_EVERY) if prec == abi.SG_PREC_FP32C else 0)),
         "fixup_ions_per_coulomb_call": fixups / max(1, 6 * attempts),
@@ -421,7 +437,9 @@ def run_ours(args, dist: Dist):
         "roofline": {"bound": "fp32" if prec == abi.SG_PREC_FP32C else "fp64",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
-                     "kernel": coulomb_kernel_name(prec, batch.variant()),
+                     "kernel": ("fused_attempts_kernel (cluster of %d CTAs per cloud; whole "
+                                "attempts, Coulomb flops counted)" % fused_cluster
+                                if fused_cluster else coulomb_kernel_name(prec, batch.variant())),
                      "flops_per_interaction": FLOPS_PER_INTERACTION,
                      "peak_source": "measured in-run by FMA issue probes (sg_probe_peaks)",
                      "coulomb_share_of_step": kt["coulomb_ms"] / kt_total_ms if kt_total_ms else None,
@@ -544,7 +562,7 @@ def run_batched(args, dist: Dist):
     # the same clouds one at a time, from the same settled state and step sizes
     seq_ms, seq_sim = 0.0, 0.0
     off = 0
-    for k, n in enumerate(w.counts):
+    for k, n in enumerate([] if args.no_sequential else w.counts):
         o = w.odes[k]
         op = mk_ode(o.rtol, o.atol, snap[k]["h"], o.t_end, t0=snap[k]["t"])
         b1 = Batch(ctx, [n], [w.fields[k]], [op], prec)
@@ -558,7 +576,7 @@ def run_batched(args, dist: Dist):
         seq_ms += ctx.timer_stop()
         seq_sim += (b1.info()[0]["t"] - i0[0]["t"]) * 1e6
         off += n
-    seq_value = seq_sim / (seq_ms * 1e-3)
+    seq_value = seq_sim / (seq_ms * 1e-3) if seq_ms else None
     out = {
         "metric": "summed sim-us/wall-s over the clouds of a batched frequency scan",
         "value": value, "unit": "sim-us/wall-s", "n_gpus": dist.world,
@@ -584,6 +602,7 @@ def run_batched(args, dist: Dist):
         "one_at_a_time": {"value": seq_value, "unit": "sim-us/wall-s",
                           "ms_total": seq_ms, "sim_us_total": seq_sim},
         "speedup_vs_one_at_a_time": value / seq_value if seq_value else None,
+        "coulomb_variant": batch.variant(),
         "clocks": clk,
     }
     ctx.close()

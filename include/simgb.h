@@ -255,6 +255,18 @@ int sg_mlp_train(sg_ctx* ctx, int n, const float* X, const float* Y, int iters, 
 /* Use the MLP (w != NULL) with step-size safety factor `safety` in (0, 1] for the
  * clouds of the batch, or the reference's controller (w == NULL). */
 int sg_batch_set_proposer(sg_ctx* ctx, const float* w, double safety);
+/* Small clouds (no counterpart in the reference): FP32c Dormand-Prince batches whose
+ * clouds are small, in the plain ion order and without a recorder, operations,
+ * dissociation, step log or proposer, run whole attempts in one launch, one thread-block
+ * cluster of up to 16 CTAs per cloud.  sg_set_fused(ctx, mode): 1 (default) for clouds
+ * of at most 512 ions, where it is faster than the tiled kernels; 2 for clouds of up to
+ * 2,048 ions; 0 never.  sg_batch_fused gives the cluster size
+ * the current batch runs with (0: the tiled kernels).  sg_fused_timing: CUDA-event time
+ * of the fused launches while sg_set_kernel_timing is on. */
+int sg_set_fused(sg_ctx* ctx, int on);
+int sg_batch_fused(sg_ctx* ctx, int* cluster);
+int sg_fused_timing(sg_ctx* ctx, double* ms, int64_t* launches);
+
 /* In-run check of the FP32c Coulomb sums (no counterpart in the reference).  Every
  * `every_attempts` attempts (default 16; 0 = off) the last Coulomb sum of the attempt
  * is checked, per cloud, at eight probe ions -- the two ions without fix-up whose far
@@ -273,6 +285,9 @@ typedef struct sg_check_info {
     int64_t checks;      /* checks made                                                   */
     int64_t probes;      /* probe ions evaluated                                          */
     int64_t breaches;    /* probes above 1e-6                                             */
+    double max_err_far;    /* largest error of the far-ranked probes                      */
+    double max_err_near;   /* ... of the near-ranked probes                               */
+    double max_err_random; /* ... of the random probes                                    */
 } sg_check_info;
 int sg_batch_set_force_check(sg_ctx* ctx, int every_attempts);
 int sg_batch_force_check(sg_ctx* ctx, sg_check_info* out);  /* out[n_clouds] */

@@ -77,7 +77,9 @@ class CheckInfo(ctypes.Structure):
     _fields_ = [("max_err", ctypes.c_double), ("last_err", ctypes.c_double),
                 ("c_far", ctypes.c_double), ("kfar", ctypes.c_double),
                 ("kfar_prior", ctypes.c_double), ("checks", ctypes.c_int64),
-                ("probes", ctypes.c_int64), ("breaches", ctypes.c_int64)]
+                ("probes", ctypes.c_int64), ("breaches", ctypes.c_int64),
+                ("max_err_far", ctypes.c_double), ("max_err_near", ctypes.c_double),
+                ("max_err_random", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -105,6 +107,7 @@ EXPORTED = [
     "sg_create", "sg_destroy", "sg_status_string", "sg_last_cuda_error", "sg_sync",
     "sg_version", "sg_coulomb_accel", "sg_force", "sg_coulomb_accel_noalloc", "sg_set_wait_test",
     "sg_batch_set_force_check", "sg_batch_force_check", "sg_batch_set_far_threshold",
+    "sg_set_fused", "sg_batch_fused", "sg_fused_timing",
     "sg_batch_create", "sg_batch_upload",
     "sg_batch_set_state", "sg_batch_download", "sg_batch_attempts", "sg_dp45_step",
     "sg_batch_run", "sg_batch_info", "sg_batch_set_field", "sg_batch_set_t_end",
@@ -148,6 +151,9 @@ def _declare(L):
     L.sg_batch_set_force_check.argtypes = [_vp, ctypes.c_int]
     L.sg_batch_force_check.argtypes = [_vp, ctypes.POINTER(CheckInfo)]
     L.sg_batch_set_far_threshold.argtypes = [_vp, ctypes.c_double]
+    L.sg_set_fused.argtypes = [_vp, ctypes.c_int]
+    L.sg_batch_fused.argtypes = [_vp, ctypes.POINTER(ctypes.c_int)]
+    L.sg_fused_timing.argtypes = [_vp, _dp, ctypes.POINTER(ctypes.c_int64)]
     L.sg_batch_create.argtypes = [_vp, ctypes.c_int, _ip, ctypes.POINTER(FieldParams),
                                   ctypes.POINTER(OdeParams), ctypes.c_int]
     L.sg_batch_upload.argtypes = [_vp, _dp, _dp, _dp, _ip]

@@ -148,6 +148,19 @@ class Context:
     def set_use_graph(self, on: bool):
         check(self._L.sg_set_use_graph(self._h, int(bool(on))), "sg_set_use_graph")
 
+    def set_fused(self, mode):
+        """Whole attempts of small clouds in one cluster launch: 1 (default, True) for
+        clouds of up to 512 ions, 2 up to 2,048 ions, 0 (False) never."""
+        check(self._L.sg_set_fused(self._h, int(mode)), "sg_set_fused")
+
+    def fused_timing(self):
+        """(ms, launches) of the fused launches timed while kernel timing is on."""
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        check(self._L.sg_fused_timing(self._h, ctypes.byref(ms), ctypes.byref(n)),
+              "sg_fused_timing")
+        return {"ms": ms.value, "launches": n.value}
+
     def set_wait_test(self, tile: int, limit_us: int = 1000):
         """Make the FP32c Coulomb kernels of the current batch give up a bounded wait at
         j-tile `tile` after limit_us (tile < 0: off); see sg_set_wait_test."""
@@ -206,6 +219,13 @@ class Batch:
     def attempts(self, n: int):
         self._live()
         check(self._L.sg_batch_attempts(self.ctx.handle, int(n)), "sg_batch_attempts")
+
+    def fused(self) -> int:
+        """Cluster size of the fused small-cloud path this batch runs with (0: tiled)."""
+        self._live()
+        v = ctypes.c_int()
+        check(self._L.sg_batch_fused(self.ctx.handle, ctypes.byref(v)), "sg_batch_fused")
+        return v.value
 
     def set_force_check(self, every_attempts: int):
         """In-run check of the FP32c sums every `every_attempts` attempts (0: off)."""

@@ -16,7 +16,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 OUT = os.path.join(PKG, "libsimgb.so")
-UNITS = ["coulomb.cu", "dp45.cu", "capi.cu", "aux_kernels.cu", "noalloc.cu", "check.cu",
+UNITS = ["coulomb.cu", "dp45.cu", "capi.cu", "aux_kernels.cu", "noalloc.cu", "check.cu", "fused.cu",
          "proposer.cu", "cloud_io.cu", "observe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
@@ -38,7 +38,8 @@ def _stale(out: str, deps: list[str]) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, "sg_internal.cuh"),
+    headers = [os.path.join(CSRC, "sg_internal.cuh"), os.path.join(CSRC, "fp32c_math.cuh"),
+               os.path.join(CSRC, "dp_tableau.cuh"),
                os.path.join(os.path.dirname(PKG), "include", "simgb.h")]
     procs, objs = [], []
     for u in UNITS:

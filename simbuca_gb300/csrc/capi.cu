@@ -88,11 +88,16 @@ struct Problem {
     int check_every = 16;
     long long attempt_count = 0;
     double kfar_prior = 0.0;  // > 0: the far fix-up threshold's prior of every cloud
+    // fused small-cloud attempts (fused.cu)
+    double* errp = nullptr;   // [clouds][SG_FUSED_MAX_CTAS]
+    int fused_cluster = -1;   // cluster size for this batch (0: not launchable), -1 unknown
+    int max_npad = 0;         // largest padded cloud
 };
 
 struct TimedLaunch {
     cudaEvent_t a, b;
     double inter;
+    int fused;  // a fused-attempts launch (else a Coulomb pair kernel)
 };
 
 }  // namespace
@@ -119,6 +124,9 @@ struct sg_ctx {
     std::vector<cudaEvent_t> free_ev;
     double coul_ms = 0.0, coul_inter = 0.0;
     long long coul_launches = 0;
+    double fused_ms = 0.0;
+    long long fused_launches = 0;
+    int use_fused = 1;  // 0 off, 1 clouds up to SG_FUSED_AUTO_IONS, 2 up to SG_FUSED_MAX_IONS
     bool use_graph = true;
     cudaGraphExec_t graph = nullptr;
     // timed graph: the same attempt with an event pair around each Coulomb launch
@@ -200,6 +208,7 @@ void free_problem(Problem& P) {
     cudaFree(P.risk);
     cudaFree(P.ran);
     cudaFree(P.dchk);
+    cudaFree(P.errp);
     if (P.hctrl) cudaFreeHost(P.hctrl);
     P = Problem();
 }
@@ -448,6 +457,9 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(dalloc(&P.stage, 6 * N));
     CK(dalloc(&P.flags, SG_NFLAGS));
     CK(cudaMemset(P.flags, 0, SG_NFLAGS * sizeof(int)));
+    CK(dalloc(&P.errp, (size_t)std::max(P.n_clouds, 1) * SG_FUSED_MAX_CTAS));
+    P.max_npad = 0;
+    for (int c = 0; c < P.n_clouds; c++) P.max_npad = std::max(P.max_npad, P.hc[c].npad);
     if (P.precision == SG_PREC_FP32C) {
         CK(dalloc(&P.risk, 2 * N));
         CK(dalloc(&P.ran, (size_t)std::max(P.n_clouds, 1)));
@@ -640,9 +652,14 @@ void flush_timing(sg_ctx* ctx) {
     for (auto& tl : ctx->pending) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, tl.a, tl.b) == cudaSuccess) {
-            ctx->coul_ms += ms;
-            ctx->coul_launches += 1;
-            ctx->coul_inter += tl.inter;
+            if (tl.fused) {
+                ctx->fused_ms += ms;
+                ctx->fused_launches += 1;
+            } else {
+                ctx->coul_ms += ms;
+                ctx->coul_launches += 1;
+                ctx->coul_inter += tl.inter;
+            }
         }
         ctx->free_ev.push_back(tl.a);
         ctx->free_ev.push_back(tl.b);
@@ -684,7 +701,7 @@ int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter, double
             ca.ran = P.ran;
         }
     }
-    TimedLaunch tl{nullptr, nullptr, inter};
+    TimedLaunch tl{nullptr, nullptr, inter, 0};
     const int cap = ctx->capture_events;
     if (cap >= 0) {
         // external event nodes: recorded by each replay and readable from the host
@@ -836,15 +853,76 @@ int capture_attempt(sg_ctx* ctx, Problem& P, bool timed, cudaGraphExec_t* out) {
 
 // The in-run force check (check.cu) after an attempt, every check_every attempts of an
 // FP32c batch; its launches are not part of the attempt graph.
-int maybe_check(sg_ctx* ctx, Problem& P) {
+int maybe_check(sg_ctx* ctx, Problem& P, int attempts = 1) {
     if (!P.dchk || P.check_every <= 0 || !P.any_coulomb) return SG_OK;
-    if (++P.attempt_count % P.check_every != 0) return SG_OK;
+    const long long before = P.attempt_count;
+    P.attempt_count += attempts;
+    if (P.attempt_count / P.check_every == before / P.check_every) return SG_OK;
     CK(sg_force_check(P.dc, P.n_clouds, P.ran, P.risk, P.c64, P.npad, P.coulS, P.n, P.dchk,
                       ctx->stream));
     return SG_OK;
 }
 
+// The fused small-cloud path (fused.cu) applies to FP32c Dormand-Prince batches of
+// clouds of at most SG_FUSED_AUTO_IONS ions (SG_FUSED_MAX_IONS when forced) in the plain
+// ion order, without a recorder,
+// operations, dissociation, step log or proposer, when the device can launch a cluster
+// with at most SG_FUSED_THREADS ions per CTA.
+bool fused_eligible(sg_ctx* ctx, Problem& P) {
+    if (!ctx->use_fused || P.precision != SG_PREC_FP32C || P.method != 5 || P.sorted ||
+        P.rec_cap > 0 || !P.hops.empty() || P.n_dis > 0 || P.use_mlp || P.log_cap > 0 ||
+        P.n_clouds == 0)
+        return false;
+    int big = 0;
+    const int limit = ctx->use_fused == 2 ? SG_FUSED_MAX_IONS : SG_FUSED_AUTO_IONS;
+    for (int c = 0; c < P.n_clouds; c++) {
+        if (P.hc[c].n < 1 || P.hc[c].n > limit) return false;
+        big = std::max(big, P.hc[c].n);
+    }
+    if (P.fused_cluster < 0) P.fused_cluster = sg_fused_cluster_size(P.max_npad);
+    return P.fused_cluster > 0 && big <= P.fused_cluster * SG_FUSED_THREADS;
+}
+
+// n attempts of every active cloud at most (a cloud stops early once done or held);
+// `counted`: attempts counted towards the in-run check's interval.
+int run_fused(sg_ctx* ctx, Problem& P, int n, int counted) {
+    SgFusedArgs f;
+    f.clouds = P.dc;
+    f.ctrl = P.dctrl;
+    f.y = P.y;
+    f.ys = P.ys;
+    f.k = P.k;
+    f.coul1 = P.coul1;
+    f.coul7 = P.coul7;
+    f.coulS = P.coulS;
+    f.kq = P.kq;
+    f.qm = P.qm;
+    f.c64 = P.c64;
+    f.c32 = P.c32;
+    f.errp = P.errp;
+    f.flags = P.flags;
+    f.risk = P.risk;
+    f.ran = P.ran;
+    f.n = P.n;
+    f.npad = P.npad;
+    f.n_clouds = P.n_clouds;
+    f.max_attempts = n;
+    TimedLaunch tl{nullptr, nullptr, 0.0, 1};
+    if (ctx->timing) {
+        tl.a = take_event(ctx);
+        tl.b = take_event(ctx);
+        CK(cudaEventRecord(tl.a, ctx->stream));
+    }
+    CK(sg_fused_attempts(f, P.fused_cluster, P.max_npad, ctx->stream));
+    if (ctx->timing) {
+        CK(cudaEventRecord(tl.b, ctx->stream));
+        ctx->pending.push_back(tl);
+    }
+    return maybe_check(ctx, P, counted);
+}
+
 int run_attempts(sg_ctx* ctx, Problem& P, int n) {
+    if (fused_eligible(ctx, P)) return run_fused(ctx, P, n, n);
     if (ctx->use_graph && ctx->timing) {
         // graph replays one at a time, reading the Coulomb event pairs after each
         if (!ctx->graph_timed) {
@@ -1383,9 +1461,11 @@ int sg_dp45_step(sg_ctx* ctx, sg_step_info* info) {
     // hold-on-accept on (any nonzero word) without a host-to-device copy
     CK(cudaMemsetAsync(P.flags + 1, 1, sizeof(int), ctx->stream));
     int st = SG_OK;
-    // every cloud that is active now takes exactly one accepted step (or fails)
+    // every cloud that is active now takes exactly one accepted step (or fails); the
+    // fused path loops over a cloud's attempts inside one launch until it holds
+    const bool fused = fused_eligible(ctx, P);
     for (long long guard = 0; guard < (1ll << 40); guard++) {
-        st = run_attempts(ctx, P, 1);
+        st = fused ? run_fused(ctx, P, 64, 1) : run_attempts(ctx, P, 1);
         if (st != SG_OK) break;
         st = sync_ctrl(ctx, P);
         if (st != SG_OK) break;
@@ -1766,6 +1846,8 @@ int sg_set_kernel_timing(sg_ctx* ctx, int on) {
     ctx->coul_launches = 0;
     ctx->stage_ms = 0.0;
     ctx->stage_launches = 0;
+    ctx->fused_ms = 0.0;
+    ctx->fused_launches = 0;
     return SG_OK;
 }
 
@@ -1812,6 +1894,32 @@ int sg_batch_variant(sg_ctx* ctx, int* variant) {
     if (!ctx || !variant) return SG_BAD_ARG;
     if (ctx->batch.n_clouds == 0) return SG_NOT_READY;
     *variant = ctx->batch.precision == SG_PREC_FP32C ? ctx->batch.variant : 0;
+    return SG_OK;
+}
+
+int sg_set_fused(sg_ctx* ctx, int on) {
+    if (!ctx) return SG_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (on < 0 || on > 2) return SG_BAD_ARG;
+    ctx->use_fused = on;
+    return SG_OK;
+}
+
+int sg_fused_timing(sg_ctx* ctx, double* ms, int64_t* launches) {
+    if (!ctx) return SG_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    flush_timing(ctx);
+    if (ms) *ms = ctx->fused_ms;
+    if (launches) *launches = ctx->fused_launches;
+    return SG_OK;
+}
+
+int sg_batch_fused(sg_ctx* ctx, int* cluster) {
+    if (!ctx || !cluster) return SG_BAD_ARG;
+    Problem& P = ctx->batch;
+    if (P.n_clouds == 0) return SG_NOT_READY;
+    CK(cudaSetDevice(ctx->device));
+    *cluster = fused_eligible(ctx, P) ? P.fused_cluster : 0;
     return SG_OK;
 }
 
@@ -2084,6 +2192,9 @@ int sg_batch_force_check(sg_ctx* ctx, sg_check_info* out) {
         o.checks = h[c].checks;
         o.probes = h[c].probes;
         o.breaches = h[c].breaches;
+        o.max_err_far = h[c].max_kind[0];
+        o.max_err_near = h[c].max_kind[1];
+        o.max_err_random = h[c].max_kind[2];
     }
     return SG_OK;
 }

@@ -177,6 +177,8 @@ __global__ void check_update_kernel(int* __restrict__ ran, SgCheck* __restrict__
     for (int k = 0; k < SG_CHECK_PROBES; k++) {
         last = fmax(last, h.err[k]);
         br += h.err[k] > kBound ? 1 : 0;
+        const int kind = k < 2 ? 0 : (k < kRanked ? 1 : 2);
+        h.max_kind[kind] = fmax(h.max_kind[kind], h.err[k]);
     }
     for (int k = 0; k < 2; k++)
         if (h.rf[k] > kFarRatioMin) h.c_far = fmax(h.c_far, h.err[k] / (double)h.rf[k]);

@@ -24,6 +24,7 @@
 // 1/sqrt(1-e) = 1 + e/2 + 3e^2/8 (e = 1 - r^2 y0^2), accurate to ~1 ulp.
 #include <stdio.h>
 
+#include "fp32c_math.cuh"
 #include "sg_internal.cuh"
 
 namespace {
@@ -88,84 +89,6 @@ __device__ __forceinline__ void fence_proxy_async() {
 __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
-__device__ __forceinline__ float rsqrt_approx(float x) {
-    float y;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-// packed FP32x2 (two floats in one 64-bit register pair)
-typedef unsigned long long f2;
-__device__ __forceinline__ f2 pk(float a, float b) {
-    f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void upk(f2 v, float& a, float& b) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-}
-__device__ __forceinline__ f2 add2(f2 a, f2 b) {
-    f2 d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
-    f2 d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
-    f2 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
-    f2 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-
-// Softening added to r^2 in frame units (u ~ 1): below the rounding of any real
-// pair distance, it keeps the self pair (dx = 0) finite: 1/r^3 = 1e36 < FLT_MAX.
-constexpr float kTiny = 1e-24f;
-
-// One FP32c pair term, scalar form.  Written with explicit rounding intrinsics so the
-// close-pair re-evaluation reproduces it bit for bit.
-struct PairF {
-    float dx, dy, dz, y3;
-};
-__device__ __forceinline__ PairF pair_f32(float xjh, float yjh, float zjh, float xjl, float yjl,
-                                          float zjl, float xih, float yih, float zih, float xil,
-                                          float yil, float zil) {
-    PairF p;
-    p.dx = __fadd_rn(__fsub_rn(xjh, xih), __fsub_rn(xjl, xil));
-    p.dy = __fadd_rn(__fsub_rn(yjh, yih), __fsub_rn(yjl, yil));
-    p.dz = __fadd_rn(__fsub_rn(zjh, zih), __fsub_rn(zjl, zil));
-    float r2 = __fmaf_rn(p.dx, p.dx, kTiny);
-    r2 = __fmaf_rn(p.dy, p.dy, r2);
-    r2 = __fmaf_rn(p.dz, p.dz, r2);
-    const float y = rsqrt_approx(r2);
-    p.y3 = __fmul_rn(__fmul_rn(y, y), y);
-    return p;
-}
-
-__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
-    const float y = __fsub_rn(x, c);
-    const float t = __fadd_rn(s, y);
-    c = __fsub_rn(__fsub_rn(t, s), y);
-    s = t;
-}
-
-
-__device__ __forceinline__ double rsqrt_fp64(double r2) {
-    // FP32 SFU seed, then y = y0 (1 + e/2 + 3 e^2/8), e = 1 - r2 y0^2 (binomial series of
-    // (1-e)^(-1/2)); the truncation error is ~(5/16) e^3 with |e| < 2^-22.
-    const double y0 = (double)rsqrt_approx(__double2float_rn(r2));
-    const double e = fma(-r2 * y0, y0, 1.0);
-    const double p = fma(e, 0.375, 0.5);
-    return fma(y0 * e, p, y0);
-}
-
 // Close pairs of one flagged ion against one shared-memory tile, evaluated by the
 // whole warp (lanes stride over the tile): pairs whose FP32 1/r^3 exceeded wc get their
 // exact FP64 term, minus the capped FP32 term the main loop already summed (a product
@@ -380,10 +303,11 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
         corr[1][li] = 0.0;
         corr[2][li] = 0.0;
     }
-    float ks[IPT][3], kc[IPT][3], s2[IPT];
+    float ks[IPT][3], kc[IPT][3], s2[IPT], fmx[IPT];
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
         s2[k] = 0.f;
+        fmx[k] = 0.f;
 #pragma unroll
         for (int c = 0; c < 3; c++) ks[k][c] = kc[k][c] = 0.f;
     }
@@ -479,6 +403,11 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
                 s2[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2[k])));
             }
         }
+        // the strongest single pair so far (conditioning estimate), from tiles without a
+        // close pair: those are evaluated exactly below, the fix-up cannot improve them
+#pragma unroll
+        for (int k = 0; k < IPT; k++)
+            if (y3max[k] <= wc) fmx[k] = fmaxf(fmx[k], y3max[k]);
         // close pairs of this tile, one flagged ion at a time by the whole warp
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
@@ -529,7 +458,7 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
         if (ipad[k] < 0) continue;
         const int li = tid + k * NT;
         const int ig = ipad[k];
-        P[3 * (size_t)npad_total + ig] = (double)s2[k] * (qscale * qscale);
+        P[3 * (size_t)npad_total + ig] = (double)conditioning_s2(s2[k], fmx[k]) * (qscale * qscale);
         P[4 * (size_t)npad_total + ig] = 0.0;  // no far tiles in this form
         // P_i = sum q_j (x_i - x_j)/r^3 = -invL^2 qscale sum w (u_j - u_i) + close-pair
         // terms, w carrying the charges q_j / qscale
@@ -621,11 +550,12 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         corr[1][li] = 0.0;
         corr[2][li] = 0.0;
     }
-    float ks[IPT][3], kc[IPT][3], s2[IPT], s2f[IPT];
+    float ks[IPT][3], kc[IPT][3], s2[IPT], s2f[IPT], fmx[IPT];
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
         s2[k] = 0.f;
         s2f[k] = 0.f;
+        fmx[k] = 0.f;
 #pragma unroll
         for (int c = 0; c < 3; c++) ks[k][c] = kc[k][c] = 0.f;
     }
@@ -733,6 +663,11 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
                 fold_partials<IPT, S2F>(ax, ay, az, ks, kc, s2, s2f, !far);
             }
         }
+        // the strongest single pair so far (conditioning estimate), from tiles without a
+        // close pair: those are evaluated exactly below, the fix-up cannot improve them
+#pragma unroll
+        for (int k = 0; k < IPT; k++)
+            if (y3max[k] <= wc) fmx[k] = fmaxf(fmx[k], y3max[k]);
         // close pairs of this tile, one flagged ion at a time by the whole warp
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
@@ -783,7 +718,7 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
         if (ipad[k] < 0) continue;
         const int li = IPT * tid + k;
         const int ig = ipad[k];
-        P[3 * (size_t)npad_total + ig] = (double)s2[k] * (qscale * qscale);
+        P[3 * (size_t)npad_total + ig] = (double)conditioning_s2(s2[k], fmx[k]) * (qscale * qscale);
         if (S2F) P[4 * (size_t)npad_total + ig] = (double)s2f[k] * (qscale * qscale);
         // P_i = sum q_j (x_i - x_j)/r^3 = -invL^2 qscale sum w (u_j - u_i) + close-pair
         // terms, w carrying the charges q_j / qscale

@@ -15,30 +15,10 @@
 // The force count still follows the reference (7 per attempt, bin/ode.cpp:101-175).
 #include <math.h>
 
+#include "dp_tableau.cuh"
 #include "sg_internal.cuh"
 
 namespace {
-
-// Tableau of bin/ode.cpp:76-86.
-__constant__ double c_a[8][7] = {
-    {0, 0, 0, 0, 0, 0, 0},
-    {0, 0, 0, 0, 0, 0, 0},
-    {1.0 / 5.0, 0, 0, 0, 0, 0, 0},
-    {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0, 0, 0},
-    {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0, 0, 0, 0, 0},
-    {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0, 0, 0, 0},
-    {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0, 0, 0},
-    {35.0 / 384.0, 0.0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0, 0}};
-__constant__ double c_c[8] = {0, 0.0, 1.0 / 5.0, 3.0 / 10.0, 4.0 / 5.0, 8.0 / 9.0, 1.0, 1.0};
-// e = b - b* (bin/ode.cpp:85-86); index by stage 1..7
-__constant__ double c_e[8] = {0,
-                              71.0 / 57600.0,
-                              0.0,
-                              -71.0 / 16695.0,
-                              71.0 / 1920.0,
-                              -17253.0 / 339200.0,
-                              22.0 / 525.0,
-                              -1.0 / 40.0};
 
 typedef SgDpArgs DpArgs;
 
@@ -444,44 +424,9 @@ __global__ void dp_control_kernel(SgCloud* __restrict__ clouds, SgCtrl* __restri
         cs.status = flags[SG_FLAG_ERR];
         cs.done = 1;
         accepted = 0;
-    } else if (!isfinite(err)) {
-        cs.status = SG_NONFINITE;
-        cs.done = 1;
-        accepted = 0;
-    } else if (cs.adaptive && cs.method != 1) {  // step() turns control off for Gear
-        // beta = 0: the reference's I-controller, pow(errold, 0) = 1 exactly
-        const double beta = cs.beta, alpha = 0.2 - beta * 0.75, safe = 0.9, minscale = 0.2,
-                     maxscale = 10.0;
-        if (err <= 1.0) {
-            double scale;
-            if (err == 0.0)
-                scale = maxscale;
-            else {
-                scale = safe * pow(err, -alpha) * pow(cs.errold, beta);
-                if (scale < minscale) scale = minscale;
-                if (scale > maxscale) scale = maxscale;
-            }
-            cs.hnext = cs.reject ? cs.h * ((1.0 < scale) ? 1.0 : scale) : cs.h * scale;
-            cs.errold = (err < 1.0e-4) ? 1.0e-4 : err;
-            cs.reject = 0;
-        } else {
-            double scale = safe * pow(err, -alpha);
-            scale = (scale < minscale) ? minscale : scale;
-            cs.h *= scale;
-            cs.reject = 1;
-            accepted = 0;
-            cs.rejects++;
-            cs.rejects_here++;
-            // IonCloud::pos[0][0] (bin/ode.cpp:482): x of the caller's first ion
-            const double x0 = fabs(y[cl.ion0]);
-            if (fabs(cs.h) <= x0 * 2.220446049250313e-16) {
-                cs.status = SG_H_UNDERFLOW;
-                cs.done = 1;
-            } else if (cs.max_rejects > 0 && cs.rejects_here >= cs.max_rejects) {
-                cs.status = SG_TOO_MANY_REJECTS;
-                cs.done = 1;
-            }
-        }
+    } else {
+        // IonCloud::pos[0][0] (bin/ode.cpp:482): x of the caller's first ion
+        accepted = sg_error_succes(cs, err, y + cl.ion0);
     }
     if (accepted) {
         cs.h_last = cs.h;

@@ -151,6 +151,51 @@ struct SgCtrl {
     double beta;  // PI term of error_succes (0: the reference's I-controller)
 };
 
+// error_succes and the retry bookkeeping of step() (bin/ode.cpp:426-494) for one attempt
+// of one cloud with error norm err: returns 1 if the attempt is accepted.  A non-finite
+// norm stops the cloud (SG_NONFINITE); a reject shrinks h and checks the underflow
+// |h| <= |pos[0][0]| eps against *x0 (the caller's first ion) and the reject budget.
+// Gear (method 1) and fixed-step runs accept every attempt.  beta = 0 is the
+// reference's I-controller: pow(errold, 0) = 1 exactly.
+__device__ inline int sg_error_succes(SgCtrl& cs, double err, const double* x0) {
+    if (!isfinite(err)) {
+        cs.status = SG_NONFINITE;
+        cs.done = 1;
+        return 0;
+    }
+    if (!cs.adaptive || cs.method == 1) return 1;  // step() turns control off for Gear
+    const double beta = cs.beta, alpha = 0.2 - beta * 0.75, safe = 0.9, minscale = 0.2,
+                 maxscale = 10.0;
+    if (err <= 1.0) {
+        double scale;
+        if (err == 0.0)
+            scale = maxscale;
+        else {
+            scale = safe * pow(err, -alpha) * pow(cs.errold, beta);
+            if (scale < minscale) scale = minscale;
+            if (scale > maxscale) scale = maxscale;
+        }
+        cs.hnext = cs.reject ? cs.h * ((1.0 < scale) ? 1.0 : scale) : cs.h * scale;
+        cs.errold = (err < 1.0e-4) ? 1.0e-4 : err;
+        cs.reject = 0;
+        return 1;
+    }
+    double scale = safe * pow(err, -alpha);
+    scale = (scale < minscale) ? minscale : scale;
+    cs.h *= scale;
+    cs.reject = 1;
+    cs.rejects++;
+    cs.rejects_here++;
+    if (fabs(cs.h) <= fabs(*x0) * 2.220446049250313e-16) {
+        cs.status = SG_H_UNDERFLOW;
+        cs.done = 1;
+    } else if (cs.max_rejects > 0 && cs.rejects_here >= cs.max_rejects) {
+        cs.status = SG_TOO_MANY_REJECTS;
+        cs.done = 1;
+    }
+    return 0;
+}
+
 // One operation of the sequence (sg_operation plus the row of its dissociation table).
 struct SgOp {
     int32_t kind, print_after;
@@ -334,6 +379,36 @@ struct SgDpArgs {
     int fp32c;            // write the FP32 frame coordinates
 };
 
+// ---- fused small-cloud attempts (fused.cu) -----------------------------------------
+// One thread-block cluster per cloud runs whole Dormand-Prince attempts (FP32c, no
+// recorder, operations or proposer) for clouds of at most SG_FUSED_MAX_IONS ions, and
+// at most SG_FUSED_THREADS ions per CTA of the cluster.
+#define SG_FUSED_THREADS 512
+#define SG_FUSED_MAX_CTAS 16
+#define SG_FUSED_MAX_IONS 2048
+// Clouds the fused path takes by default (sg_set_fused mode 1): measured on GB300 it
+// needs ~180 us per attempt at 256 ions against ~245 us for the tiled kernels, breaks
+// even near 1,000 ions and loses beyond; mode 2 takes it up to SG_FUSED_MAX_IONS.
+#define SG_FUSED_AUTO_IONS 512
+struct SgFusedArgs {
+    const SgCloud* clouds;
+    SgCtrl* ctrl;
+    double *y, *ys, *k, *coul1, *coul7, *coulS;
+    const double *kq, *qm;
+    double* c64;
+    float* c32;
+    double* errp;    // [clouds][SG_FUSED_MAX_CTAS] error partials of an attempt
+    int* flags;      // the context's flag words (error word, hold on accept)
+    float* risk;     // in-run force check inputs (null: not written)
+    int* ran;
+    int n, npad, n_clouds;
+    int max_attempts;  // attempts per launch at most
+};
+// The cluster size the fused kernel can be launched with on this device for clouds of
+// up to max_npad padded ions (16, 8 or 4), or 0 if none.
+int sg_fused_cluster_size(int max_npad);
+cudaError_t sg_fused_attempts(const SgFusedArgs& f, int cluster, int max_npad, cudaStream_t st);
+
 // ---- device-side observables (observe.cu) -------------------------------------------
 // A record of a cloud: [0] t, then per species s < n_species the PrintCloud statistics
 // (bin/ioncloud.cpp:148-183) x0 y0 z0 x1 y1 z1 (m) energy (eV) n_s n, then the state
@@ -437,6 +512,7 @@ struct SgCheck {
     double max_err;    // largest per-ion relative error over every check
     double last_err;   // largest of the last check
     double c_far;      // largest err / (sqrt(s2f)/|P|) of the far-ranked probes
+    double max_kind[3];  // largest error of the far-ranked, near-ranked, random probes
     long long checks, probes, breaches;  // breaches: probes above 1e-6
     float kfar2;       // measured far fix-up threshold (kfar^2); +inf until measured
     int32_t pad;

@@ -386,10 +386,11 @@ def test_reference_mirror_step_and_force(ctx):
 
 
 def test_kernel_timing_in_graph_and_direct(ctx):
-    """Coulomb launches are timed with CUDA events both inside the attempt graph and with
-    direct launches; both count 6 Coulomb sums per attempt."""
+    """Coulomb launches of the tiled path are timed with CUDA events both inside the
+    attempt graph and with direct launches; both count 6 Coulomb sums per attempt."""
     w = configs.penning_1k(n=700, seed=8)
     c = w.clouds[0]
+    ctx.set_fused(False)
     for graph in (True, False):
         ctx.set_use_graph(graph)
         b = one_cloud(ctx, c.pos, c.vel, c.mass, c.charge, configs.penning_field(), 1e-9, 1e-15,
@@ -405,6 +406,7 @@ def test_kernel_timing_in_graph_and_direct(ctx):
         assert kt["coulomb_launches"] == 6 * attempts
         assert kt["coulomb_ms"] > 0 and kt["interactions"] == 6 * attempts * 700 * 699
     ctx.set_use_graph(True)
+    ctx.set_fused(True)
 
 
 @pytest.mark.parametrize("method,coul,stages", [(5, 6, 9), (4, 6, 9), (1, 1, 4)])
@@ -414,16 +416,20 @@ def test_kernel_timing_counts(ctx, method, coul, stages):
     w = configs.penning_1k(n=600, seed=31)
     c = w.clouds[0]
     fp = configs.penning_field(delta=1e3)
-    b = one_cloud(ctx, c.pos, c.vel, c.mass, c.charge, fp, 1e-9, 1e-15, 2e-9, 1.0,
-                  SG_PREC_FP32C, adaptive=(method != 1), method=method)
-    b.attempts(2)
-    ctx.set_kernel_timing(True)
+    ctx.set_fused(False)  # the tiled path's launches
     try:
-        b.attempts(5)
-        kt = ctx.kernel_timing()
-        st = ctx.stage_timing()
+        b = one_cloud(ctx, c.pos, c.vel, c.mass, c.charge, fp, 1e-9, 1e-15, 2e-9, 1.0,
+                      SG_PREC_FP32C, adaptive=(method != 1), method=method)
+        b.attempts(2)
+        ctx.set_kernel_timing(True)
+        try:
+            b.attempts(5)
+            kt = ctx.kernel_timing()
+            st = ctx.stage_timing()
+        finally:
+            ctx.set_kernel_timing(False)
     finally:
-        ctx.set_kernel_timing(False)
+        ctx.set_fused(True)
     assert kt["coulomb_launches"] == 5 * coul and kt["coulomb_ms"] > 0
     assert kt["interactions"] == pytest.approx(5 * coul * 600 * 599)
     assert st["stage_launches"] == 5 * stages and st["stage_ms"] > 0

@@ -142,8 +142,12 @@ def test_controller_safety_mode(ctx):
     """The ablation mode: the reference's rule with its own safety factor 0.9 reproduces
     the reference controller's run exactly; a smaller factor takes smaller steps."""
     ev = configs.learned_4k(n=512, seed=13, sim_time=1e-6)
-    ref = proposer.run_controller(ctx, ev, 1e-6)
-    same = proposer.run_controller(ctx, ev, 1e-6, controller_safety=0.9)
+    ctx.set_fused(False)  # the ablation runs through the proposer kernel: tiled path for both
+    try:
+        ref = proposer.run_controller(ctx, ev, 1e-6)
+        same = proposer.run_controller(ctx, ev, 1e-6, controller_safety=0.9)
+    finally:
+        ctx.set_fused(True)
     for k in ("steps", "rejects", "force_evals", "sim_us"):
         assert same[k] == ref[k], k
     low = proposer.run_controller(ctx, ev, 1e-6, controller_safety=0.7)

@@ -23,6 +23,7 @@ def test_ring_wait_times_out_and_context_recovers(ctx, variant):
     c = configs.penning_1k(n=4096, seed=5).clouds[0]
     fp = configs.penning_field(quad=(0.5, configs.nu_c(132.905), 0.0, 0.0, 1.0), delta=1e3)
     ctx.set_coulomb_variant(variant)  # -1: automatic (plain shape here), 9: k-d ordered
+    ctx.set_fused(False)              # the tiled kernels, whose copy ring is under test
     try:
         b = Batch(ctx, [len(c.mass)], [fp], [configs.ode(1e-9, 1e-15, 1e-9, 1e-6)],
                   SG_PREC_FP32C)
@@ -50,3 +51,4 @@ def test_ring_wait_times_out_and_context_recovers(ctx, variant):
         assert np.array_equal(p, ref_p) and np.array_equal(v, ref_v)
     finally:
         ctx.set_coulomb_variant(-1)
+        ctx.set_fused(True)
