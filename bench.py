@@ -60,8 +60,14 @@ def parse():
     ap.add_argument("--proposer", default="off", choices=["on", "off"],
                     help="the reference's controller (default) or the learned step-size "
                          "proposer with the shipped weights")
+    ap.add_argument("--beta", type=float, default=0.0,
+                    help="beta of the controller's PI form (bin/ode.cpp:428-439) in both arms; "
+                         "0 is the reference's compiled I-controller")
     ap.add_argument("--proposer-safety", type=float, default=None,
                     help="safety factor of the proposer (default: the trained one's)")
+    ap.add_argument("--fused", default="auto", choices=["auto", "on", "off"],
+                    help="fused small-cloud path: automatic (clouds of up to 512 ions), on "
+                         "(up to 2,048: sg_set_fused 2) or off")
     ap.add_argument("--settle", type=int, default=60,
                     help="at most this many steps to let the step size settle before warm-up")
     return ap.parse_args()
@@ -239,11 +245,17 @@ def check_summary(records, every):
 CHECK_EVERY = 16  # the library's default interval of the in-run force check
 
 
+def controller_name(args) -> str:
+    if args.beta > 0.0:
+        return f"PI controller, beta {args.beta:g} (bin/ode.cpp:428-439)"
+    return "reference I-controller (bin/ode.cpp:426-457)"
+
+
 def apply_step_control(args, batch) -> str:
     """The learned proposer with the shipped weights (every attempt still accepted or
     rejected by the Dormand-Prince error estimate), or the reference's I-controller."""
     if args.proposer == "off":
-        return "reference I-controller (bin/ode.cpp:426-457)"
+        return controller_name(args)
     from simbuca_gb300 import proposer
     s = args.proposer_safety if args.proposer_safety is not None else proposer.DEFAULT_SAFETY
     batch.set_proposer(proposer.default_weights(), s)
@@ -261,9 +273,11 @@ def run_ours(args, dist: Dist):
     prec = abi.SG_PREC_FP32C if args.precision == "fp32c" else abi.SG_PREC_FP64
     for o in w.odes:
         o.method = args.method
+        o.beta = args.beta
     ctx = Context(dist.local)
     if args.variant >= 0:
         ctx.set_coulomb_variant(args.variant)
+    ctx.set_fused({"auto": 1, "on": 2, "off": 0}[args.fused])
     peaks = ctx.probe_peaks()
     batch = Batch(ctx, w.counts, w.fields, w.odes, prec)
     batch.upload(allc.pos, allc.vel, allc.mass, allc.charge)
@@ -471,11 +485,13 @@ def run_ours(args, dist: Dist):
         # plain FP64 GPU form and a second FP32c run, both from the settled snapshot
         # (same state, time and step size), each on its own context
         from simbuca_gb300.configs import ode as mk_ode
-        odes = [mk_ode(o.rtol, o.atol, s["h"], o.t_end, t0=s["t"]) for o, s in zip(w.odes, snap)]
+        odes = [mk_ode(o.rtol, o.atol, s["h"], o.t_end, t0=s["t"], beta=args.beta)
+                for o, s in zip(w.odes, snap)]
         n64 = max(2, min(args.steps, 4))
         runs = {}
         for tag, pr in (("fp64", abi.SG_PREC_FP64), ("fp32c", abi.SG_PREC_FP32C)):
             cx = Context(dist.local)
+            cx.set_fused({"auto": 1, "on": 2, "off": 0}[args.fused])
             bb = Batch(cx, w.counts, w.fields, odes, pr)
             bb.upload(snap_pos, snap_vel, allc.mass, allc.charge)
             bb.step()  # untimed: captures and instantiates the attempt graph
@@ -519,9 +535,12 @@ def run_batched(args, dist: Dist):
     w = configs.WORKLOADS[args.workload]()
     allc = w.concat()
     prec = abi.SG_PREC_FP32C if args.precision == "fp32c" else abi.SG_PREC_FP64
+    for o in w.odes:
+        o.beta = args.beta
     ctx = Context(dist.local)
     if args.variant >= 0:
         ctx.set_coulomb_variant(args.variant)
+    ctx.set_fused({"auto": 1, "on": 2, "off": 0}[args.fused])
     batch = Batch(ctx, w.counts, w.fields, w.odes, prec)
     batch.upload(allc.pos, allc.vel, allc.mass, allc.charge)
     step_control = apply_step_control(args, batch)
@@ -564,7 +583,7 @@ def run_batched(args, dist: Dist):
     off = 0
     for k, n in enumerate([] if args.no_sequential else w.counts):
         o = w.odes[k]
-        op = mk_ode(o.rtol, o.atol, snap[k]["h"], o.t_end, t0=snap[k]["t"])
+        op = mk_ode(o.rtol, o.atol, snap[k]["h"], o.t_end, t0=snap[k]["t"], beta=args.beta)
         b1 = Batch(ctx, [n], [w.fields[k]], [op], prec)
         sl = slice(off, off + n)
         b1.upload(snap_pos[sl], snap_vel[sl], allc.mass[sl], allc.charge[sl])
@@ -676,7 +695,8 @@ def run_reference(args, dist: Dist):
         nonlocal pos, vel, t, h
         p2, v2, cc, hist, nh = oracle.dp45_run(pos, vel, cl0.mass, cl0.charge, fp,
                                                rtol=op.rtol, atol=op.atol, h0=h, t0=t,
-                                               t_end=float("inf"), max_steps=1, hist_cap=64)
+                                               t_end=float("inf"), max_steps=1, hist_cap=64,
+                                               beta=args.beta)
         dsim = cc.t - t
         pos, vel, t, h = p2, v2, cc.t, cc.h
         return dsim, max(nh, 1)
@@ -717,7 +737,7 @@ def run_reference(args, dist: Dist):
                    "l2": "not applicable (CPU)",
                    "settle_steps": len(hist_h), "h_settled": h_settled,
                    "method": "dormand-prince",
-                   "step_control": "reference I-controller (bin/ode.cpp:426-457)",
+                   "step_control": controller_name(args),
                    "coulomb_variant": "CPU FP64 direct sum",
                    "timed_steps": f"{steps} of {args.steps} (timing stops after "
                                   f"{REF_TIME_CAP_S:.0f} s)",

@@ -288,6 +288,12 @@ typedef struct sg_check_info {
     double max_err_far;    /* largest error of the far-ranked probes                      */
     double max_err_near;   /* ... of the near-ranked probes                               */
     double max_err_random; /* ... of the random probes                                    */
+    /* the probe with the largest error over every check */
+    double worst_err;      /* its relative error                                          */
+    double worst_rf;       /* its far ratio sqrt(s2f)/|P| (-1: flagged and fixed up)       */
+    double worst_rn;       /* its near ratio sqrt(s2)/|P| (-1: flagged and fixed up)       */
+    int32_t worst_ion;     /* its index within the cloud, in the caller's order (-1: none) */
+    int32_t worst_kind;    /* 0 far-ranked, 1 near-ranked, 2 random                       */
 } sg_check_info;
 int sg_batch_set_force_check(sg_ctx* ctx, int every_attempts);
 int sg_batch_force_check(sg_ctx* ctx, sg_check_info* out);  /* out[n_clouds] */

@@ -79,7 +79,9 @@ class CheckInfo(ctypes.Structure):
                 ("kfar_prior", ctypes.c_double), ("checks", ctypes.c_int64),
                 ("probes", ctypes.c_int64), ("breaches", ctypes.c_int64),
                 ("max_err_far", ctypes.c_double), ("max_err_near", ctypes.c_double),
-                ("max_err_random", ctypes.c_double)]
+                ("max_err_random", ctypes.c_double), ("worst_err", ctypes.c_double),
+                ("worst_rf", ctypes.c_double), ("worst_rn", ctypes.c_double),
+                ("worst_ion", ctypes.c_int32), ("worst_kind", ctypes.c_int32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -71,7 +71,6 @@ struct Problem {
     std::vector<double> hmass0;
     double *pmass = nullptr, *pmass0 = nullptr;  // print masses (dissociation), both orders
     int* fix_list = nullptr;   // FP32c fix-up work lists: counts, then (ion, cloud) pairs
-    double* fix_pf = nullptr;
     double* fix_part = nullptr;  // fix-up work units' corrections [listed][units][3]
     int* fix_done = nullptr;     // finished units per listed ion (zero between calls)
     // operation sequence
@@ -192,7 +191,6 @@ void free_problem(Problem& P) {
     cudaFree(P.pmass);
     cudaFree(P.pmass0);
     cudaFree(P.fix_list);
-    cudaFree(P.fix_pf);
     cudaFree(P.fix_part);
     cudaFree(P.fix_done);
     cudaFree(P.dops);
@@ -485,11 +483,11 @@ int alloc_problem(sg_ctx* ctx, Problem& P) {
     CK(dalloc(&P.pmass0, N));
     // two lists (near-only ions; ions with a far fix-up): counts, then N pairs each
     CK(dalloc(&P.fix_list, 2 + 4 * N));
-    CK(dalloc(&P.fix_pf, 2 * N));
     CK(cudaMemset(P.fix_list, 0, 2 * sizeof(int)));
-    CK(dalloc(&P.fix_part, (size_t)SG_FIX_CHUNKED_CAP * SG_FIX_UNITS * 3));
-    CK(dalloc(&P.fix_done, SG_FIX_CHUNKED_CAP));
-    CK(cudaMemset(P.fix_done, 0, sizeof(int) * SG_FIX_CHUNKED_CAP));
+    // two lists (row re-evaluations, far corrections) of up to SG_FIX_CHUNKED_CAP ions
+    CK(dalloc(&P.fix_part, (size_t)2 * SG_FIX_CHUNKED_CAP * SG_FIX_UNITS * 3));
+    CK(dalloc(&P.fix_done, 2 * SG_FIX_CHUNKED_CAP));
+    CK(cudaMemset(P.fix_done, 0, sizeof(int) * 2 * SG_FIX_CHUNKED_CAP));
     CK(cudaMemset(P.pmass, 0, N * sizeof(double)));
     CK(cudaMemset(P.pmass0, 0, N * sizeof(double)));
     CK(dalloc(&P.bbox, (size_t)std::max(P.ntiles, 1) * 8));
@@ -690,7 +688,6 @@ int launch_coulomb(sg_ctx* ctx, Problem& P, bool with_ctrl, double inter, double
     ca.variant = P.variant;
     ca.bbox = P.bbox;
     ca.fix_list = P.fix_list;
-    ca.fix_pf = P.fix_pf;
     ca.fix_part = P.fix_part;
     ca.fix_done = P.fix_done;
     ca.far_estimate = far_estimate ? 1 : 0;
@@ -880,7 +877,11 @@ bool fused_eligible(sg_ctx* ctx, Problem& P) {
         big = std::max(big, P.hc[c].n);
     }
     if (P.fused_cluster < 0) P.fused_cluster = sg_fused_cluster_size(P.max_npad);
-    return P.fused_cluster > 0 && big <= P.fused_cluster * SG_FUSED_THREADS;
+    if (P.fused_cluster <= 0 || big > P.fused_cluster * SG_FUSED_THREADS) return false;
+    // automatic: only while every cloud's cluster fits on the device at once; a larger
+    // batch of small clouds runs faster through the batched tiled kernels (167 clouds of
+    // <= 300 ions: 4.6x)
+    return ctx->use_fused == 2 || (long long)P.n_clouds * P.fused_cluster <= ctx->n_sm;
 }
 
 // n attempts of every active cloud at most (a cloud stops early once done or held);
@@ -2195,6 +2196,12 @@ int sg_batch_force_check(sg_ctx* ctx, sg_check_info* out) {
         o.max_err_far = h[c].max_kind[0];
         o.max_err_near = h[c].max_kind[1];
         o.max_err_random = h[c].max_kind[2];
+        o.worst_err = h[c].worst_err;
+        o.worst_rf = h[c].worst_rf;
+        o.worst_rn = h[c].worst_rn;
+        o.worst_kind = h[c].worst_kind;
+        const int wi = h[c].worst_ion;
+        o.worst_ion = h[c].worst_err > 0.0 && wi >= 0 && wi < P.n ? P.perm[wi] - cl[c].off : -1;
     }
     return SG_OK;
 }

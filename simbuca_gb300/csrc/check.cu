@@ -179,6 +179,13 @@ __global__ void check_update_kernel(int* __restrict__ ran, SgCheck* __restrict__
         br += h.err[k] > kBound ? 1 : 0;
         const int kind = k < 2 ? 0 : (k < kRanked ? 1 : 2);
         h.max_kind[kind] = fmax(h.max_kind[kind], h.err[k]);
+        if (h.err[k] > h.worst_err) {
+            h.worst_err = h.err[k];
+            h.worst_rf = h.rf[k];
+            h.worst_rn = h.rn[k];
+            h.worst_ion = h.ion[k];
+            h.worst_kind = kind;
+        }
     }
     for (int k = 0; k < 2; k++)
         if (h.rf[k] > kFarRatioMin) h.c_far = fmax(h.c_far, h.err[k] / (double)h.rf[k]);

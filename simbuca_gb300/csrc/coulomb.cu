@@ -92,7 +92,9 @@ __device__ __forceinline__ void fence_mbar_init() {
 // Close pairs of one flagged ion against one shared-memory tile, evaluated by the
 // whole warp (lanes stride over the tile): pairs whose FP32 1/r^3 exceeded wc get their
 // exact FP64 term, minus the capped FP32 term the main loop already summed (a product
-// of two floats, exact in FP64).  Returns the warp-reduced correction (all lanes).
+// of two floats, exact in FP64).  Returns the warp-reduced correction (all lanes) and,
+// in ymx, the tile's strongest FP32 term as a y3 (pairs below the cap, capped terms:
+// capped_term_y3), which the main loop's y3max cannot give for a tile with a close pair.
 template <int TL>
 __device__ __forceinline__ void close_pairs_warp(const float (*tl)[TL], int len, int j0,
                                                  int ig, float xih, float yih, float zih,
@@ -100,14 +102,17 @@ __device__ __forceinline__ void close_pairs_warp(const float (*tl)[TL], int len,
                                                  double invL2, double qscale,
                                                  const double* __restrict__ c64,
                                                  int npad_total, double& ox, double& oy,
-                                                 double& oz) {
+                                                 double& oz, float& ymx) {
     const int lane = threadIdx.x & 31;
     const double xi = c64[ig], yi = c64[npad_total + ig], zi = c64[2 * (size_t)npad_total + ig];
     double cx = 0.0, cy = 0.0, cz = 0.0;
+    float ym = 0.f;
     for (int jj = lane; jj < len; jj += 32) {
         const PairF p = pair_f32(tl[0][jj], tl[1][jj], tl[2][jj], tl[4][jj], tl[5][jj],
                                  tl[6][jj], xih, yih, zih, xil, yil, zil);
         const int jg = j0 + jj;
+        if (jg != ig && tl[3][jj] != 0.f)
+            ym = fmaxf(ym, p.y3 > wc ? capped_term_y3(p.y3, wc) : p.y3);
         if (p.y3 > wc && jg != ig) {
             const float wf = __fmul_rn(tl[3][jj], wc);
             const double rx = xi - c64[jg];
@@ -130,6 +135,8 @@ __device__ __forceinline__ void close_pairs_warp(const float (*tl)[TL], int len,
     ox = cx;
     oy = cy;
     oz = cz;
+    // non-negative floats order as their bit patterns
+    ymx = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(ym)));
 }
 
 // Main loop over one shared-memory j-tile for the IPT ions of a thread: packed FP32x2
@@ -182,25 +189,6 @@ __device__ __forceinline__ void tile_pairs(const float* tx, const float* ty, con
     }
 }
 
-
-// Pair term from the high parts only (tiles farther apart than SgCloud::dfar): the
-// quantisation of |u| ~ 1 costs ~1e-7 relative only for pairs this far apart.
-struct PairH {
-    float dx, dy, dz, y3;
-};
-__device__ __forceinline__ PairH pair_hi(float xjh, float yjh, float zjh, float xih, float yih,
-                                         float zih) {
-    PairH p;
-    p.dx = __fsub_rn(xjh, xih);
-    p.dy = __fsub_rn(yjh, yih);
-    p.dz = __fsub_rn(zjh, zih);
-    float r2 = __fmaf_rn(p.dx, p.dx, kTiny);
-    r2 = __fmaf_rn(p.dy, p.dy, r2);
-    r2 = __fmaf_rn(p.dz, p.dz, r2);
-    const float y = rsqrt_approx(r2);
-    p.y3 = __fmul_rn(__fmul_rn(y, y), y);
-    return p;
-}
 
 // Squared distance between two tile bounding boxes (frame units).
 __device__ __forceinline__ float box_dist2(const float* a, const float* b) {
@@ -403,8 +391,8 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
                 s2[k] = fmaf(tx_, tx_, fmaf(ty_, ty_, fmaf(tz_, tz_, s2[k])));
             }
         }
-        // the strongest single pair so far (conditioning estimate), from tiles without a
-        // close pair: those are evaluated exactly below, the fix-up cannot improve them
+        // the strongest single FP32 term so far (conditioning estimate); a tile with a
+        // close pair gives its strongest term below the cap from the close-pair pass
 #pragma unroll
         for (int k = 0; k < IPT; k++)
             if (y3max[k] <= wc) fmx[k] = fmaxf(fmx[k], y3max[k]);
@@ -430,9 +418,11 @@ __global__ void __launch_bounds__(NT) coulomb_fp32c_kernel(const float* __restri
                 const float zil = __shfl_sync(0xffffffffu, a, src);
                 const int igs = __shfl_sync(0xffffffffu, ipad[k], src);
                 double ox, oy, oz;
+                float ymx;
                 close_pairs_warp(tile[s], len, j0, igs, xih, yih, zih, xil, yil, zil, wc, invL2, qscale,
-                                 c64, npad_total, ox, oy, oz);
+                                 c64, npad_total, ox, oy, oz, ymx);
                 if ((tid & 31) == src) {
+                    fmx[k] = fmaxf(fmx[k], ymx);
                     const int li = tid + k * NT;
                     corr[0][li] += ox;
                     corr[1][li] += oy;
@@ -663,8 +653,8 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
                 fold_partials<IPT, S2F>(ax, ay, az, ks, kc, s2, s2f, !far);
             }
         }
-        // the strongest single pair so far (conditioning estimate), from tiles without a
-        // close pair: those are evaluated exactly below, the fix-up cannot improve them
+        // the strongest single FP32 term so far (conditioning estimate); a tile with a
+        // close pair gives its strongest term below the cap from the close-pair pass
 #pragma unroll
         for (int k = 0; k < IPT; k++)
             if (y3max[k] <= wc) fmx[k] = fmaxf(fmx[k], y3max[k]);
@@ -690,9 +680,11 @@ __global__ void __launch_bounds__(NT, MINB) coulomb_fp32c_sorted_kernel(const fl
                 const float zil = __shfl_sync(0xffffffffu, a, src);
                 const int igs = __shfl_sync(0xffffffffu, ipad[k], src);
                 double ox, oy, oz;
+                float ymx;
                 close_pairs_warp(tile[s], len, j0, igs, xih, yih, zih, xil, yil, zil, wc, invL2, qscale,
-                                 c64, npad_total, ox, oy, oz);
+                                 c64, npad_total, ox, oy, oz, ymx);
                 if ((tid & 31) == src) {
+                    fmx[k] = fmaxf(fmx[k], ymx);
                     const int li = IPT * tid + k;
                     corr[0][li] += ox;
                     corr[1][li] += oy;
@@ -806,9 +798,8 @@ __global__ void __launch_bounds__(NT) coulomb_fp64_kernel(const double* __restri
 // FP32c only: the conditioning test.  sqrt(s2) estimates sqrt(sum_j |f_ij|^2) of the
 // FP32 terms; the rounding of those terms is random, so the error of P_i is about
 // 2.5e-7 * sqrt(s2).  An ion whose FP32 terms cancel strongly (sqrt(s2) > 1.5 |P_i|,
-// e.g. near the centre of a cloud) gets its dominant pairs -- those with
-// |f_ij| > 0.1 |P_i| that the main kernel did not already take in FP64 -- re-evaluated
-// in FP64, one block per flagged ion over the cloud's j-range.
+// e.g. near the centre of a cloud, or a single term above 1.5 |P_i|) gets its whole row
+// re-evaluated in FP64 (fixup_row), spread over work units for a large cloud.
 //
 // k-d ordered shapes: the far tile pairs were summed from the high FP32 parts only, an
 // error of ~1e-7 per pair that averages out unless the ion's net force is small next to
@@ -823,8 +814,6 @@ constexpr double kKappa2 = 2.25;
 // kinds of fix-up of a flagged ion
 constexpr int kFixNear = 1, kFixFar = 2;
 
-// tiles listed for the fix-up scan of one ion in k-d order
-constexpr int kNearCap = 1024;
 // blocks of the fix-up kernel (each takes every kFixupBlocks-th work unit)
 constexpr int kFixupBlocks = 512;
 // work units of one listed ion in the fix-up kernel, and the listed ions that get them
@@ -843,8 +832,6 @@ __device__ __forceinline__ float two_diff_err(float a, float b, float s) {
 template <int NTH>
 struct FixupShared {
     double wsum[NTH / 32][3];
-    int wcnt[NTH / 32];
-    int near_tiles[kNearCap];
 };
 
 struct Corr3 {
@@ -877,85 +864,30 @@ __device__ Corr3 block_sum3(double ax, double ay, double az, FixupShared<NTH>& s
     return r;
 }
 
-// Near fix-up of ion i (frame-unit force magnitude pf) by the whole block of NTH threads:
-// the pairs with |f_ij| > |P_i| / 10 are re-evaluated in FP64 and their FP32 terms, as
-// the Coulomb kernel summed them, removed.  Returns the correction of P_i (thread 0).
+// Row of a flagged ion in FP64, chunk c of nch (contiguous j-ranges of the cloud's padded
+// range; the padding ions carry no charge), by the whole block of NTH threads: the sum
+// of q_j (x_i - x_j) / r^3 over the chunk, from the SI coordinates (thread 0's result).
+// Re-evaluating only the dominant pairs is not enough: an ion whose FP32 terms cancel
+// keeps the rounding of every addition made while a dominant term was in its partial sum
+// (~1e-7 |f_max|), so the flagged ion's sum is replaced by its exact row.
 template <int NTH>
-__device__ Corr3 fixup_near(const SgCloud& cl, int i, double pf, const float* __restrict__ c32,
-                            const double* __restrict__ c64, int npad_total,
-                            const float* __restrict__ bbox, FixupShared<NTH>& sh) {
-    int* wcnt = sh.wcnt;
-    int* near_tiles = sh.near_tiles;
-    const int li = threadIdx.x;
-    const int warp = li >> 5, lane = li & 31;
+__device__ Corr3 fixup_row(const SgCloud& cl, int i, const double* __restrict__ c64,
+                           int npad_total, int c, int nch, FixupShared<NTH>& sh) {
     const size_t NP = (size_t)npad_total;
     const int igk = cl.poff + (i - cl.off);
-    const double invL2 = cl.invL * cl.invL;
-    const float wc = cl.wc;
-    const double tq = 0.1 * pf;
-    const float thr3 = (float)(tq * sqrt(tq));  // (|P|/10)^(3/2): |f_ij| > |P|/10
-    const float xih = c32[igk], yih = c32[NP + igk], zih = c32[2 * NP + igk];
-    const float xil = c32[4 * NP + igk], yil = c32[5 * NP + igk], zil = c32[6 * NP + igk];
     const double xi = c64[igk], yi = c64[NP + igk], zi = c64[2 * NP + igk];
+    const int len = (cl.npad + nch - 1) / nch;
+    const int j0 = c * len, j1 = min(cl.npad, j0 + len);
     double ax = 0.0, ay = 0.0, az = 0.0;
-    const float* ibox = bbox ? bbox + 8 * (size_t)(cl.tile0 + (igk - cl.poff) / 128) : nullptr;
-    // k-d ordered clouds: scan only the tiles near the ion's own tile, listed in order by
-    // a block-wide ballot (far tiles are the far fix-up's); the whole cloud if the list
-    // would overflow
-    int n_near = 0;
-    if (ibox != nullptr) {
-        const int nt = (cl.npad + 127) / 128, itile = (igk - cl.poff) / 128;
-        const float dfar2 = cl.dfar * cl.dfar;
-        for (int t0 = 0; t0 < nt; t0 += NTH) {
-            const int t = t0 + li;
-            const bool nr = t < nt && (t == itile ||
-                                       box_dist2(ibox, bbox + 8 * (size_t)(cl.tile0 + t)) <= dfar2);
-            const unsigned m = __ballot_sync(0xffffffffu, nr);
-            if (lane == 0) wcnt[warp] = __popc(m);
-            __syncthreads();
-            int off = n_near, tot = 0;
-            for (int w = 0; w < NTH / 32; w++) {
-                if (w < warp) off += wcnt[w];
-                tot += wcnt[w];
-            }
-            if (nr) {
-                const int at = off + __popc(m & ((1u << lane) - 1u));
-                if (at < kNearCap) near_tiles[at] = t;
-            }
-            __syncthreads();
-            n_near += tot;
-        }
-    }
-    const bool listed = ibox != nullptr && n_near <= kNearCap;
-    const int n_scan = listed ? n_near * 128 : cl.npad;
-    for (int qj = li; qj < n_scan; qj += NTH) {
-        const int j = listed ? near_tiles[qj >> 7] * 128 + (qj & 127) : qj;
-        if (j >= cl.npad) continue;
+    for (int j = j0 + (int)threadIdx.x; j < j1; j += NTH) {
         const int jg = cl.poff + j;
-        PairF p = pair_f32(c32[jg], c32[NP + jg], c32[2 * NP + jg], c32[4 * NP + jg],
-                           c32[5 * NP + jg], c32[6 * NP + jg], xih, yih, zih, xil, yil, zil);
-        if (ibox != nullptr && !listed) {
-            // the sorted kernel summed this pair from the high parts if its tiles are far
-            const float* jbox = bbox + 8 * (size_t)(cl.tile0 + j / 128);
-            const bool same = (igk - cl.poff) / 128 == j / 128;
-            if (!same && box_dist2(ibox, jbox) > cl.dfar * cl.dfar) {
-                const PairH q = pair_hi(c32[jg], c32[NP + jg], c32[2 * NP + jg], xih, yih, zih);
-                p.dx = q.dx;
-                p.dy = q.dy;
-                p.dz = q.dz;
-                p.y3 = q.y3;
-            }
-        }
-        if (p.y3 > thr3 && p.y3 <= wc && jg != igk) {
-            const float wf = __fmul_rn(c32[3 * NP + jg], p.y3);
-            const double rx = xi - c64[jg], ry = yi - c64[NP + jg], rz = zi - c64[2 * NP + jg];
-            const double inv = rsqrt_fp64(rx * rx + ry * ry + rz * rz);
-            const double wq = c64[3 * NP + jg] * inv * inv * inv;
-            const double wsc = invL2 * (double)cl.qscale * (double)wf;
-            ax += wq * rx + wsc * (double)p.dx;
-            ay += wq * ry + wsc * (double)p.dy;
-            az += wq * rz + wsc * (double)p.dz;
-        }
+        if (jg == igk) continue;
+        const double rx = xi - c64[jg], ry = yi - c64[NP + jg], rz = zi - c64[2 * NP + jg];
+        const double inv = rsqrt_fp64(rx * rx + ry * ry + rz * rz);
+        const double wq = c64[3 * NP + jg] * inv * inv * inv;
+        ax = fma(wq, rx, ax);
+        ay = fma(wq, ry, ay);
+        az = fma(wq, rz, az);
     }
     return block_sum3<NTH>(ax, ay, az, sh);
 }
@@ -1019,26 +951,29 @@ __device__ Corr3 fixup_far(const SgCloud& cl, int i, const float* __restrict__ c
     return r;
 }
 
-// Whole fix-up of one flagged ion by one block: kFixFar (k-d ordered shapes) and/or
-// kFixNear, added to out by thread 0.  The j-ions are taken in a fixed order, so the
-// result does not depend on which block runs it or when.
+// Whole fix-up of one flagged ion by one block: kFixNear replaces its sum by the exact
+// FP64 row (which also covers its far terms); kFixFar alone adds the far correction
+// (k-d ordered shapes).  Written to out by thread 0.  The j-ions are taken in a fixed
+// order, so the result does not depend on which block runs it or when.
 template <int NTH>
-__device__ void fixup_ion(const SgCloud& cl, int i, double pf, int kind,
-                          const float* __restrict__ c32, const double* __restrict__ c64,
-                          int npad_total, double* __restrict__ out, int n_total,
-                          const float* __restrict__ bbox, FixupShared<NTH>& sh) {
-    Corr3 r{0.0, 0.0, 0.0};
-    if ((kind & kFixFar) && bbox != nullptr) r = fixup_far<NTH>(cl, i, c32, npad_total, bbox, 0, 1, sh);
+__device__ void fixup_ion(const SgCloud& cl, int i, int kind, const float* __restrict__ c32,
+                          const double* __restrict__ c64, int npad_total,
+                          double* __restrict__ out, int n_total, const float* __restrict__ bbox,
+                          FixupShared<NTH>& sh) {
     if (kind & kFixNear) {
-        const Corr3 q = fixup_near<NTH>(cl, i, pf, c32, c64, npad_total, bbox, sh);
-        r.x += q.x;
-        r.y += q.y;
-        r.z += q.z;
-    }
-    if (threadIdx.x == 0) {
-        out[i] += r.x;
-        out[(size_t)n_total + i] += r.y;
-        out[2 * (size_t)n_total + i] += r.z;
+        const Corr3 r = fixup_row<NTH>(cl, i, c64, npad_total, 0, 1, sh);
+        if (threadIdx.x == 0) {
+            out[i] = r.x;
+            out[(size_t)n_total + i] = r.y;
+            out[2 * (size_t)n_total + i] = r.z;
+        }
+    } else if (bbox != nullptr) {
+        const Corr3 r = fixup_far<NTH>(cl, i, c32, npad_total, bbox, 0, 1, sh);
+        if (threadIdx.x == 0) {
+            out[i] += r.x;
+            out[(size_t)n_total + i] += r.y;
+            out[2 * (size_t)n_total + i] += r.z;
+        }
     }
     __syncthreads();
 }
@@ -1055,7 +990,7 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     const SgRowBlock* __restrict__ rows, const SgCloud* __restrict__ clouds,
     const SgCtrl* __restrict__ ctrl, const double* __restrict__ part, int npad_total,
     double* __restrict__ out, int n_total, int* __restrict__ counters,
-    int* __restrict__ fix_list, double* __restrict__ fix_pf, const float* __restrict__ c32,
+    int* __restrict__ fix_list, const float* __restrict__ c32,
     const double* __restrict__ c64, const float* __restrict__ bbox, float* __restrict__ risk,
     int* __restrict__ ran, const SgCheck* __restrict__ chk) {
     sg_griddep_wait();
@@ -1102,13 +1037,13 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     if (!F32) return;
     if (!INBLOCK) {
         if (kind) {
-            // two lists: near-only ions from fix_list[2], the others from fix_list[2 + 2N]
-            const bool far = (kind & kFixFar) != 0;
+            // two lists: ions whose row is re-evaluated (kFixNear) from fix_list[2], the
+            // far-only ones from fix_list[2 + 2N]
+            const bool far = kind == kFixFar;
             const int at = atomicAdd(fix_list + (far ? 1 : 0), 1);
             const size_t base = far ? 2 + 2 * (size_t)n_total : 2;
             fix_list[base + 2 * at] = i;
             fix_list[base + 2 * at + 1] = rb.cloud | (kind << 28);
-            fix_pf[(far ? (size_t)n_total : 0) + at] = pf;
             if (counters != nullptr) atomicAdd(counters, 1);
         }
         return;
@@ -1117,96 +1052,94 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     __shared__ int nflag;
     __shared__ int flist[SG_ROWS];
     __shared__ int fkind[SG_ROWS];
-    __shared__ double fpf[SG_ROWS];
     if (li == 0) nflag = 0;
     __syncthreads();
     if (kind) {
         const int at = atomicAdd(&nflag, 1);
         flist[at] = i;
         fkind[at] = kind;
-        fpf[at] = pf;
         if (counters != nullptr) atomicAdd(counters, 1);
     }
     __syncthreads();  // also orders this block's writes of out before the corrections
     const int nf = nflag;
     for (int k = 0; k < nf; k++)
-        fixup_ion(cl, flist[k], fpf[k], fkind[k], c32, c64, npad_total, out, n_total, bbox, sh);
+        fixup_ion(cl, flist[k], fkind[k], c32, c64, npad_total, out, n_total, bbox, sh);
 }
 
-// The flagged ions of a whole batch.  A near-only ion is one work unit.  Each of the
-// first kChunkedCap ions with a far fix-up is kFarChunks units (unit 0 also does its near
-// fix-up), so that the far scan of the whole cloud is spread over blocks: each unit leaves
-// its correction in fix_part and the last unit of the ion (counted in fix_done) adds them
-// to out in unit order -- the result does not depend on the order the units ran in.
-// Units are numbered so that every ion's first units come first.  Far ions past the cap
-// are one unit each.  Blocks of 256 threads, three per SM (80 registers, no spills):
-// the units of a 65,536-ion call (about 170) run in one wave.
+// The flagged ions of a whole batch, in two lists: the ions whose row is re-evaluated in
+// FP64 (kFixNear) and the far-only ones (kFixFar).  Each of the first kChunkedCap ions of
+// a list is kFarChunks work units, so that the scan of a large cloud is spread over
+// blocks: each unit leaves its part in fix_part and the last unit of the ion (counted in
+// fix_done) combines them in unit order -- writing the row, or adding the far correction
+// -- so the result does not depend on the order the units ran in.  Units are numbered
+// so that every ion's first units come first.  Ions past the caps are one unit each.
+// Blocks of 256 threads, three per SM: the units of a 65,536-ion call run in one or two
+// waves.
 constexpr int kFixupThreads = 256;
 __global__ void __launch_bounds__(kFixupThreads, 3) coulomb_fixup_kernel(
     const SgCloud* __restrict__ clouds, const float* __restrict__ c32,
     const double* __restrict__ c64, int npad_total, double* __restrict__ out, int n_total,
-    const int* __restrict__ fix_list, const double* __restrict__ fix_pf,
-    const float* __restrict__ bbox, double* __restrict__ fix_part, int* __restrict__ fix_done) {
+    const int* __restrict__ fix_list, const float* __restrict__ bbox,
+    double* __restrict__ fix_part, int* __restrict__ fix_done) {
     sg_griddep_wait();
     __shared__ FixupShared<kFixupThreads> sh;
     __shared__ int last;
+    constexpr int U = kFarChunks;
     const int cn = fix_list[0], cf = fix_list[1];
-    const int* near_list = fix_list + 2;
+    const int* row_list = fix_list + 2;
     const int* far_list = fix_list + 2 + 2 * (size_t)n_total;
-    const double* far_pf = fix_pf + n_total;
-    const int cfc = min(cf, kChunkedCap);
-    const int units = cn + cfc * kFarChunks + (cf - cfc);
+    const int cnc = min(cn, kChunkedCap), cfc = min(cf, kChunkedCap);
+    const int u_rows = cnc * U + (cn - cnc);
+    const int units = u_rows + cfc * U + (cf - cfc);
     for (int u = blockIdx.x; u < units; u += gridDim.x) {
-        if (u < cn) {
-            const int ck = near_list[2 * u + 1];
-            fixup_ion<kFixupThreads>(clouds[ck & 0x0FFFFFFF], near_list[2 * u], fix_pf[u],
-                                     ck >> 28, c32, c64, npad_total, out, n_total, bbox, sh);
+        const bool row = u < u_rows;
+        const int v = row ? u : u - u_rows;
+        const int nc = row ? cnc : cfc;
+        const int* list = row ? row_list : far_list;
+        if (v >= nc * U) {  // past the cap: the whole ion in this unit
+            const int k = nc + (v - nc * U);
+            const int ck = list[2 * k + 1];
+            fixup_ion<kFixupThreads>(clouds[ck & 0x0FFFFFFF], list[2 * k], ck >> 28, c32, c64,
+                                     npad_total, out, n_total, bbox, sh);
             continue;
         }
-        const int v = u - cn;
-        if (v >= cfc * kFarChunks) {
-            const int k = cfc + (v - cfc * kFarChunks);
-            const int ck = far_list[2 * k + 1];
-            fixup_ion<kFixupThreads>(clouds[ck & 0x0FFFFFFF], far_list[2 * k], far_pf[k],
-                                     ck >> 28, c32, c64, npad_total, out, n_total, bbox, sh);
-            continue;
-        }
-        const int k = v % cfc, c = v / cfc;
-        const int i = far_list[2 * k];
-        const int ck = far_list[2 * k + 1];
-        const SgCloud& cl = clouds[ck & 0x0FFFFFFF];
-        const int kind = ck >> 28;
+        const int k = v % nc, c = v / nc;
+        const int i = list[2 * k];
+        const SgCloud& cl = clouds[list[2 * k + 1] & 0x0FFFFFFF];
         Corr3 r{0.0, 0.0, 0.0};
-        if (bbox != nullptr)
-            r = fixup_far<kFixupThreads>(cl, i, c32, npad_total, bbox, c, kFarChunks, sh);
-        if (c == 0 && (kind & kFixNear)) {
-            const Corr3 q = fixup_near<kFixupThreads>(cl, i, far_pf[k], c32, c64, npad_total, bbox, sh);
-            r.x += q.x;
-            r.y += q.y;
-            r.z += q.z;
-        }
+        if (row)
+            r = fixup_row<kFixupThreads>(cl, i, c64, npad_total, c, U, sh);
+        else if (bbox != nullptr)
+            r = fixup_far<kFixupThreads>(cl, i, c32, npad_total, bbox, c, U, sh);
+        const size_t slot = (row ? 0 : (size_t)kChunkedCap) + (size_t)k;
         if (threadIdx.x == 0) {
-            double* fp = fix_part + ((size_t)k * kFarChunks + c) * 3;
+            double* fp = fix_part + (slot * U + c) * 3;
             fp[0] = r.x;
             fp[1] = r.y;
             fp[2] = r.z;
             __threadfence();
-            last = atomicAdd(&fix_done[k], 1) == kFarChunks - 1;
+            last = atomicAdd(&fix_done[slot], 1) == U - 1;
         }
         __syncthreads();
         if (last && threadIdx.x == 0) {
             __threadfence();
-            const volatile double* vp = fix_part + (size_t)k * kFarChunks * 3;
+            const volatile double* vp = fix_part + slot * U * 3;
             double sx = 0.0, sy = 0.0, sz = 0.0;
-            for (int q = 0; q < kFarChunks; q++) {
+            for (int q = 0; q < U; q++) {
                 sx += vp[3 * q];
                 sy += vp[3 * q + 1];
                 sz += vp[3 * q + 2];
             }
-            out[i] += sx;
-            out[(size_t)n_total + i] += sy;
-            out[2 * (size_t)n_total + i] += sz;
-            fix_done[k] = 0;  // ready for the next call
+            if (row) {
+                out[i] = sx;
+                out[(size_t)n_total + i] = sy;
+                out[2 * (size_t)n_total + i] = sz;
+            } else {
+                out[i] += sx;
+                out[(size_t)n_total + i] += sy;
+                out[2 * (size_t)n_total + i] += sz;
+            }
+            fix_done[slot] = 0;  // ready for the next call
         }
         __syncthreads();
     }
@@ -1339,24 +1272,24 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
         if (n_total <= kInBlockFixupMax) {
             sg_launch(coulomb_reduce_kernel<true, true>, n_rows, SG_ROWS, 0, s, 
                 rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, nullptr,
-                nullptr, a.c32, a.c64, bbox, a.risk, a.ran, a.chk);
+                a.c32, a.c64, bbox, a.risk, a.ran, a.chk);
             return cudaGetLastError();
         }
         cudaError_t e = cudaMemsetAsync(a.fix_list, 0, 2 * sizeof(int), s);
         if (e != cudaSuccess) return e;
         coulomb_reduce_kernel<true, false><<<n_rows, SG_ROWS, 0, s>>>(
             rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, a.fix_list,
-            a.fix_pf, nullptr, nullptr, nullptr, a.risk, a.ran, a.chk);
+            nullptr, nullptr, nullptr, a.risk, a.ran, a.chk);
         // a block per flagged ion: a fixed grid that strides over however many there are
         // (flagged ions are a small fraction: small batches get a small grid)
         const int grid = n_total / 256 < 1 ? 1 : (n_total / 256 > kFixupBlocks ? kFixupBlocks : n_total / 256);
         sg_launch(coulomb_fixup_kernel, grid, kFixupThreads, 0, s, 
-            a.clouds, a.c32, a.c64, a.npad_total, out, n_total, a.fix_list, a.fix_pf, bbox,
+            a.clouds, a.c32, a.c64, a.npad_total, out, n_total, a.fix_list, bbox,
             a.fix_part, a.fix_done);
     } else {
         sg_launch(coulomb_reduce_kernel<false, false>, n_rows, SG_ROWS, 0, s, 
             rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, nullptr,
-            nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+            nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
     }
     return cudaGetLastError();
 }

@@ -89,10 +89,19 @@ __device__ __forceinline__ double rsqrt_fp64(double r2) {
 
 // The conditioning estimate of an ion: the sum of squares of its FP32 partial sums, or,
 // if larger, the squared magnitude of its strongest single pair term, |f|^2 = (1/r^3)^(4/3)
-// in frame units for a unit charge (y3max, self pair excluded, over the tiles without a
-// close pair).  A dominant pair whose partial sum is cancelled by other terms of the
-// same block must still flag the ion for the FP64 re-evaluation of its dominant pairs.  A threshold test: FP32 suffices
-// (an overflow to infinity only flags the ion).
+// in frame units for a unit charge (y3max, self pair excluded; in tiles with a close
+// pair, the pairs below the cap and the capped terms, capped_term_y3).  A dominant pair
+// whose partial sum is cancelled by other terms of the same block must still flag the ion
+// for the FP64 re-evaluation of its row.  A threshold test: FP32 suffices (an overflow to
+// infinity only flags the ion).
+// A close pair (y3 > wc) enters the main loop's sums with its 1/r^3 capped at wc: a term
+// of magnitude wc r, whose rounding in the partial sum stays although the pair itself is
+// re-evaluated exactly.  As a strongest-term candidate it counts as the y3 whose |f| is
+// that magnitude: (wc r)^(3/2) = wc sqrt(wc / y3) (<= wc).
+__device__ __forceinline__ float capped_term_y3(float y3, float wc) {
+    return wc * sqrtf(wc / y3);
+}
+
 __device__ __forceinline__ float conditioning_s2(float s2, float y3max) {
     const float r1 = cbrtf(y3max);  // 1/r
     const float f = r1 * r1;        // |f| = 1/r^2

@@ -48,8 +48,7 @@ struct FusedShared {
     float s2[kThreads];        // per thread: its conditioning estimate
     int nflag;
     int flag_il[kThreads];     // flagged ions (local index) ...
-    float flag_pf[kThreads];   // ... their |P| in frame units ...
-    double flag_corr[kThreads][3];  // ... and their FP64 corrections
+    double flag_corr[kThreads][3];  // ... and their FP64 rows
 };
 
 __device__ __forceinline__ int ldcg_int(const int* p) { return __ldcg(p); }
@@ -258,7 +257,8 @@ __device__ void coulomb_phase(const SgFusedArgs& f, const SgCloud& cl, int lo, i
             s2 = fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, s2)));
             if (y3max <= wc) fmx = fmaxf(fmx, y3max);  // blocks without a close pair
             if (y3max > wc) {
-                // close pairs of this partial: the exact FP64 term, minus the capped FP32 term
+                // close pairs of this partial: the exact FP64 term, minus the capped FP32 term;
+                // the block's strongest FP32 term (below the cap, or capped) for fmx
                 const double xi = SX[li], yi = SY[li], zi = SZ[li];
                 for (int u = 0; u < kFlush; u++) {
                     const int p = p0 + (u >> 1) * G;
@@ -266,6 +266,8 @@ __device__ void coulomb_phase(const SgFusedArgs& f, const SgCloud& cl, int lo, i
                     const int jj = 2 * p + (u & 1);
                     const PairF pr = pair_f32(X[jj], Y[jj], Z[jj], XL[jj], YL[jj], ZL[jj], xih,
                                               yih, zih, xil, yil, zil);
+                    if (jj != li && Q[jj] != 0.f)
+                        fmx = fmaxf(fmx, pr.y3 > wc ? capped_term_y3(pr.y3, wc) : pr.y3);
                     if (pr.y3 > wc && jj != li) {
                         const float wf = __fmul_rn(Q[jj], wc);
                         const double rx = xi - SX[jj];
@@ -313,7 +315,6 @@ __device__ void coulomb_phase(const SgFusedArgs& f, const SgCloud& cl, int lo, i
         if (flagged) {
             const int at = atomicAdd(&sh.nflag, 1);
             sh.flag_il[at] = tid;
-            sh.flag_pf[at] = pf;
         }
         if (f.risk != nullptr) {
             f.risk[i] = flagged ? -1.f : 0.f;
@@ -321,31 +322,23 @@ __device__ void coulomb_phase(const SgFusedArgs& f, const SgCloud& cl, int lo, i
         }
     }
     __syncthreads();
-    // near fix-up of the flagged ions, one warp per ion: the pairs with |f_ij| > |P_i|/10
-    // that were not close pairs, re-evaluated in FP64 (the FP32 term removed)
+    // fix-up of the flagged ions, one warp per ion: the whole row in FP64 from the SI
+    // coordinates, which replaces the ion's sum (re-evaluating only its dominant pairs
+    // would keep the rounding of the FP32 additions made while they were in a partial sum)
     const int nf = sh.nflag;
     const int warp = tid >> 5, lane = tid & 31;
     for (int k = warp; k < nf; k += kThreads / 32) {
         const int li = lo + sh.flag_il[k] - cl.off;
-        const float tq = 0.1f * sh.flag_pf[k];
-        const float thr3 = tq * sqrtf(tq);
-        const float xih = X[li], yih = Y[li], zih = Z[li];
-        const float xil = XL[li], yil = YL[li], zil = ZL[li];
         double ax = 0.0, ay = 0.0, az = 0.0;
         const double xi = SX[li], yi = SY[li], zi = SZ[li];
         for (int jj = lane; jj < npc; jj += 32) {
-            const PairF p = pair_f32(X[jj], Y[jj], Z[jj], XL[jj], YL[jj], ZL[jj], xih, yih, zih,
-                                     xil, yil, zil);
-            if (p.y3 > thr3 && p.y3 <= wc && jj != li) {
-                const float wf = __fmul_rn(Q[jj], p.y3);
-                const double rx = xi - SX[jj], ry = yi - SY[jj], rz = zi - SZ[jj];
-                const double inv = rsqrt_fp64(rx * rx + ry * ry + rz * rz);
-                const double wq = SQ[jj] * inv * inv * inv;
-                const double wsc = invL2 * qscale * (double)wf;
-                ax += wq * rx + wsc * (double)p.dx;
-                ay += wq * ry + wsc * (double)p.dy;
-                az += wq * rz + wsc * (double)p.dz;
-            }
+            if (jj == li) continue;
+            const double rx = xi - SX[jj], ry = yi - SY[jj], rz = zi - SZ[jj];
+            const double inv = rsqrt_fp64(rx * rx + ry * ry + rz * rz);
+            const double wq = SQ[jj] * inv * inv * inv;
+            ax = fma(wq, rx, ax);
+            ay = fma(wq, ry, ay);
+            az = fma(wq, rz, az);
         }
         for (int o = 16; o > 0; o >>= 1) {
             ax += __shfl_down_sync(0xffffffffu, ax, o);
@@ -361,9 +354,9 @@ __device__ void coulomb_phase(const SgFusedArgs& f, const SgCloud& cl, int lo, i
     __syncthreads();
     for (int k = 0; k < nf; k++)
         if (sh.flag_il[k] == tid) {
-            P[0] += sh.flag_corr[k][0];
-            P[1] += sh.flag_corr[k][1];
-            P[2] += sh.flag_corr[k][2];
+            P[0] = sh.flag_corr[k][0];
+            P[1] = sh.flag_corr[k][1];
+            P[2] = sh.flag_corr[k][2];
         }
     if (tid < m) {
         const size_t N = (size_t)f.n;

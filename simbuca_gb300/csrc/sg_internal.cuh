@@ -490,7 +490,6 @@ struct SgCoulombArgs {
     // FP32c conditioning fix-up work list, filled by the reduction: [0] count, then
     // per flagged ion its global index and cloud (ints) and |P| in frame units
     int* fix_list;
-    double* fix_pf;
     // per listed ion and work unit its correction, and the count of finished units
     double* fix_part;
     int* fix_done;
@@ -519,6 +518,11 @@ struct SgCheck {
     int32_t ion[SG_CHECK_PROBES];
     float rf[SG_CHECK_PROBES], rn[SG_CHECK_PROBES];
     double err[SG_CHECK_PROBES];
+    // the probe with the largest error over every check: its error, its ratios (-1:
+    // flagged, fixed up), its ion (device order) and kind (0 far, 1 near, 2 random)
+    double worst_err;
+    float worst_rf, worst_rn;
+    int32_t worst_ion, worst_kind;
 };
 cudaError_t sg_force_check(const SgCloud* clouds, int n_clouds, int* ran, const float* risk,
                            const double* c64, int npad_total, const double* out, int n_total,

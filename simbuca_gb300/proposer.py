@@ -131,7 +131,8 @@ def run_controller(ctx: Context, w: configs.Workload, horizon: float, weights=No
 
 
 def compare(ctx: Context, w: configs.Workload, horizon: float, betas, weights=None,
-            safety=DEFAULT_SAFETY, log_cap: int = 0, max_attempts: int = 1 << 40):
+            safety=DEFAULT_SAFETY, log_cap: int = 0, max_attempts: int = 1 << 40,
+            on_result=None):
     """The same workload and horizon under the reference's I-controller and PI
     controllers (beta > 0), and with the learned proposer when weights are given."""
     res = {}
@@ -139,10 +140,14 @@ def compare(ctx: Context, w: configs.Workload, horizon: float, betas, weights=No
         tag = "i_controller" if beta == 0 else f"pi_beta_{beta}"
         res[tag] = run_controller(ctx, w, horizon, beta=beta, log_cap=log_cap,
                                   max_attempts=max_attempts)
+        if on_result:
+            on_result(tag, res[tag])
     if weights is not None:
-        res[f"mlp_safety_{safety}"] = run_controller(ctx, w, horizon, weights=weights,
-                                                     safety=safety, log_cap=log_cap,
-                                                     max_attempts=max_attempts)
+        tag = f"mlp_safety_{safety}"
+        res[tag] = run_controller(ctx, w, horizon, weights=weights, safety=safety,
+                                  log_cap=log_cap, max_attempts=max_attempts)
+        if on_result:
+            on_result(tag, res[tag])
     return res
 
 
@@ -175,9 +180,14 @@ def main():
         kw = {} if a.seed is None else {"seed": a.seed}
         ev = (configs.learned_4k(sim_time=a.horizon, **kw) if a.eval == "learned_4k"
               else configs.WORKLOADS[a.eval]())
+        def save(tag, r):
+            with open(os.path.join(a.out, f"compare_{tag}.json"), "w") as f:
+                json.dump({k: v for k, v in r.items() if k != "log"}, f, indent=1)
+            print(tag, json.dumps({k: v for k, v in r.items() if k != "log"}), flush=True)
+
         res = compare(ctx, ev, a.horizon, [float(b) for b in a.betas.split(",")],
                       weights=default_weights() if a.with_mlp else None,
-                      log_cap=a.log_cap, max_attempts=a.max_attempts)
+                      log_cap=a.log_cap, max_attempts=a.max_attempts, on_result=save)
         logs = {}
         for k, r in res.items():
             lg = r.pop("log", None)

@@ -116,3 +116,63 @@ def test_in_run_check_repairs_a_far_threshold_set_too_high(ctx):
     print("after", rec)
     assert rec["checks"] == 3
     assert rec["last_err"] <= BOUND and rec["kfar"] <= first["kfar"] * (1 + 1e-6)
+
+
+def planted(n, seed):
+    """A Gaussian cloud (sigma 1 mm) whose ion 0 sits at the centre between three pairs of
+    ions at about 0.9 of the mean ion spacing on each axis, the other ions moved out of a
+    5-spacing ball around it: six strong pair terms that nearly cancel, outside the
+    close-pair radius (0.6 spacings), with a net force of 2 % of one of those terms: ion 0
+    is summed in FP32 and flagged by the conditioning test."""
+    c = configs.gaussian_cloud(configs.rng_for(seed), n, 1e-3, 300.0, np.full(n, configs.M_CS))
+    pos = c.pos.copy()
+    ctr = pos.mean(0)
+    spacing = np.cbrt((2 * np.pi) ** 1.5 * np.prod(pos.std(0)) / n)
+    r = pos - ctr
+    d = np.linalg.norm(r, axis=1)
+    inner = d < 5 * spacing
+    pos[inner] = ctr + r[inner] * ((5 * spacing + d[inner]) / d[inner])[:, None]
+    # the spacing the library's frame takes (from the moved cloud's spreads)
+    spacing = np.cbrt((2 * np.pi) ** 1.5 * np.prod(pos.std(0)) / n)
+    # ion 0 at the centre; on each axis one neighbour at -a and one at +a_ax, a_ax chosen
+    # so that the pair cancels the rest of the cloud's field there up to a net force of
+    # 2 % of one neighbour's term
+    q = c.charge.astype(np.float64)
+    a = 0.9 * spacing
+    pos[0] = ctr
+    d = ctr - pos[7:]
+    bg = (q[7:, None] * d / ((d * d).sum(1) ** 1.5)[:, None]).sum(0)
+    target = 0.02 / a ** 2 * np.ones(3) / np.sqrt(3.0)
+    for ax in range(3):
+        # field on ion 0 along ax: q/a^2 - q/a_ax^2 + bg_ax = target_ax
+        inv2 = 1.0 / a ** 2 + (bg[ax] - target[ax]) / q[1 + 2 * ax]
+        pos[1 + 2 * ax] = ctr
+        pos[1 + 2 * ax, ax] += 1.0 / np.sqrt(inv2)
+        pos[2 + 2 * ax] = ctr
+        pos[2 + 2 * ax, ax] -= a
+    return pos, q, c.mass
+
+
+@pytest.mark.parametrize("n,variant", [(300, -1), (4096, -1), (20000, -1), (20000, 9),
+                                       (65536, 14)])
+def test_flagged_ion_gets_its_exact_row(ctx, n, variant):
+    """An ion whose FP32 terms cancel keeps, after its dominant pairs alone are re-taken in
+    FP64, the rounding of the FP32 additions made while they were in its partial sums
+    (~1e-7 of its strongest term: up to ~5e-6 of its net force in the 512-cloud scan).
+    A flagged ion's sum is therefore replaced by its FP64 row: in-block for batches of up
+    to 8,192 ions, spread over 16 work units beyond; for the plain and k-d ordered shapes."""
+    pos, q, mass = planted(n, 20 + n % 7)
+    kq = kq_of(mass, q)
+    assert np.isfinite(pos).all()
+    try:
+        ctx.set_coulomb_variant(variant)
+        a32 = ctx.coulomb_accel(pos, q, kq, SG_PREC_FP32C)
+    finally:
+        ctx.set_coulomb_variant(-1)
+    a64 = ctx.coulomb_accel(pos, q, kq, SG_PREC_FP64)
+    ref = oracle.coulomb_kq_rows(pos, q, kq, 0, 1)[0]
+    e = rel_err_per_ion(a32, a64)
+    e0 = float(np.linalg.norm(a32[0] - ref) / np.linalg.norm(ref))
+    print(n, variant, "planted ion", e0, "all ions", summary(e))
+    assert e0 <= 1e-12
+    assert e.max() <= BOUND

@@ -8,9 +8,10 @@ the moments kernel (itself checked against the oracle in test_observables_gpu.py
 
 * The 512-cloud frequency scan (clouds of 64 to 8,192 ions, quadrupole drive at
   nu_c + Delta, Delta over +-5 Hz, 0.2 V, buffer gas 5e2 /s) over its full 100 us in one
-  FP32c batch, and 16 evenly spaced clouds of it in one FP64 batch: per cloud the
-  temperatures and RMS sizes agree, and the final radial temperature against Delta is
-  the scan's readout.
+  FP32c batch (the readout: final radial temperature against Delta, and the in-run
+  force check over the whole run), and 16 evenly spaced clouds of it as one batch in
+  both forms over the first 20 us (the FP64 form of the 8,035-ion cloud alone would take
+  ~15 GPU-minutes over 100 us): per cloud the temperatures and RMS sizes agree.
 * The 65,536-ion cloud (quadrupole drive at the mass-weighted nu_c, buffer gas 1e3 /s)
   over 0.3 us from the same state in both forms; the FP32c sums on the FP64 run's end
   state stay within the 1e-6 per-ion bound.
@@ -37,6 +38,7 @@ pytestmark = [pytest.mark.gpu, pytest.mark.slow,
                                  reason="long-horizon runs: set SIMGB_LONG=1")]
 
 SCAN_SUBSET = np.linspace(0, 511, 16).round().astype(int)
+SUBSET_T = 20e-6
 C2_T = 0.3e-6
 
 
@@ -93,15 +95,19 @@ def scan32():
 
 
 @pytest.fixture(scope="module")
-def scan64():
+def subset():
+    """The 16 evenly spaced clouds of the scan as one batch over SUBSET_T, in both forms."""
     w = configs.scan_512()
     sub = [int(k) for k in SCAN_SUBSET]
-    f64 = run_batch([w.clouds[k] for k in sub], [w.fields[k] for k in sub],
-                    [w.odes[k] for k in sub], SG_PREC_FP64)
-    rec = summarize("scan_fp64_subset", f64, [len(w.clouds[k].mass) for k in sub])
-    rec["clouds"] = sub
-    record("scan_fp64_subset", rec)
-    return f64
+    odes = [configs.ode(o.rtol, o.atol, o.h0, SUBSET_T) for o in (w.odes[k] for k in sub)]
+    out = {}
+    for tag, prec in (("fp32c", SG_PREC_FP32C), ("fp64", SG_PREC_FP64)):
+        r = run_batch([w.clouds[k] for k in sub], [w.fields[k] for k in sub], odes, prec)
+        rec = summarize(f"scan_subset_{tag}", r, [len(w.clouds[k].mass) for k in sub])
+        rec["clouds"] = sub
+        record(f"scan_subset_{tag}", rec)
+        out[tag] = r
+    return out
 
 
 def test_scan_runs_its_horizon(scan32):
@@ -134,10 +140,12 @@ def test_scan_readout_against_detuning(scan32):
     assert np.isfinite(tr).all() and abs(slope) * 10.0 <= 3 * tr.std()
 
 
-def test_scan_fp32c_matches_fp64_subset(scan32, scan64):
-    w, f32 = scan32
-    a = observables(f32["moments"])[SCAN_SUBSET]
-    b = observables(scan64["moments"])
+def test_scan_subset_fp32c_matches_fp64(subset):
+    """Measured: at most 1.9e-4 (RMS x), in the two clouds whose runs end 3.6 and 0.6 ns
+    apart (the loop stops at the first accepted step past t_end, and FP32c force noise
+    moves the last step sizes); the other clouds agree to <= 2.9e-6."""
+    a = observables(subset["fp32c"]["moments"])
+    b = observables(subset["fp64"]["moments"])
     r = np.abs(a - b) / np.abs(b)
     record("scan_compare", {"clouds": SCAN_SUBSET.tolist(), "rel_diff": r.tolist(),
                             "max_rel_diff_Tr_Tz_rmsxyz": r.max(0).tolist()})
@@ -159,6 +167,7 @@ def c2():
 
 
 def test_c2_observables_fp32c_vs_fp64(c2):
+    """Measured: 1.3e-8 at most, with the same 247 steps and 75 rejects in both forms."""
     c, f32, f64 = c2
     a, b = observables(f32["moments"])[0], observables(f64["moments"])[0]
     r = np.abs(a - b) / np.abs(b)
