@@ -811,6 +811,12 @@ __global__ void __launch_bounds__(NT) coulomb_fp64_kernel(const double* __restri
 // term (fixup_ion), which leaves it at the near tiles' FP32 accuracy.
 // ---------------------------------------------------------------------------
 constexpr double kKappa2 = 2.25;
+// Clouds of up to kSmallRow padded ions flag at sqrt(s2) > |P| instead: their FP64 row
+// is cheap, and with few terms per ion the error per unit of sqrt(s2)/|P| ran up to
+// ~9e-7 (an unflagged ion at 1.37 measured 1.2e-6 in the 512-cloud scan's small clouds;
+// 2.5e-7 at most on the 65,536-ion cloud).  Their flagged rows are one work unit each.
+constexpr double kKappa2Small = 1.0;
+constexpr int kSmallRow = 4096;
 // kinds of fix-up of a flagged ion
 constexpr int kFixNear = 1, kFixFar = 2;
 
@@ -1026,7 +1032,8 @@ __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
             // the far threshold: the prior of the frame set-up, or the measured one
             const double kf2 = chk ? fmin((double)cl.kfar2, (double)chk[rb.cloud].kfar2)
                                    : (double)cl.kfar2;
-            kind = (s2 > kKappa2 * pf * pf ? kFixNear : 0) | (s2f > kf2 * pf * pf ? kFixFar : 0);
+            const double kap2 = cl.npad <= kSmallRow ? kKappa2Small : kKappa2;
+            kind = (s2 > kap2 * pf * pf ? kFixNear : 0) | (s2f > kf2 * pf * pf ? kFixFar : 0);
             if (risk != nullptr) {
                 risk[i] = kind ? -1.f : (float)(sqrt(s2f) / pf);
                 risk[(size_t)n_total + i] = kind ? -1.f : (float)(sqrt(s2) / pf);
@@ -1106,6 +1113,12 @@ __global__ void __launch_bounds__(kFixupThreads, 3) coulomb_fixup_kernel(
         const int k = v % nc, c = v / nc;
         const int i = list[2 * k];
         const SgCloud& cl = clouds[list[2 * k + 1] & 0x0FFFFFFF];
+        if (row && cl.npad <= kSmallRow) {  // a small cloud's row: unit 0 alone, whole
+            if (c == 0)
+                fixup_ion<kFixupThreads>(cl, i, kFixNear, c32, c64, npad_total, out, n_total,
+                                         bbox, sh);
+            continue;
+        }
         Corr3 r{0.0, 0.0, 0.0};
         if (row)
             r = fixup_row<kFixupThreads>(cl, i, c64, npad_total, c, U, sh);
@@ -1280,9 +1293,9 @@ cudaError_t sg_launch_coulomb_reduce(const SgCoulombArgs& a, const SgRowBlock* r
         coulomb_reduce_kernel<true, false><<<n_rows, SG_ROWS, 0, s>>>(
             rows, a.clouds, a.ctrl, a.part, a.npad_total, out, n_total, counters, a.fix_list,
             nullptr, nullptr, nullptr, a.risk, a.ran, a.chk);
-        // a block per flagged ion: a fixed grid that strides over however many there are
-        // (flagged ions are a small fraction: small batches get a small grid)
-        const int grid = n_total / 256 < 1 ? 1 : (n_total / 256 > kFixupBlocks ? kFixupBlocks : n_total / 256);
+        // a fixed grid that strides over however many work units there are (a batch of
+        // small clouds can flag a few percent of its ions; unused blocks exit at once)
+        const int grid = kFixupBlocks;
         sg_launch(coulomb_fixup_kernel, grid, kFixupThreads, 0, s, 
             a.clouds, a.c32, a.c64, a.npad_total, out, n_total, a.fix_list, bbox,
             a.fix_part, a.fix_done);

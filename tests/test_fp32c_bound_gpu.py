@@ -15,7 +15,7 @@ import pytest
 
 import oracle
 from simbuca_gb300 import configs
-from simbuca_gb300.abi import SG_PREC_FP32C
+from simbuca_gb300.abi import SG_PREC_FP32C, SG_PREC_FP64
 from simbuca_gb300.api import Batch
 from helpers import kq_of, rel_err_per_ion, summary
 
