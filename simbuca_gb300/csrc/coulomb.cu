@@ -885,6 +885,8 @@ __device__ Corr3 fixup_row(const SgCloud& cl, int i, const double* __restrict__ 
     const int len = (cl.npad + nch - 1) / nch;
     const int j0 = c * len, j1 = min(cl.npad, j0 + len);
     double ax = 0.0, ay = 0.0, az = 0.0;
+    // independent pairs in flight: each one's 1/r is a chain of dependent FP64 operations
+#pragma unroll 4
     for (int j = j0 + (int)threadIdx.x; j < j1; j += NTH) {
         const int jg = cl.poff + j;
         if (jg == igk) continue;
