@@ -210,8 +210,8 @@ int sg_kernel_timing(sg_ctx* ctx, double* coulomb_ms, int64_t* coulomb_launches,
 /* The O(N) kernels of the attempts run with kernel timing on (stage combines, control,
  * commit; graph-replayed attempts only): summed milliseconds and launches. */
 int sg_stage_timing(sg_ctx* ctx, double* ms, int64_t* launches);
-/* FP32c conditioning fix-ups (ions whose dominant pairs were re-evaluated in FP64 by
- * the reduction kernel) since the last call; resets the count. */
+/* FP32c conditioning fix-ups (flagged ions: their rows re-evaluated in FP64, or their
+ * far terms corrected) since the last call; resets the count. */
 int sg_fixup_count(sg_ctx* ctx, int64_t* count);
 /* Launch shape of the FP32c Coulomb kernel for batches and calls created afterwards:
  * -1 = chosen from the cloud sizes (default), 0 = 128 threads x 4 ions,

@@ -987,12 +987,12 @@ __device__ void fixup_ion(const SgCloud& cl, int i, int kind, const float* __res
 }
 
 // Sums the j-chunk partials of each ion (x, y, z and the FP32c conditioning estimates
-// s2, s2f) into out.  FP32c: an ion whose near terms cancel strongly (sqrt(s2) > 1.5 |P|)
-// or whose far terms are large next to |P| (s2f > SgCloud::kfar2 |P|^2) is fixed up
-// (fixup_ion): INBLOCK, by this block right away (small batches, where a second launch
-// costs more than the work); otherwise it is put on the work list of
-// coulomb_fixup_kernel (ion index; cloud | kind << 28; |P| in frame units): the ions
-// with only a near fix-up in one list, those with a far one in the other.
+// s2, s2f) into out.  FP32c: an ion whose near terms cancel strongly (sqrt(s2) > 1.5 |P|,
+// > |P| in clouds of up to kSmallRow ions) or whose far terms are large next to |P|
+// (s2f > SgCloud::kfar2 |P|^2) is fixed up (fixup_ion): INBLOCK, by this block right away
+// (small batches, where a second launch costs more than the work); otherwise it is put
+// on a work list of coulomb_fixup_kernel (ion index; cloud | kind << 28): the ions whose
+// row is re-evaluated in one list, the far-only ones in the other.
 template <bool F32, bool INBLOCK>
 __global__ void __launch_bounds__(SG_ROWS) coulomb_reduce_kernel(
     const SgRowBlock* __restrict__ rows, const SgCloud* __restrict__ clouds,

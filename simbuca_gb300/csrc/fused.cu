@@ -18,7 +18,7 @@
 //     (float-float differences, SFU 1/r, 1/r^3 capped with FP64 close pairs, partial sums
 //     folded into Kahan accumulators every 16 j-ions); the G parts are added in FP64 in a
 //     fixed order, and an ion whose terms cancel strongly (sqrt(s2) > 1.5 |P|) gets its
-//     dominant pairs re-evaluated in FP64, as the tiled reduction does;
+//     whole row in FP64 instead, as the tiled reduction does;
 //   * control (CTA 0): error_succes and step() (sg_error_succes), then the commit
 //     pos <- pos2, vel <- vel2 of accepted attempts (bin/ode.cpp:488-489).
 // The cloud's coordinates, FP32 frame and SI, sit in shared memory during a Coulomb phase
@@ -41,7 +41,7 @@ namespace {
 constexpr int kThreads = SG_FUSED_THREADS;
 constexpr int kMaxIons = SG_FUSED_MAX_IONS;
 constexpr int kFlush = 16;        // j-ions per FP32 partial sum before the Kahan fold
-constexpr double kKappa2 = 2.25;  // near fix-up when s2 > 2.25 |P|^2 (the tiled reduction's)
+constexpr double kKappa2 = 2.25;  // FP64 row when s2 > 2.25 |P|^2 (the tiled reduction's for large clouds)
 
 struct FusedShared {
     double part[kThreads][3];  // per thread: its part of P x, y, z (FP64)
